@@ -1,0 +1,445 @@
+#!/usr/bin/env python
+"""Benchmark of the CKKS hot path on one GB300 (or N independent replicas under torchrun).
+
+Headline workload (BASELINE config 3b): N = 2^16, Q = 30 towers (one 60-bit + 29 x 50-bit primes, all
+= 1 mod 2^17), dnum = 3 with 10 special 60-bit primes; a batch of 64 ciphertexts at levels uniform in 1..29,
+each rotated once by an index from {+-2^k}; 32 rotation keys resident in HBM.  One step = the 64 rotations.
+`value` is HRotate ops/s with inputs resident in HBM; `e2e` is the same through the C ABI from pinned host
+buffers (H2D of every input ciphertext, D2H of every result inside the timed region).
+
+Alongside: config 3a (one ciphertext, 32 hoisted rotations) and config 2 (batched NTT -> INTT over 16
+polynomials x 40 primes at N = 2^16), whose kernel gives the roofline object.  Inputs are seeded synthetic
+residues of those shapes (random keys cost exactly what real keys cost); every working set exceeds L2.
+
+`--impl reference` times the CPU restatement of the same op (oracle/, OpenMP over towers) on this host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LOGN = 16
+N = 1 << LOGN
+S_BYTES = 8 * N
+NQ, NP, DNUM = 30, 10, 3
+ALPHA = (NQ + DNUM - 1) // DNUM
+INDICES = [s * (1 << k) for k in range(16) for s in (1, -1)]
+METRIC = "HRotate/HMult ops/s at N=2^16 (served vs per-op), p50/p99 latency, NTT % HBM BW"
+
+
+def hrotate_bytes(t: int) -> int:
+    beta = (t + ALPHA - 1) // ALPHA
+    return (2 * t + 2 * beta * (t + NP) + 2 * t) * S_BYTES
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def gen_primes_host(bits, count, two_n, exclude=()):
+    """Descending search for primes = 1 mod 2N below 2^bits (deterministic Miller-Rabin)."""
+    def is_prime(n):
+        if n < 2:
+            return False
+        for q in (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37):
+            if n % q == 0:
+                return n == q
+        d, r = n - 1, 0
+        while d % 2 == 0:
+            d //= 2
+            r += 1
+        for a in (2, 325, 9375, 28178, 450775, 9780504, 1795265022):
+            a %= n
+            if a == 0:
+                continue
+            x = pow(a, d, n)
+            if x in (1, n - 1):
+                continue
+            for _ in range(r - 1):
+                x = x * x % n
+                if x == n - 1:
+                    break
+            else:
+                return False
+        return True
+    top = (1 << bits) - 1
+    c = top - top % two_n + 1
+    if c > top:
+        c -= two_n
+    out = []
+    while len(out) < count:
+        if c not in exclude and is_prime(c):
+            out.append(c)
+        c -= two_n
+    return out
+
+
+def moduli_cfg3():
+    two_n = 2 * N
+    q0 = gen_primes_host(60, 1, two_n)
+    q = q0 + gen_primes_host(50, 29, two_n)
+    p = gen_primes_host(60, NP, two_n, exclude=set(q0))
+    return q + p
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        busy = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------------------
+
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    import torch
+
+    import fideslib_gb300 as F
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    F.lib()
+    mods = moduli_cfg3()
+    ctx = F.CryptoContext(LOGN, mods, NP, DNUM)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0x5EED0003 + rank)
+    modt = torch.tensor(mods, dtype=torch.int64, device=dev)
+
+    def rand_res(shape, tower_dim_mods):
+        x = torch.randint(0, 1 << 62, shape, dtype=torch.int64, device=dev, generator=gen)
+        return x % tower_dim_mods
+
+    # 32 rotation keys [2][dnum][ntow][N]
+    for idx in INDICES:
+        k = rand_res((2, DNUM, NQ + NP, N), modt.view(1, 1, -1, 1))
+        ctx.load_rotation_key_device(ctx.galois(idx), k.data_ptr())
+        del k
+    rng = np.random.default_rng(0x5EED0003)
+    levels = rng.integers(1, 30, 64)
+    towers = [NQ - int(l) for l in levels]
+    rot_idx = [INDICES[int(i)] for i in rng.integers(0, len(INDICES), 64)]
+    cts, handles = [], []
+    for t in towers:
+        x = rand_res((2, t, N), modt[:t].view(1, -1, 1))
+        cts.append(x)
+        handles.append(ctx.load_ciphertext_device(x.data_ptr(), t, scale=2.0 ** 50))
+    torch.cuda.synchronize()
+    op_bytes = sum(hrotate_bytes(t) for t in towers)
+
+    def step():
+        outs = [ctx.eval_rotate(h, i) for h, i in zip(handles, rot_idx)]
+        for o in outs:
+            ctx.free(o)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = F.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev.index) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = F.kernel_launches() - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    clocks = clk.summary()
+    ops_per_s = 64 * world / (ms / 1e3)
+
+    # single-op latency distribution (per-op path, one op in flight)
+    lat = []
+    for h, i in zip(handles, rot_idx):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        o = ctx.eval_rotate(h, i)
+        b.record(stream)
+        b.synchronize()
+        lat.append(a.elapsed_time(b))
+        ctx.free(o)
+    lat.sort()
+
+    # e2e: host pinned ciphertexts in, results out, through the C ABI
+    host_in = [torch.empty((2, t, N), dtype=torch.int64, pin_memory=True) for t in towers]
+    for hi, x in zip(host_in, cts):
+        hi.copy_(x.cpu())
+    host_out = [torch.empty_like(hi) for hi in host_in]
+    h2d = sum(hi.numel() * 8 for hi in host_in)
+
+    def e2e_step():
+        for hi, ho, i, t in zip(host_in, host_out, rot_idx, towers):
+            h = ctx.load_ciphertext(hi.numpy().view(np.uint64), scale=2.0 ** 50)
+            o = ctx.eval_rotate(h, i)
+            ctx.store_ciphertext(o, ho.numpy().view(np.uint64))
+            ctx.free(h)
+            ctx.free(o)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # config 3a: one ciphertext at 30 towers, 32 hoisted rotations
+    x30 = rand_res((2, NQ, N), modt[:NQ].view(1, -1, 1))
+    h30 = ctx.load_ciphertext_device(x30.data_ptr(), NQ)
+    for _ in range(2):
+        for o in ctx.eval_fast_rotation(h30, INDICES):
+            ctx.free(o)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    reps = 3
+    for _ in range(reps):
+        for o in ctx.eval_fast_rotation(h30, INDICES):
+            ctx.free(o)
+    b.record(stream)
+    b.synchronize()
+    hoisted_ms = a.elapsed_time(b) / reps
+
+    # config 2: batched NTT -> INTT, 16 polys x 40 primes, kernel roofline
+    ntt = ntt_bench(args, dev, stream)
+    peak, peak_kind = peaks()
+    achieved = op_bytes / (ms / 1e3) / 1e9
+    result = {
+        "metric": METRIC,
+        "value": round(ops_per_s, 2),
+        "unit": "HRotate ops/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic (seeded uniform residues; random keys of the real shape)",
+        "config": {"workload": "cfg3b: 64 ciphertexts at levels U{1..29}, one HRotate each (per-op path)",
+                   "N": N, "towers_q": NQ, "special": NP, "dnum": DNUM, "batch": 64,
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (keys 3.8 GiB, cts ~1 GiB)"},
+        "e2e": {"value": round(64 * world / (e2e_ms / 1e3), 2), "unit": "HRotate ops/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+        "gpu_launches": int(launches),
+        "hrotate": {"achieved_gbs": round(achieved, 1), "frac_of_hbm": round(achieved / peak, 4),
+                    "algorithmic_bytes_per_step": op_bytes,
+                    "latency_ms_p50": round(lat[len(lat) // 2], 4),
+                    "latency_ms_p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4)},
+        "hoisted_cfg3a": {"ms_for_32_rotations": round(hoisted_ms, 4),
+                          "ops_per_s": round(32 / (hoisted_ms / 1e3), 2)},
+        "ntt_cfg2": ntt["summary"],
+        "roofline": ntt["roofline"],
+        "clocks": clocks,
+    }
+    return result
+
+
+def ntt_bench(args, dev, stream):
+    import torch
+
+    import fideslib_gb300 as F
+    mods = gen_primes_host(60, 41, 2 * N)
+    ctx = F.CryptoContext(LOGN, mods, 1, 1)
+    ctx.set_stream(stream.cuda_stream)
+    modt = torch.tensor(mods[:40], dtype=torch.int64, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(0x5EED0002)
+    data = torch.randint(0, 1 << 62, (16, 40, N), dtype=torch.int64, device=dev, generator=g) % modt.view(1, -1, 1)
+    ptr = data.data_ptr()
+    for _ in range(max(3, args.warmup)):
+        ctx.ntt_device(ptr, 16, 40, 0, False, stream.cuda_stream)
+        ctx.ntt_device(ptr, 16, 40, 0, True, stream.cuda_stream)
+    torch.cuda.synchronize()
+    reps = max(5, args.steps)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps + 1)]
+    ev[0].record(stream)
+    for r in range(reps):
+        ctx.ntt_device(ptr, 16, 40, 0, False, stream.cuda_stream)
+        ev[2 * r + 1].record(stream)
+        ctx.ntt_device(ptr, 16, 40, 0, True, stream.cuda_stream)
+        ev[2 * r + 2].record(stream)
+    torch.cuda.synchronize()
+    fwd = [ev[2 * r].elapsed_time(ev[2 * r + 1]) for r in range(reps)]
+    inv = [ev[2 * r + 1].elapsed_time(ev[2 * r + 2]) for r in range(reps)]
+    ctx.set_stream(None)
+    algo = 640 * 2 * S_BYTES  # one read + one write per limb
+    peak, kind = peaks()
+    f_ms, i_ms = statistics.mean(fwd), statistics.mean(inv)
+    ach = algo / (f_ms / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "ntt_fwd_traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("bytes_per_launch")
+    return {
+        "summary": {"ms_ntt": round(f_ms, 4), "ms_intt": round(i_ms, 4),
+                    "ntt_gbs": round(ach, 1), "intt_gbs": round(algo / (i_ms / 1e3) / 1e9, 1),
+                    "ntt_frac_of_hbm": round(ach / peak, 4),
+                    "limbs_per_launch": 640, "algorithmic_bytes_per_launch": algo},
+        "roofline": {"kernel": "ntt_fwd_kernel<16> (config 2: 16 polys x 40 primes, N=2^16)",
+                     "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "peak_kind": f"{kind} burst copy",
+                     "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": traffic},
+    }
+
+
+# ------------------------------------------------------------------------------------------------------------
+# CPU arm: the oracle restatement (the reference's CPU path for these ops lives in OpenFHE, absent here)
+# ------------------------------------------------------------------------------------------------------------
+
+def cpu_rotations(n_ops: int, threads: int, seed: int):
+    import numpy as np
+
+    import oracle as O
+    mods = moduli_cfg3()
+    orc = O.Ctx(N, NQ, NP, DNUM, mods, threads=threads)
+    rng = np.random.default_rng(seed)
+    key = np.zeros(orc.key_shape(), dtype=np.uint64)
+    for i in range(NQ + NP):
+        key[:, :, i] = rng.integers(0, mods[i], (2, DNUM, N), dtype=np.uint64)
+    t_total = 0.0
+    for _ in range(n_ops):
+        t = NQ - int(rng.integers(1, 30))
+        ct = np.stack([np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(t)]) for _ in range(2)])
+        g = orc.galois(INDICES[int(rng.integers(0, len(INDICES)))])
+        t0 = time.perf_counter()
+        orc.rotate(ct, g, key)
+        t_total += time.perf_counter() - t0
+    return n_ops / t_total
+
+
+def run_reference(args):
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_rotations(1, threads, 7)
+    vals = []
+    for s in range(args.steps):
+        vals.append(cpu_rotations(2, threads, 100 + s))
+    v = statistics.mean(vals)
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "HRotate ops/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(2e3 / v, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "cfg3b: ciphertexts at levels U{1..29}, one HRotate each", "N": N,
+                   "towers_q": NQ, "special": NP, "dnum": DNUM},
+        "cpu_baseline": {"value": round(v, 4), "unit": "HRotate ops/s", "cores": threads, "kind": "port",
+                         "sample": f"{2 * args.steps} rotations at seeded levels U{{1..29}} (OpenMP over towers)"},
+        "e2e": {"value": round(v, 4), "unit": "HRotate ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as D
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        D.init_process_group("nccl")
+        dist = D
+    res = run_ours(args, rank, world, dist)
+    if rank == 0:
+        if world == 1 and not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            v = cpu_rotations(4, threads, 42)
+            res["cpu_baseline"] = {"value": round(v, 4), "unit": "HRotate ops/s", "cores": threads, "kind": "port",
+                                   "sample": "4 rotations at seeded levels U{1..29}, oracle (OpenMP over towers)"}
+        print(json.dumps(res), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,254 @@
+"""fideslib_gb300 — GB300-native CKKS evaluation engine (Python binding over the C ABI).
+
+The engine itself is CUDA/C++ (fideslib_gb300/csrc) behind the C ABI declared in include/fideslib_gb300.h;
+this module is a thin ctypes binding used by the tests and the benchmark.  It never falls back to a CPU
+path: if the compiled library is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libfideslib_gb300.so")
+HEADER = os.path.join(HERE, "..", "include", "fideslib_gb300.h")
+
+FIDES_OK, FIDES_EINVAL, FIDES_ENOKEY, FIDES_ENOMEM, FIDES_ECUDA, FIDES_ENODEV = 0, -1, -2, -3, -4, -5
+FIXEDMANUAL, FIXEDAUTO, FLEXIBLEAUTO, FLEXIBLEAUTOEXT = 0, 1, 2, 3
+
+u64p = C.POINTER(C.c_uint64)
+u32p = C.POINTER(C.c_uint32)
+i32p = C.POINTER(C.c_int32)
+
+
+class FidesError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("log_n", C.c_uint32), ("nq", C.c_uint32), ("np", C.c_uint32), ("dnum", C.c_uint32),
+                ("moduli", u64p), ("roots", u64p), ("scaling_technique", C.c_int32)]
+
+
+class CtMeta(C.Structure):
+    _fields_ = [("towers", C.c_uint32), ("noise_deg", C.c_uint32), ("slots", C.c_uint32),
+                ("reserved", C.c_uint32), ("scale", C.c_double)]
+
+
+_lib = None
+
+_SIGS = {
+    "fides_last_error": (C.c_char_p, []),
+    "fides_version": (C.c_char_p, []),
+    "fides_ctx_create": (C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
+    "fides_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "fides_ctx_moduli": (C.c_int, [C.c_void_p, u64p, u64p]),
+    "fides_galois_element": (C.c_uint32, [C.c_void_p, C.c_int32]),
+    "fides_synchronize": (C.c_int, [C.c_void_p]),
+    "fides_ctx_stream": (C.c_void_p, [C.c_void_p]),
+    "fides_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fides_kernel_launches": (C.c_uint64, []),
+    "fides_ntt_batch_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int,
+                                         C.c_void_p]),
+    "fides_ntt_batch_host": (C.c_int, [C.c_void_p, u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
+    "fides_load_eval_mult_key": (C.c_int, [C.c_void_p, u64p]),
+    "fides_load_rotation_key": (C.c_int, [C.c_void_p, C.c_uint32, u64p]),
+    "fides_load_rotation_key_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "fides_ct_load": (C.c_int, [C.c_void_p, u64p, C.POINTER(CtMeta), u32p]),
+    "fides_ct_load_device": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CtMeta), u32p]),
+    "fides_ct_store": (C.c_int, [C.c_void_p, C.c_uint32, u64p, C.POINTER(CtMeta)]),
+    "fides_ct_meta_get": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(CtMeta)]),
+    "fides_ct_free": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fides_eval_add": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_sub": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_mult": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_square": (C.c_int, [C.c_void_p, C.c_uint32, u32p]),
+    "fides_rescale": (C.c_int, [C.c_void_p, C.c_uint32, u32p]),
+    "fides_eval_rotate": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int32, u32p]),
+    "fides_eval_automorphism": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_fast_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, i32p, u32p]),
+}
+
+
+def lib():
+    """Loads the compiled engine; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"fideslib_gb300 CUDA library missing ({LIB_PATH}); "
+                               "build it with `python -m fideslib_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/fideslib_gb300.h."""
+    import re
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(fides_\w+)\s*\(", src, re.M)))
+
+
+def _check(rc: int):
+    if rc != FIDES_OK:
+        raise FidesError(rc, lib().fides_last_error().decode())
+
+
+def _p(a: np.ndarray, t=u64p):
+    return a.ctypes.data_as(t)
+
+
+class CryptoContext:
+    """Device context: moduli, roots and all derived tables resident on the GPU (LoadContext)."""
+
+    def __init__(self, log_n: int, moduli, np_: int, dnum: int, roots=None, scaling_technique: int = FIXEDMANUAL):
+        moduli = np.ascontiguousarray(np.array(moduli, dtype=np.uint64))
+        self.N = 1 << log_n
+        self.log_n = log_n
+        self.np = np_
+        self.nq = len(moduli) - np_
+        self.dnum = dnum
+        self.alpha = (self.nq + dnum - 1) // dnum
+        r = None if roots is None else np.ascontiguousarray(np.array(roots, dtype=np.uint64))
+        prm = Params(log_n, self.nq, np_, dnum, _p(moduli), None if r is None else _p(r), scaling_technique)
+        h = C.c_void_p()
+        _check(lib().fides_ctx_create(C.byref(prm), C.byref(h)))
+        self._h = h
+        m = np.zeros(self.nq + np_, dtype=np.uint64)
+        rr = np.zeros(self.nq + np_, dtype=np.uint64)
+        _check(lib().fides_ctx_moduli(self._h, _p(m), _p(rr)))
+        self.moduli = [int(x) for x in m]
+        self.roots = [int(x) for x in rr]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fides_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- primitives ---
+    def galois(self, index: int) -> int:
+        return int(lib().fides_galois_element(self._h, index))
+
+    def synchronize(self):
+        _check(lib().fides_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(lib().fides_ctx_stream(self._h) or 0)
+
+    def set_stream(self, stream: int | None):
+        _check(lib().fides_ctx_set_stream(self._h, None if not stream else C.c_void_p(stream)))
+
+
+    def ntt_host(self, data: np.ndarray, first_prime: int = 0, inverse: bool = False) -> np.ndarray:
+        """data: u64[npolys][limbs][N] (host), transformed in place and returned."""
+        assert data.dtype == np.uint64 and data.flags.c_contiguous and data.ndim == 3
+        _check(lib().fides_ntt_batch_host(self._h, _p(data), data.shape[0], data.shape[1], first_prime,
+                                          1 if inverse else 0))
+        return data
+
+    def ntt_device(self, ptr: int, npolys: int, limbs: int, first_prime: int = 0, inverse: bool = False,
+                   stream: int | None = None):
+        _check(lib().fides_ntt_batch_device(self._h, C.c_void_p(ptr), npolys, limbs, first_prime,
+                                            1 if inverse else 0, None if stream is None else C.c_void_p(stream)))
+
+    # --- keys ---
+    def load_eval_mult_key(self, key: np.ndarray):
+        key = np.ascontiguousarray(key, dtype=np.uint64)
+        _check(lib().fides_load_eval_mult_key(self._h, _p(key)))
+
+    def load_rotation_key(self, galois: int, key: np.ndarray):
+        key = np.ascontiguousarray(key, dtype=np.uint64)
+        _check(lib().fides_load_rotation_key(self._h, galois, _p(key)))
+
+    def load_rotation_key_device(self, galois: int, ptr: int):
+        _check(lib().fides_load_rotation_key_device(self._h, galois, C.c_void_p(ptr)))
+
+    # --- ciphertexts ---
+    def load_ciphertext(self, ct: np.ndarray, scale: float = 1.0, noise_deg: int = 1, slots: int = 0) -> int:
+        ct = np.ascontiguousarray(ct, dtype=np.uint64)
+        assert ct.ndim == 3 and ct.shape[0] == 2 and ct.shape[2] == self.N
+        meta = CtMeta(ct.shape[1], noise_deg, slots, 0, scale)
+        h = C.c_uint32()
+        _check(lib().fides_ct_load(self._h, _p(ct), C.byref(meta), C.byref(h)))
+        return h.value
+
+    def load_ciphertext_device(self, ptr: int, towers: int, scale: float = 1.0, noise_deg: int = 1,
+                               slots: int = 0) -> int:
+        meta = CtMeta(towers, noise_deg, slots, 0, scale)
+        h = C.c_uint32()
+        _check(lib().fides_ct_load_device(self._h, C.c_void_p(ptr), C.byref(meta), C.byref(h)))
+        return h.value
+
+    def meta(self, h: int) -> CtMeta:
+        m = CtMeta()
+        _check(lib().fides_ct_meta_get(self._h, h, C.byref(m)))
+        return m
+
+    def store_ciphertext(self, h: int, out: np.ndarray | None = None) -> np.ndarray:
+        m = self.meta(h)
+        if out is None:
+            out = np.empty((2, m.towers, self.N), dtype=np.uint64)
+        _check(lib().fides_ct_store(self._h, h, _p(out), None))
+        return out
+
+    def free(self, h: int):
+        _check(lib().fides_ct_free(self._h, h))
+
+    # --- evaluation ---
+    def _bin(self, fn, a, b) -> int:
+        o = C.c_uint32()
+        _check(fn(self._h, a, b, C.byref(o)))
+        return o.value
+
+    def eval_add(self, a: int, b: int) -> int:
+        return self._bin(lib().fides_eval_add, a, b)
+
+    def eval_sub(self, a: int, b: int) -> int:
+        return self._bin(lib().fides_eval_sub, a, b)
+
+    def eval_mult(self, a: int, b: int) -> int:
+        return self._bin(lib().fides_eval_mult, a, b)
+
+    def eval_square(self, a: int) -> int:
+        o = C.c_uint32()
+        _check(lib().fides_eval_square(self._h, a, C.byref(o)))
+        return o.value
+
+    def rescale(self, a: int) -> int:
+        o = C.c_uint32()
+        _check(lib().fides_rescale(self._h, a, C.byref(o)))
+        return o.value
+
+    def eval_rotate(self, a: int, index: int) -> int:
+        return self._bin(lib().fides_eval_rotate, a, index)
+
+    def eval_automorphism(self, a: int, galois: int) -> int:
+        return self._bin(lib().fides_eval_automorphism, a, galois)
+
+    def eval_fast_rotation(self, a: int, indices) -> list[int]:
+        idx = np.ascontiguousarray(np.array(indices, dtype=np.int32))
+        outs = np.zeros(len(idx), dtype=np.uint32)
+        _check(lib().fides_eval_fast_rotation(self._h, a, len(idx), _p(idx, i32p), _p(outs, u32p)))
+        return [int(x) for x in outs]
+
+
+def kernel_launches() -> int:
+    """Engine kernels launched by this process so far."""
+    return int(lib().fides_kernel_launches())

@@ -1,0 +1,346 @@
+// extern "C" boundary of the engine (declarations and contract: include/fideslib_gb300.h).
+#include <cstring>
+#include <string>
+
+#include "../../include/fideslib_gb300.h"
+#include "engine.hpp"
+
+struct fides_ctx {
+  fgb::Context* c;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? FIDES_ENOMEM : FIDES_ECUDA;
+}
+
+#define CK(call, where)                            \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+  } while (0)
+
+fgb::DevCt* find_ct(fides_ctx* ctx, uint32_t h) {
+  auto it = ctx->c->cts.find(h);
+  return it == ctx->c->cts.end() ? nullptr : &it->second;
+}
+
+uint32_t register_ct(fides_ctx* ctx, const fgb::DevCt& ct) {
+  uint32_t h = ctx->c->next_handle++;
+  if (ctx->c->next_handle == 0) ctx->c->next_handle = 1;
+  ctx->c->cts[h] = ct;
+  return h;
+}
+
+int new_ct(fides_ctx* ctx, int t, const fgb::DevCt& like, fgb::DevCt* out) {
+  *out = like;
+  out->t = t;
+  out->data = ctx->c->alloc_limbs((size_t)2 * t, ctx->c->stream);
+  if (!out->data) return fail(FIDES_ENOMEM, "ciphertext allocation failed");
+  return FIDES_OK;
+}
+
+bool valid_ctx(fides_ctx* ctx) { return ctx && ctx->c; }
+
+// The ModUp kernel keeps one digit's towers in registers: at most 32 towers per digit.
+int check_ks_shape(fides_ctx* ctx) {
+  if (ctx->c->alpha > 32) return fail(FIDES_EINVAL, "key switching supports at most 32 towers per digit (raise dnum)");
+  return FIDES_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fides_last_error(void) { return g_err.c_str(); }
+const char* fides_version(void) { return "fideslib_gb300 0.1 (sm_103a)"; }
+
+int fides_ctx_create(const fides_params* p, fides_ctx** out) {
+  if (!p || !out || !p->moduli) return fail(FIDES_EINVAL, "null argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(FIDES_ENODEV, "no CUDA device");
+  std::string err;
+  fgb::Context* c = fgb::Context::create((int)p->log_n, (int)p->nq, (int)p->np, (int)p->dnum, (const fgb::u64*)p->moduli,
+                                                (const fgb::u64*)p->roots, &err);
+  if (!c) return fail(FIDES_EINVAL, err);
+  *out = new fides_ctx{c};
+  return FIDES_OK;
+}
+
+int fides_ctx_destroy(fides_ctx* ctx) {
+  if (!ctx) return FIDES_OK;
+  delete ctx->c;
+  delete ctx;
+  return FIDES_OK;
+}
+
+int fides_ctx_moduli(const fides_ctx* ctx, uint64_t* moduli, uint64_t* roots) {
+  if (!ctx || !ctx->c) return fail(FIDES_EINVAL, "null context");
+  const fgb::Context* c = ctx->c;
+  for (int i = 0; i < c->ntow; i++) {
+    if (moduli) moduli[i] = c->mod[i];
+    if (roots) roots[i] = c->psi[i];
+  }
+  return FIDES_OK;
+}
+
+uint32_t fides_galois_element(const fides_ctx* ctx, int32_t index) {
+  if (!ctx || !ctx->c) return 0;
+  return fgb::Context::galois_for_index(ctx->c->N, index);
+}
+
+int fides_synchronize(fides_ctx* ctx) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  CK(cudaStreamSynchronize(ctx->c->stream), "synchronize");
+  return FIDES_OK;
+}
+
+void* fides_ctx_stream(fides_ctx* ctx) { return valid_ctx(ctx) ? (void*)ctx->c->stream : nullptr; }
+
+int fides_ctx_set_stream(fides_ctx* ctx, void* stream) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  fgb::Context* c = ctx->c;
+  CK(cudaStreamSynchronize(c->stream), "set stream");
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return FIDES_OK;
+}
+
+uint64_t fides_kernel_launches(void) { return fgb::launch_count(); }
+
+int fides_ntt_batch_device(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint32_t limbs, uint32_t first_prime,
+                           int inverse, void* stream) {
+  if (!valid_ctx(ctx) || !data) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  if (limbs == 0 || npolys == 0) return FIDES_OK;
+  if (limbs > 64 || first_prime + limbs > (uint32_t)c->ntow) return fail(FIDES_EINVAL, "tower range out of bounds");
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  CK(c->ntt((fgb::u64*)data, (int)npolys, (int)limbs, (int)first_prime, (long long)limbs * c->N, inverse != 0, s),
+     "ntt launch");
+  return FIDES_OK;
+}
+
+int fides_ntt_batch_host(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint32_t limbs, uint32_t first_prime,
+                         int inverse) {
+  if (!valid_ctx(ctx) || !data) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  const size_t bytes = (size_t)npolys * limbs * c->N * sizeof(uint64_t);
+  if (bytes == 0) return FIDES_OK;
+  fgb::u64* d = c->alloc_limbs((size_t)npolys * limbs, c->stream);
+  if (!d) return fail(FIDES_ENOMEM, "device allocation failed");
+  CK(cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, c->stream), "H2D");
+  int rc = fides_ntt_batch_device(ctx, (uint64_t*)d, npolys, limbs, first_prime, inverse, c->stream);
+  if (rc == FIDES_OK) {
+    CK(cudaMemcpyAsync(data, d, bytes, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  }
+  c->free_limbs(d, c->stream);
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return rc;
+}
+
+static int load_key(fides_ctx* ctx, const uint64_t* key, bool device, fgb::u64** slot) {
+  fgb::Context* c = ctx->c;
+  const size_t bytes = (size_t)2 * c->dnum * c->ntow * c->N * sizeof(uint64_t);
+  if (!*slot) {
+    void* p = nullptr;
+    CK(cudaMalloc(&p, bytes), "key allocation");
+    *slot = (fgb::u64*)p;
+  }
+  CK(cudaMemcpyAsync(*slot, key, bytes, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
+     "key copy");
+  CK(cudaStreamSynchronize(c->stream), "key copy");
+  return FIDES_OK;
+}
+
+int fides_load_eval_mult_key(fides_ctx* ctx, const uint64_t* key) {
+  if (!valid_ctx(ctx) || !key) return fail(FIDES_EINVAL, "null argument");
+  return load_key(ctx, key, false, &ctx->c->relin_key);
+}
+
+int fides_load_rotation_key(fides_ctx* ctx, uint32_t galois, const uint64_t* key) {
+  if (!valid_ctx(ctx) || !key) return fail(FIDES_EINVAL, "null argument");
+  if ((galois & 1) == 0 || galois >= 2u * ctx->c->N) return fail(FIDES_EINVAL, "Galois element must be odd and < 2N");
+  fgb::u64*& slot = ctx->c->rot_keys[galois];
+  return load_key(ctx, key, false, &slot);
+}
+
+int fides_load_rotation_key_device(fides_ctx* ctx, uint32_t galois, const uint64_t* dev_key) {
+  if (!valid_ctx(ctx) || !dev_key) return fail(FIDES_EINVAL, "null argument");
+  if ((galois & 1) == 0 || galois >= 2u * ctx->c->N) return fail(FIDES_EINVAL, "Galois element must be odd and < 2N");
+  fgb::u64*& slot = ctx->c->rot_keys[galois];
+  return load_key(ctx, dev_key, true, &slot);
+}
+
+static int ct_load_impl(fides_ctx* ctx, const uint64_t* data, const fides_ct_meta* meta, uint32_t* handle,
+                        bool device) {
+  if (!valid_ctx(ctx) || !data || !meta || !handle) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  if (meta->towers < 1 || meta->towers > (uint32_t)c->nq) return fail(FIDES_EINVAL, "towers out of range");
+  fgb::DevCt ct;
+  ct.t = (int)meta->towers;
+  ct.scale = meta->scale;
+  ct.noise_deg = (int)meta->noise_deg;
+  ct.slots = (int)meta->slots;
+  ct.data = c->alloc_limbs((size_t)2 * ct.t, c->stream);
+  if (!ct.data) return fail(FIDES_ENOMEM, "ciphertext allocation failed");
+  CK(cudaMemcpyAsync(ct.data, data, (size_t)2 * ct.t * c->N * sizeof(uint64_t),
+                     device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
+     "ciphertext copy");
+  *handle = register_ct(ctx, ct);
+  return FIDES_OK;
+}
+
+int fides_ct_load(fides_ctx* ctx, const uint64_t* data, const fides_ct_meta* meta, uint32_t* handle) {
+  return ct_load_impl(ctx, data, meta, handle, false);
+}
+
+int fides_ct_load_device(fides_ctx* ctx, const uint64_t* dev_data, const fides_ct_meta* meta, uint32_t* handle) {
+  return ct_load_impl(ctx, dev_data, meta, handle, true);
+}
+
+int fides_ct_meta_get(fides_ctx* ctx, uint32_t handle, fides_ct_meta* meta) {
+  if (!valid_ctx(ctx) || !meta) return fail(FIDES_EINVAL, "null argument");
+  fgb::DevCt* ct = find_ct(ctx, handle);
+  if (!ct) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  meta->towers = (uint32_t)ct->t;
+  meta->noise_deg = (uint32_t)ct->noise_deg;
+  meta->slots = (uint32_t)ct->slots;
+  meta->reserved = 0;
+  meta->scale = ct->scale;
+  return FIDES_OK;
+}
+
+int fides_ct_store(fides_ctx* ctx, uint32_t handle, uint64_t* data, fides_ct_meta* meta) {
+  if (!valid_ctx(ctx) || !data) return fail(FIDES_EINVAL, "null argument");
+  fgb::DevCt* ct = find_ct(ctx, handle);
+  if (!ct) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  fgb::Context* c = ctx->c;
+  CK(cudaMemcpyAsync(data, ct->data, (size_t)2 * ct->t * c->N * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                     c->stream),
+     "ciphertext store");
+  CK(cudaStreamSynchronize(c->stream), "ciphertext store");
+  if (meta) return fides_ct_meta_get(ctx, handle, meta);
+  return FIDES_OK;
+}
+
+int fides_ct_free(fides_ctx* ctx, uint32_t handle) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  auto it = ctx->c->cts.find(handle);
+  if (it == ctx->c->cts.end()) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  ctx->c->free_limbs(it->second.data, ctx->c->stream);
+  ctx->c->cts.erase(it);
+  return FIDES_OK;
+}
+
+static int binary_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out, bool sub) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::DevCt *A = find_ct(ctx, a), *B = find_ct(ctx, b);
+  if (!A || !B) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, *A, &r);
+  if (rc) return rc;
+  r.noise_deg = A->noise_deg > B->noise_deg ? A->noise_deg : B->noise_deg;
+  CK(fgb::launch_addsub(A->data, B->data, r.data, 2, A->t, ctx->c->N, sub, ctx->c->d_pc, ctx->c->stream), "add");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_eval_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return binary_add(ctx, a, b, out, false); }
+int fides_eval_sub(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return binary_add(ctx, a, b, out, true); }
+
+int fides_eval_mult(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt *A = find_ct(ctx, a), *B = find_ct(ctx, b);
+  if (!A || !B) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
+  if (!c->relin_key) return fail(FIDES_ENOKEY, "no relinearisation key loaded");
+  if (int rc0 = check_ks_shape(ctx)) return rc0;
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, *A, &r);
+  if (rc) return rc;
+  r.noise_deg = A->noise_deg + B->noise_deg;
+  r.scale = A->scale * B->scale;
+  CK(c->mult(A->data, B->data, A->t, c->relin_key, r.data, c->stream), "mult");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_eval_square(fides_ctx* ctx, uint32_t a, uint32_t* out) { return fides_eval_mult(ctx, a, a, out); }
+
+int fides_rescale(fides_ctx* ctx, uint32_t a, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  if (A->t < 2) return fail(FIDES_EINVAL, "cannot rescale a ciphertext with one tower");
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t - 1, *A, &r);
+  if (rc) return rc;
+  r.noise_deg = A->noise_deg > 1 ? A->noise_deg - 1 : 1;
+  r.scale = A->scale / (double)c->mod[A->t - 1];
+  CK(c->rescale(A->data, A->t, r.data, c->stream), "rescale");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  auto it = c->rot_keys.find(galois);
+  if (it == c->rot_keys.end()) return fail(FIDES_ENOKEY, "no rotation key for Galois element " + std::to_string(galois));
+  if (int rc0 = check_ks_shape(ctx)) return rc0;
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, *A, &r);
+  if (rc) return rc;
+  CK(c->rotate(A->data, A->t, galois, it->second, r.data, c->stream), "rotate");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_eval_rotate(fides_ctx* ctx, uint32_t a, int32_t index, uint32_t* out) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  return fides_eval_automorphism(ctx, a, fgb::Context::galois_for_index(ctx->c->N, index), out);
+}
+
+int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs) {
+  if (!valid_ctx(ctx) || (n && (!indices || !outs))) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  std::vector<fgb::u64*> keys(n);
+  std::vector<uint32_t> gal(n);
+  for (uint32_t r = 0; r < n; r++) {
+    gal[r] = fgb::Context::galois_for_index(c->N, indices[r]);
+    auto it = c->rot_keys.find(gal[r]);
+    if (it == c->rot_keys.end())
+      return fail(FIDES_ENOKEY, "no rotation key for index " + std::to_string(indices[r]));
+    keys[r] = it->second;
+  }
+  if (int rc0 = check_ks_shape(ctx)) return rc0;
+  const int t = A->t;
+  const size_t P = (size_t)t * c->N;
+  CK(c->modup(A->data + P, t, c->stream), "modup");
+  for (uint32_t r = 0; r < n; r++) {
+    fgb::DevCt res;
+    int rc = new_ct(ctx, t, *A, &res);
+    if (rc) return rc;
+    CK(c->ks_from_digits(A->data + P, t, keys[r], A->data, nullptr, res.data, c->galois_inverse(gal[r]), c->stream),
+       "hoisted rotate");
+    outs[r] = register_ct(ctx, res);
+    A = find_ct(ctx, a);  // registry may have rehashed
+  }
+  return FIDES_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Host-side CKKS evaluation engine: context tables, device-resident ciphertexts and keys, op pipelines.
+//
+// Reference counterparts: FIDESlib::CKKS::ContextData (src/CKKS/Context.cuh:47-184), SetupConstants
+// (src/ConstantsGPU.cu:125-697), Ciphertext::mult/rotate/rotate_hoisted/rescale (src/CKKS/Ciphertext.cpp)
+// and LimbPartition::modup_ksk_moddown_mgpu (src/CKKS/LimbPartitionMGPU.cu:588-1870, single-GPU branch).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "arith.cuh"
+#include "kernels.cuh"
+#include "ntt.cuh"
+
+namespace fgb {
+
+struct DevCt {
+  u64* data = nullptr;  // [2][t][N]
+  int t = 0;            // active Q towers
+  double scale = 0.0;   // scaling factor (RawCipherText::Noise)
+  int noise_deg = 1;    // RawCipherText::NoiseLevel
+  int slots = 0;
+};
+
+class Context {
+ public:
+  ~Context();
+  // Creates tables on the current device.  `roots` may be null (generated as g^((p-1)/2N), smallest
+  // generator g).  Returns an error string on failure.
+  static Context* create(int logN, int nq, int np, int dnum, const u64* moduli, const u64* roots, std::string* err);
+
+  int N = 0, logN = 0, nq = 0, np = 0, dnum = 0, alpha = 0, ntow = 0;
+  std::vector<u64> mod, psi;
+  cudaStream_t stream = nullptr;      // stream all work is ordered on
+  cudaStream_t own_stream = nullptr;  // the context's own stream
+
+  DeviceTables tabs{};
+  CrtTables crt{};
+  PrimeConst* d_pc = nullptr;
+
+  // --- primitives on device memory ---
+  cudaError_t ntt(u64* data, int npolys, int limbs, int first_prime, long long poly_stride, bool inverse,
+                  cudaStream_t s);
+
+  // Key switch of a (evaluation form, t towers) with `key` ([2][dnum][ntow][N] device).  The results
+  // (ModDown(sum D b) + add0, ModDown(sum D a) + add1) are written to out [2][t][N], permuted by the
+  // automorphism whose inverse Galois element is galois_inv (1 = none).  `out` must not alias the inputs.
+  cudaError_t keyswitch(const u64* a, int t, const u64* key, const u64* add0, const u64* add1, u64* out,
+                        uint32_t galois_inv, cudaStream_t s);
+  // ModUp only (fills the conversion workspace for `t` towers of a); then per key the inner product and ModDown.
+  cudaError_t modup(const u64* a, int t, cudaStream_t s);
+  cudaError_t ks_from_digits(const u64* a, int t, const u64* key, const u64* add0, const u64* add1, u64* out,
+                             uint32_t galois_inv, cudaStream_t s);
+
+  cudaError_t mult(const u64* x, const u64* y, int t, const u64* rlk, u64* out, cudaStream_t s);
+  cudaError_t rescale(const u64* x, int t, u64* out, cudaStream_t s);
+  cudaError_t rotate(const u64* x, int t, uint32_t galois, const u64* key, u64* out, cudaStream_t s);
+
+  // --- object registry (handles as in api/CryptoContext.hpp:233-246) ---
+  std::mutex mu;
+  std::unordered_map<uint32_t, DevCt> cts;
+  uint32_t next_handle = 1;
+  std::map<uint32_t, u64*> rot_keys;  // Galois element -> key
+  u64* relin_key = nullptr;
+
+  u64* alloc_limbs(size_t nlimbs, cudaStream_t s);
+  void free_limbs(u64* p, cudaStream_t s);
+
+  uint32_t galois_inverse(uint32_t g) const;
+  static uint32_t galois_for_index(int N, int32_t index);
+
+ private:
+  Context() = default;
+  bool build(const u64* roots, std::string* err);
+  std::vector<void*> owned_;  // device allocations freed at destruction
+  void* dmalloc(size_t bytes);
+
+  // workspace sized for t = nq
+  u64* ws_coeff_ = nullptr;  // [nq][N]
+  u64* ws_conv_ = nullptr;   // [dnum][ntow][N]
+  u64* ws_inner_ = nullptr;  // [2][ntow][N]
+  u64* ws_md_ = nullptr;     // [2][nq][N]
+  u64* ws_tensor_ = nullptr; // [3][nq][N]
+  u64* ws_top_ = nullptr;    // [2][N]
+  u64* ws_rs_ = nullptr;     // [2][nq][N]
+  int digits_t_ = 0;         // t of the digits currently held by ws_conv_
+};
+
+}  // namespace fgb

@@ -1,0 +1,338 @@
+// Batched 64-bit negacyclic NTT / INTT, one HBM read and one HBM write per limb.
+//
+// Reference counterpart: src/NTT.cu:331-769 (NTT_/INTT_, a two-kernel four-step transform with 10 KiB of
+// shared memory per 128-thread CTA, i.e. two HBM round trips per limb).  Here one limb of N = 2^16 residues
+// (512 KiB) is held by a thread-block cluster of C = N/8192 CTAs, 64 KiB of shared memory each:
+//   forward (Cooley–Tukey, natural -> bit-reversed, twiddle table index m+i as in OpenFHE's
+//   ForwardTransformToBitReverse, test/cpuNTT_nega.cpp:38-85):
+//     phase X : the log2(C) stages that pair residues held by different CTAs.  CTA c loads the columns
+//               l in [c*E/C, (c+1)*E/C) of all C blocks, runs a radix-C butterfly on them and writes each
+//               result into the shared memory of the CTA that owns its block (distributed shared memory);
+//     pass A  : stages on bits [LOGE-1 .. 8]   (32 residues per thread, stride 256),
+//     pass B  : stages on bits [7 .. 4]        (16 residues per thread, stride 16),
+//     pass C  : stages on bits [3 .. 0]        (16 contiguous residues), then the store to HBM.
+//   inverse (Gentleman–Sande, bit-reversed -> natural, N^-1 applied on the way out) runs the passes in the
+//   reverse order.
+// Butterflies are Harvey-lazy: forward values live in [0, 4p), inverse in [0, 2p); outputs are reduced to
+// [0, p).  Shared memory is XOR-swizzled (word l stored at l ^ ((l >> 5) & 15)) so every pass reads and
+// writes with at most the two-wavefront minimum of 64-bit accesses.
+#include <cooperative_groups.h>
+
+#include "ntt.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace fgb {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int swz(int l) { return l ^ ((l >> 5) & 15); }
+
+// X, Y in [0, 4p) -> X + wY, X - wY in [0, 4p).
+__device__ __forceinline__ void ct_bfly(u64& X, u64& Y, const ulonglong2& w, u64 p, u64 p2) {
+  u64 x = X >= p2 ? X - p2 : X;
+  u64 t = shoup_lazy(Y, w.x, w.y, p);
+  X = x + t;
+  Y = x - t + p2;
+}
+
+// X, Y in [0, 2p) -> X + Y, (X - Y) w in [0, 2p).
+__device__ __forceinline__ void gs_bfly(u64& X, u64& Y, const ulonglong2& w, u64 p, u64 p2) {
+  u64 s = X + Y;
+  s = s >= p2 ? s - p2 : s;
+  u64 d = X - Y + p2;
+  X = s;
+  Y = shoup_lazy(d, w.x, w.y, p);
+}
+
+// Radix-2^LOGR stages over x[k] = a[G*2^(LOGS+LOGR) + k*2^LOGS + low] (low < 2^LOGS).  At the sub-stage on
+// bit kb of k the pair distance is 2^(LOGS+kb), the global stage is s = LOGN-1-(LOGS+kb) and the twiddle of
+// the pair whose lower member is k has table index 2^s + G*2^(LOGR-1-kb) + (k >> (kb+1)).
+template <int LOGR, int LOGS, int LOGN>
+__device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 p,
+                                          u64 p2) {
+#pragma unroll
+  for (int kb = LOGR - 1; kb >= 0; kb--) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int s = LOGN - 1 - (LOGS + kb);
+    const int nw = 1 << (LOGR - 1 - kb);
+    const ulonglong2* row = tw + (1 << s) + G * nw;
+#pragma unroll
+    for (int k = 0; k < (1 << LOGR); k++) {
+      if (k & (1 << kb)) continue;
+      const ulonglong2 w = __ldg(row + (k >> (kb + 1)));
+      ct_bfly(x[k], x[k + (1 << kb)], w, p, p2);
+    }
+  }
+}
+
+template <int LOGR, int LOGS, int LOGN>
+__device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 p,
+                                          u64 p2) {
+#pragma unroll
+  for (int kb = 0; kb < LOGR; kb++) {
+    const int s = LOGN - 1 - (LOGS + kb);
+    const int nw = 1 << (LOGR - 1 - kb);
+    const ulonglong2* row = tw + (1 << s) + G * nw;
+#pragma unroll
+    for (int k = 0; k < (1 << LOGR); k++) {
+      if (k & (1 << kb)) continue;
+      const ulonglong2 w = __ldg(row + (k >> (kb + 1)));
+      gs_bfly(x[k], x[k + (1 << kb)], w, p, p2);
+    }
+  }
+}
+
+struct LimbRef {
+  u64* ptr;
+  int prime;
+};
+
+__device__ __forceinline__ LimbRef locate(const NttBatch& b, int limb, int N) {
+  LimbRef r{nullptr, 0};
+#pragma unroll 1
+  for (int s = 0; s < b.nseg; s++) {
+    const NttSeg& g = b.seg[s];
+    const int n = g.limbs * g.npolys;
+    if (limb >= g.limb_begin && limb < g.limb_begin + n) {
+      const int q = limb - g.limb_begin;
+      const int poly = q / g.limbs, j = q - poly * g.limbs;
+      r.ptr = g.data + poly * g.poly_stride + (long long)j * N;
+      r.prime = g.prime_of[j];
+    }
+  }
+  return r;
+}
+
+template <int LOGN>
+struct Shape {
+  static constexpr int N = 1 << LOGN;
+  static constexpr int LOGE = LOGN < 13 ? LOGN : 13;
+  static constexpr int E = 1 << LOGE;
+  static constexpr int LOGC = LOGN - LOGE;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int LOGRA = LOGE - 8;  // pass A radix
+};
+
+template <int LOGN>
+__global__ void __launch_bounds__(kThreads) ntt_fwd_kernel(const __grid_constant__ NttBatch b,
+                                                           const __grid_constant__ DeviceTables T, int limb0) {
+  using S = Shape<LOGN>;
+  extern __shared__ __align__(16) u64 sm[];
+  const int tid = threadIdx.x;
+  const LimbRef L = locate(b, limb0 + blockIdx.y, S::N);
+  const u64 p = T.pc[L.prime].p, p2 = T.pc[L.prime].p2;
+  const ulonglong2* __restrict__ tw = T.tw_fwd + (size_t)L.prime * S::N;
+  int h = 0;
+
+  if constexpr (S::C > 1) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int c = (int)cl.block_rank();
+    constexpr int LPC = S::E / S::C;
+    constexpr int IT = LPC / kThreads;
+    u64 x[IT][S::C];
+#pragma unroll
+    for (int it = 0; it < IT; it++) {
+      const int l = c * LPC + it * kThreads + tid;
+#pragma unroll
+      for (int hh = 0; hh < S::C; hh++) x[it][hh] = __ldg(L.ptr + hh * S::E + l);
+    }
+#pragma unroll
+    for (int it = 0; it < IT; it++) fwd_radix<S::LOGC, S::LOGE, LOGN>(x[it], 0, tw, p, p2);
+    cl.sync();  // every CTA of the cluster is running before its shared memory is written
+#pragma unroll
+    for (int it = 0; it < IT; it++) {
+      const int l = c * LPC + it * kThreads + tid;
+#pragma unroll
+      for (int hh = 0; hh < S::C; hh++) {
+        u64* dst = cl.map_shared_rank(sm, hh);
+        dst[swz(l)] = x[it][hh];
+      }
+    }
+    cl.sync();
+    h = c;
+  }
+
+  {  // pass A
+    constexpr int R = 1 << S::LOGRA;
+    u64 x[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+      const int l = k * 256 + tid;
+      if constexpr (S::C > 1)
+        x[k] = sm[swz(l)];
+      else
+        x[k] = (l < S::E) ? __ldg(L.ptr + l) : 0ull;
+    }
+    fwd_radix<S::LOGRA, 8, LOGN>(x, h, tw, p, p2);
+#pragma unroll
+    for (int k = 0; k < R; k++) sm[swz(k * 256 + tid)] = x[k];
+  }
+  __syncthreads();
+
+#pragma unroll 1
+  for (int g = tid; g < S::E / 16; g += kThreads) {  // pass B
+    const int low = g & 15, high = g >> 4;
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
+    fwd_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, p, p2);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
+  }
+  __syncthreads();
+
+#pragma unroll 1
+  for (int g = tid; g < S::E / 16; g += kThreads) {  // pass C
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
+    fwd_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, p, p2);
+    ulonglong2* out = reinterpret_cast<ulonglong2*>(L.ptr + h * S::E + g * 16);
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+      ulonglong2 v;
+      v.x = csub(csub(x[k], p2), p);
+      v.y = csub(csub(x[k + 1], p2), p);
+      out[k / 2] = v;
+    }
+  }
+}
+
+template <int LOGN>
+__global__ void __launch_bounds__(kThreads) ntt_inv_kernel(const __grid_constant__ NttBatch b,
+                                                           const __grid_constant__ DeviceTables T, int limb0) {
+  using S = Shape<LOGN>;
+  extern __shared__ __align__(16) u64 sm[];
+  const int tid = threadIdx.x;
+  const LimbRef L = locate(b, limb0 + blockIdx.y, S::N);
+  const PrimeConst& pc = T.pc[L.prime];
+  const u64 p = pc.p, p2 = pc.p2, ninv = pc.ninv, ninv_sh = pc.ninv_sh;
+  const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
+  int h = 0;
+  if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
+
+#pragma unroll 1
+  for (int g = tid; g < S::E / 16; g += kThreads) {  // pass C^-1
+    u64 x[16];
+    const ulonglong2* in = reinterpret_cast<const ulonglong2*>(L.ptr + h * S::E + g * 16);
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+      const ulonglong2 v = __ldg(in + k / 2);
+      x[k] = v.x;
+      x[k + 1] = v.y;
+    }
+    inv_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, p, p2);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(g * 16 + k)] = x[k];
+  }
+  __syncthreads();
+
+#pragma unroll 1
+  for (int g = tid; g < S::E / 16; g += kThreads) {  // pass B^-1
+    const int low = g & 15, high = g >> 4;
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
+    inv_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, p, p2);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
+  }
+  __syncthreads();
+
+  {  // pass A^-1
+    constexpr int R = 1 << S::LOGRA;
+    u64 x[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+      const int l = k * 256 + tid;
+      x[k] = (l < S::E) ? sm[swz(l)] : 0ull;
+    }
+    inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, p, p2);
+    if constexpr (S::C == 1) {
+#pragma unroll
+      for (int k = 0; k < R; k++) {
+        const int l = k * 256 + tid;
+        if (l < S::E) L.ptr[l] = csub(shoup_lazy(x[k], ninv, ninv_sh, p), p);
+      }
+      return;
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; k++) sm[swz(k * 256 + tid)] = x[k];
+    }
+  }
+
+  if constexpr (S::C > 1) {  // phase X^-1 across the cluster
+    cg::cluster_group cl = cg::this_cluster();
+    cl.sync();
+    const int c = h;
+    constexpr int LPC = S::E / S::C;
+    constexpr int IT = LPC / kThreads;
+#pragma unroll
+    for (int it = 0; it < IT; it++) {
+      const int l = c * LPC + it * kThreads + tid;
+      u64 x[S::C];
+#pragma unroll
+      for (int hh = 0; hh < S::C; hh++) {
+        const u64* src = cl.map_shared_rank(sm, hh);
+        x[hh] = src[swz(l)];
+      }
+      inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, p, p2);
+#pragma unroll
+      for (int hh = 0; hh < S::C; hh++) L.ptr[hh * S::E + l] = csub(shoup_lazy(x[hh], ninv, ninv_sh, p), p);
+    }
+    cl.sync();  // peers may still be reading this CTA's shared memory
+  }
+}
+
+template <int LOGN>
+cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
+  using S = Shape<LOGN>;
+  auto kern = inverse ? ntt_inv_kernel<LOGN> : ntt_fwd_kernel<LOGN>;
+  static bool attr_done[2] = {false, false};
+  const size_t smem = sizeof(u64) * S::E;
+  if (!attr_done[inverse]) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done[inverse] = true;
+  }
+  for (int limb0 = 0; limb0 < b.total_limbs; limb0 += 65535) {
+    const int n = (b.total_limbs - limb0) < 65535 ? (b.total_limbs - limb0) : 65535;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(S::C, n, 1);
+    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = S::C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = S::C > 1 ? 1 : 0;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, b, t, limb0);
+    if (e != cudaSuccess) return e;
+    count_launch();
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
+  if (b.total_limbs <= 0) return cudaSuccess;
+  switch (t.logN) {
+    case 10: return launch_t<10>(b, t, inverse, s);
+    case 11: return launch_t<11>(b, t, inverse, s);
+    case 12: return launch_t<12>(b, t, inverse, s);
+    case 13: return launch_t<13>(b, t, inverse, s);
+    case 14: return launch_t<14>(b, t, inverse, s);
+    case 15: return launch_t<15>(b, t, inverse, s);
+    case 16: return launch_t<16>(b, t, inverse, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace fgb

@@ -1,0 +1,124 @@
+/*
+ * fideslib_gb300 — C ABI of the GB300 CKKS evaluation engine.
+ *
+ * Plain pointers, sizes and integer status codes; no C++ types, no exceptions and no process exit cross
+ * this boundary.  Every function returns FIDES_OK (0) or a negative FIDES_E* code; fides_last_error()
+ * gives the message of the calling thread's last failure.
+ *
+ * Data contract (the one FIDESlib's OpenFHE interop extracts, src/CKKS/openfhe-interface/RawCiphertext.cuh:
+ * 19-93):
+ *   - residues are uint64 in [0, q), evaluation (NTT, bit-reversed) format, exactly the layout of
+ *     RawCipherText::sub_0 / sub_1 (RawCiphertext.cu:55-64);
+ *   - a ciphertext with t active towers (OpenFHE level = nq - t) is host memory u64[2][t][N];
+ *   - a key-switching key is u64[2][dnum][nq+np][N], index 0 = the "a" vectors, 1 = the "b" vectors, as in
+ *     RawKeySwitchKey::r_key (RawCiphertext.cu:650-666);
+ *   - moduli are the nq Q primes followed by the np special primes, each prime < 2^60 and == 1 mod 2N.
+ * Ownership: the engine owns device memory behind opaque uint32 handles (0 is never a valid handle), the
+ * caller owns every host buffer.  A context is used by one host thread at a time.
+ */
+#ifndef FIDESLIB_GB300_H
+#define FIDESLIB_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  FIDES_OK = 0,
+  FIDES_EINVAL = -1,    /* bad argument (sizes, handles, parameters) */
+  FIDES_ENOKEY = -2,    /* no relinearisation / rotation key loaded for the request */
+  FIDES_ENOMEM = -3,    /* device allocation failed */
+  FIDES_ECUDA = -4,     /* CUDA runtime error */
+  FIDES_ENODEV = -5     /* no usable CUDA device */
+};
+
+/* Scaling technique tags, same values as lbcrypto::ScalingTechnique used by Parameters::scalingTechnique
+ * (src/CKKS/Parameters.cuh:27). */
+enum { FIDES_FIXEDMANUAL = 0, FIDES_FIXEDAUTO = 1, FIDES_FLEXIBLEAUTO = 2, FIDES_FLEXIBLEAUTOEXT = 3 };
+
+typedef struct fides_ctx fides_ctx;
+
+/* Replaces RawParams + FIDESlib::CKKS::Parameters::adaptTo + GenCryptoContextGPU
+ * (src/CKKS/openfhe-interface/RawCiphertext.cuh:50-86, src/CKKS/Parameters.cu:7-34, src/CKKS/Context.cu:36-86). */
+typedef struct {
+  uint32_t log_n;           /* ring dimension N = 2^log_n, 10 <= log_n <= 16 */
+  uint32_t nq;              /* Q towers (OpenFHE L + 1) */
+  uint32_t np;              /* special towers K */
+  uint32_t dnum;            /* key-switching digits; towers per digit alpha = ceil(nq / dnum) */
+  const uint64_t* moduli;   /* nq + np primes */
+  const uint64_t* roots;    /* nq + np primitive 2N-th roots (RawParams::root_of_unity); NULL = generated */
+  int32_t scaling_technique;
+} fides_params;
+
+/* Ciphertext metadata (RawCipherText::Noise / NoiseLevel / slots, RawCiphertext.cuh:28-31). */
+typedef struct {
+  uint32_t towers;          /* active Q towers t */
+  uint32_t noise_deg;       /* noise scale degree */
+  uint32_t slots;
+  uint32_t reserved;
+  double scale;             /* scaling factor */
+} fides_ct_meta;
+
+const char* fides_last_error(void);
+const char* fides_version(void);
+
+/* Context (LoadContext, api/CryptoContext.cpp:199-249). */
+int fides_ctx_create(const fides_params* params, fides_ctx** out);
+int fides_ctx_destroy(fides_ctx* ctx);
+/* The moduli and primitive 2N-th roots actually used (nq + np entries each). */
+int fides_ctx_moduli(const fides_ctx* ctx, uint64_t* moduli, uint64_t* roots);
+/* Galois element 5^index mod 2N (2N-1 for conjugation), FindAutomorphismIndex2nComplex semantics. */
+uint32_t fides_galois_element(const fides_ctx* ctx, int32_t index);
+/* Blocks until all queued device work of the context finished (CryptoContextImpl::Synchronize,
+ * api/CryptoContext.hpp:201). */
+int fides_synchronize(fides_ctx* ctx);
+/* The cudaStream_t the context orders its work on, and a way to replace it with a caller's stream (NULL
+ * restores the context's own).  FIDESlib exposes its per-limb streams the same way through
+ * LimbPartition / Stream (src/CudaUtils.cuh:98-160). */
+void* fides_ctx_stream(fides_ctx* ctx);
+int fides_ctx_set_stream(fides_ctx* ctx, void* stream);
+/* Number of engine kernels launched by this process so far (all contexts). */
+uint64_t fides_kernel_launches(void);
+
+/* Batched negacyclic NTT (inverse = 0: coefficient -> evaluation, bit-reversed) or INTT on `npolys`
+ * polynomials of `limbs` towers each, tower j using prime first_prime + j.  Device memory, in place,
+ * ordered on `stream` (a cudaStream_t; NULL = the context stream).  Replaces the batched NTT_/INTT_
+ * launches of LimbPartition::NTT / INTT (src/CKKS/LimbPartition.cu:332-421). */
+int fides_ntt_batch_device(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint32_t limbs, uint32_t first_prime,
+                           int inverse, void* stream);
+/* Same from host memory: copies in, transforms, copies back, synchronises. */
+int fides_ntt_batch_host(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint32_t limbs, uint32_t first_prime,
+                         int inverse);
+
+/* Keys (KeySwitchingKey::Initialize via GetEvalKeySwitchKey / GetRotationKeySwitchKey,
+ * src/CKKS/KeySwitchingKey.cu:19-34, RawCiphertext.cu:672-760).  The rotation key is registered under its
+ * Galois element. */
+int fides_load_eval_mult_key(fides_ctx* ctx, const uint64_t* key);
+int fides_load_rotation_key(fides_ctx* ctx, uint32_t galois, const uint64_t* key);
+int fides_load_rotation_key_device(fides_ctx* ctx, uint32_t galois, const uint64_t* dev_key);
+
+/* Ciphertexts (LoadCiphertext / GetOpenFHECipherText, api/CryptoContext.cpp:270-289,
+ * RawCiphertext.cu:47-129). */
+int fides_ct_load(fides_ctx* ctx, const uint64_t* data, const fides_ct_meta* meta, uint32_t* handle);
+int fides_ct_load_device(fides_ctx* ctx, const uint64_t* dev_data, const fides_ct_meta* meta, uint32_t* handle);
+int fides_ct_store(fides_ctx* ctx, uint32_t handle, uint64_t* data, fides_ct_meta* meta);
+int fides_ct_meta_get(fides_ctx* ctx, uint32_t handle, fides_ct_meta* meta);
+int fides_ct_free(fides_ctx* ctx, uint32_t handle);
+
+/* Evaluation (api/CryptoContext.cpp EvalAdd/EvalSub, EvalMult 1185-1210, EvalSquare, Rescale 1669-1712,
+ * EvalRotate 1406-1430, EvalFastRotation 1451-1617).  Results are new handles. */
+int fides_eval_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out);
+int fides_eval_sub(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out);
+int fides_eval_mult(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out);
+int fides_eval_square(fides_ctx* ctx, uint32_t a, uint32_t* out);
+int fides_rescale(fides_ctx* ctx, uint32_t a, uint32_t* out);
+int fides_eval_rotate(fides_ctx* ctx, uint32_t a, int32_t index, uint32_t* out);
+int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out);
+int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

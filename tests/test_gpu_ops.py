@@ -1,0 +1,123 @@
+"""GPU parity of the CKKS evaluation ops against the oracle: every residue bit-identical, through the C ABI.
+
+Inputs are real encryptions under oracle-generated keys, so each case also states decrypted precision."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = {
+    # ring, Q bits, P bits, dnum
+    "cfg1_n13": (13, [60] + [40] * 5, [60] * 3, 2),
+    "cfg3_small": (12, [60] + [50] * 29, [60] * 10, 3),
+    "dnum4": (11, [60] + [45] * 7, [60] * 3, 4),
+}
+
+
+class Env:
+    def __init__(self, name):
+        import fideslib_gb300 as F
+        logN, qb, pb, dnum = PARAMS[name]
+        self.N = N = 1 << logN
+        self.mods = O.make_moduli(logN, qb, pb)
+        self.nq, self.np = len(qb), len(pb)
+        self.orc = O.Ctx(N, self.nq, self.np, dnum, self.mods, threads=8)
+        self.gpu = F.CryptoContext(logN, self.mods, self.np, dnum, roots=None)
+        assert self.gpu.roots == [O.root_of_unity(p, 2 * N) for p in self.mods]
+        self.s = self.orc.secret(0x5EED0003)
+        rng = np.random.default_rng(7)
+        self.z = rng.uniform(-1, 1, N // 2) + 1j * rng.uniform(-1, 1, N // 2)
+        self.scale = 2.0 ** 40
+        self.pt = self.orc.encode(self.z, self.scale, self.nq)
+        self.ct = self.orc.encrypt(21, self.s, self.pt)
+        self.rlk = self.orc.relin_key(5, self.s)
+        self.gpu.load_eval_mult_key(self.rlk)
+        self.rot = {}
+
+    def rot_key(self, index):
+        g = self.orc.galois(index)
+        if g not in self.rot:
+            self.rot[g] = self.orc.rot_key(1000 + g, self.s, g)
+            self.gpu.load_rotation_key(g, self.rot[g])
+        return g, self.rot[g]
+
+    def at(self, t):
+        return np.ascontiguousarray(self.ct[:, :t])
+
+    def decode(self, ct, scale):
+        return self.orc.decode(self.orc.decrypt(self.s, ct), scale, self.N // 2)
+
+
+@pytest.fixture(scope="module", params=list(PARAMS))
+def env(request, engine_lib):
+    return Env(request.param)
+
+
+def test_rotate_bit_exact(env):
+    for t in sorted({env.nq, max(1, env.nq // 2), 1}):
+        for index in (1, -5):
+            g, key = env.rot_key(index)
+            ct = env.at(t)
+            h = env.gpu.load_ciphertext(ct, env.scale)
+            r = env.gpu.eval_rotate(h, index)
+            got = env.gpu.store_ciphertext(r)
+            exp = env.orc.rotate(ct, g, key)
+            assert np.array_equal(got, exp), (t, index)
+            err = np.abs(env.decode(got, env.scale) - np.roll(env.z, -index)).max()
+            assert err < 1e-5, err
+
+
+def test_fast_rotation_bit_exact(env):
+    t = env.nq
+    idx = [1, 2, -3, 4]
+    gk = [env.rot_key(i) for i in idx]
+    ct = env.at(t)
+    h = env.gpu.load_ciphertext(ct, env.scale)
+    outs = env.gpu.eval_fast_rotation(h, idx)
+    exps = env.orc.rotate_hoisted(ct, [g for g, _ in gk], [k for _, k in gk])
+    for o, e in zip(outs, exps):
+        assert np.array_equal(env.gpu.store_ciphertext(o), e)
+
+
+def test_mult_square_rescale_bit_exact(env):
+    for t in sorted({env.nq, max(2, env.nq // 2 + 1), 2}):
+        ct = env.at(t)
+        h = env.gpu.load_ciphertext(ct, env.scale)
+        m = env.gpu.eval_mult(h, h)
+        got = env.gpu.store_ciphertext(m)
+        exp = env.orc.mult(ct, ct, env.rlk)
+        assert np.array_equal(got, exp), t
+        sq = env.gpu.store_ciphertext(env.gpu.eval_square(h))
+        assert np.array_equal(sq, exp)
+        r = env.gpu.rescale(m)
+        gr = env.gpu.store_ciphertext(r)
+        er = env.orc.rescale(exp)
+        assert np.array_equal(gr, er), t
+        err = np.abs(env.decode(gr, env.scale ** 2 / env.mods[t - 1]) - env.z ** 2).max()
+        assert err < 1e-4, err
+        meta = env.gpu.meta(r)
+        assert meta.towers == t - 1 and meta.noise_deg == 1
+
+
+def test_add_sub_bit_exact(env):
+    t = env.nq
+    a = env.at(t)
+    b = env.orc.encrypt(99, env.s, env.pt)
+    ha, hb = env.gpu.load_ciphertext(a), env.gpu.load_ciphertext(b)
+    assert np.array_equal(env.gpu.store_ciphertext(env.gpu.eval_add(ha, hb)), env.orc.add(a, b))
+    assert np.array_equal(env.gpu.store_ciphertext(env.gpu.eval_sub(ha, hb)), env.orc.sub(a, b))
+
+
+def test_errors_are_status_codes(env):
+    import fideslib_gb300 as F
+    h = env.gpu.load_ciphertext(env.at(env.nq))
+    with pytest.raises(F.FidesError) as e:
+        env.gpu.eval_automorphism(h, 3)  # no key for Galois element 3
+    assert e.value.code == F.FIDES_ENOKEY
+    with pytest.raises(F.FidesError):
+        env.gpu.eval_add(h, 123456)
+    h1 = env.gpu.load_ciphertext(env.at(1))
+    with pytest.raises(F.FidesError):
+        env.gpu.rescale(h1)
