@@ -71,7 +71,14 @@ _SIGS = {
     "fides_eval_rotate": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int32, u32p]),
     "fides_eval_automorphism": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_fast_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, i32p, u32p]),
+    "fides_eval_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
 }
+
+OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM = 1, 2, 3, 4, 5, 6, 7
+
+
+class Op(C.Structure):
+    _fields_ = [("op", C.c_int32), ("a", C.c_uint32), ("b", C.c_uint32), ("index", C.c_int32), ("out", C.c_uint32)]
 
 
 def lib():
@@ -241,6 +248,15 @@ class CryptoContext:
 
     def eval_automorphism(self, a: int, galois: int) -> int:
         return self._bin(lib().fides_eval_automorphism, a, galois)
+
+    def eval_batch(self, ops) -> list[int]:
+        """ops: iterable of (op_code, a, b, index); returns result handles (one batched pipeline per op family)."""
+        ops = list(ops)
+        arr = (Op * max(1, len(ops)))()
+        for i, (code, a, b, index) in enumerate(ops):
+            arr[i] = Op(code, a, b, index, 0)
+        _check(lib().fides_eval_batch(self._h, arr, len(ops)))
+        return [arr[i].out for i in range(len(ops))]
 
     def eval_fast_rotation(self, a: int, indices) -> list[int]:
         idx = np.ascontiguousarray(np.array(indices, dtype=np.int32))

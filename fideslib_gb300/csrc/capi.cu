@@ -122,7 +122,7 @@ int fides_ntt_batch_device(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint
   if (limbs == 0 || npolys == 0) return FIDES_OK;
   if (limbs > 64 || first_prime + limbs > (uint32_t)c->ntow) return fail(FIDES_EINVAL, "tower range out of bounds");
   cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
-  CK(c->ntt((fgb::u64*)data, (int)npolys, (int)limbs, (int)first_prime, (long long)limbs * c->N, inverse != 0, s),
+  CK(c->ntt((const fgb::u64*)data, (fgb::u64*)data, (int)npolys, (int)limbs, (int)first_prime, (long long)limbs * c->N, inverse != 0, s),
      "ntt launch");
   return FIDES_OK;
 }
@@ -239,108 +239,153 @@ int fides_ct_free(fides_ctx* ctx, uint32_t handle) {
   return FIDES_OK;
 }
 
-static int binary_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out, bool sub) {
-  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
-  fgb::DevCt *A = find_ct(ctx, a), *B = find_ct(ctx, b);
-  if (!A || !B) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
-  fgb::DevCt r;
-  int rc = new_ct(ctx, A->t, *A, &r);
-  if (rc) return rc;
-  r.noise_deg = A->noise_deg > B->noise_deg ? A->noise_deg : B->noise_deg;
-  CK(fgb::launch_addsub(A->data, B->data, r.data, 2, A->t, ctx->c->N, sub, ctx->c->d_pc, ctx->c->stream), "add");
-  *out = register_ct(ctx, r);
-  return FIDES_OK;
-}
+// Validates one request and prepares its output ciphertext; the compute is issued by run_batch.
+struct Pending {
+  fgb::DevCt out;
+  const fgb::DevCt* a = nullptr;
+  const fgb::DevCt* b = nullptr;
+  uint32_t galois = 0;
+  const fgb::u64* key = nullptr;
+};
 
-int fides_eval_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return binary_add(ctx, a, b, out, false); }
-int fides_eval_sub(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return binary_add(ctx, a, b, out, true); }
-
-int fides_eval_mult(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) {
-  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
   fgb::Context* c = ctx->c;
-  fgb::DevCt *A = find_ct(ctx, a), *B = find_ct(ctx, b);
-  if (!A || !B) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
-  if (!c->relin_key) return fail(FIDES_ENOKEY, "no relinearisation key loaded");
-  if (int rc0 = check_ks_shape(ctx)) return rc0;
-  fgb::DevCt r;
-  int rc = new_ct(ctx, A->t, *A, &r);
-  if (rc) return rc;
-  r.noise_deg = A->noise_deg + B->noise_deg;
-  r.scale = A->scale * B->scale;
-  CK(c->mult(A->data, B->data, A->t, c->relin_key, r.data, c->stream), "mult");
-  *out = register_ct(ctx, r);
+  fgb::DevCt* A = find_ct(ctx, op.a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(op.a));
+  fgb::DevCt* B = nullptr;
+  if (op.op == FIDES_OP_ADD || op.op == FIDES_OP_SUB || op.op == FIDES_OP_MULT) {
+    B = find_ct(ctx, op.b);
+    if (!B) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(op.b));
+    if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
+  }
+  pd->a = A;
+  pd->b = B;
+  int t_out = A->t;
+  fgb::DevCt meta = *A;
+  switch (op.op) {
+    case FIDES_OP_ADD:
+    case FIDES_OP_SUB:
+      meta.noise_deg = A->noise_deg > B->noise_deg ? A->noise_deg : B->noise_deg;
+      break;
+    case FIDES_OP_MULT:
+    case FIDES_OP_SQUARE: {
+      if (!c->relin_key) return fail(FIDES_ENOKEY, "no relinearisation key loaded");
+      if (int rc = check_ks_shape(ctx)) return rc;
+      const fgb::DevCt* Y = op.op == FIDES_OP_SQUARE ? A : B;
+      meta.noise_deg = A->noise_deg + Y->noise_deg;
+      meta.scale = A->scale * Y->scale;
+      pd->b = Y;
+      break;
+    }
+    case FIDES_OP_RESCALE:
+      if (A->t < 2) return fail(FIDES_EINVAL, "cannot rescale a ciphertext with one tower");
+      t_out = A->t - 1;
+      meta.noise_deg = A->noise_deg > 1 ? A->noise_deg - 1 : 1;
+      meta.scale = A->scale / (double)c->mod[A->t - 1];
+      break;
+    case FIDES_OP_ROTATE:
+    case FIDES_OP_AUTOMORPHISM: {
+      const uint32_t g = op.op == FIDES_OP_ROTATE ? fgb::Context::galois_for_index(c->N, op.index) : (uint32_t)op.index;
+      auto it = c->rot_keys.find(g);
+      if (it == c->rot_keys.end())
+        return fail(FIDES_ENOKEY, "no rotation key for Galois element " + std::to_string(g));
+      if (int rc = check_ks_shape(ctx)) return rc;
+      pd->galois = g;
+      pd->key = it->second;
+      break;
+    }
+    default:
+      return fail(FIDES_EINVAL, "unknown op code " + std::to_string(op.op));
+  }
+  meta.t = t_out;
+  meta.data = c->alloc_limbs((size_t)2 * t_out, c->stream);
+  if (!meta.data) return fail(FIDES_ENOMEM, "ciphertext allocation failed");
+  pd->out = meta;
   return FIDES_OK;
 }
 
-int fides_eval_square(fides_ctx* ctx, uint32_t a, uint32_t* out) { return fides_eval_mult(ctx, a, a, out); }
-
-int fides_rescale(fides_ctx* ctx, uint32_t a, uint32_t* out) {
-  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+// Runs a set of independent requests as one batch per op family: every ciphertext of a family goes through
+// each pipeline stage in a single launch.
+static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
   fgb::Context* c = ctx->c;
-  fgb::DevCt* A = find_ct(ctx, a);
-  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  if (A->t < 2) return fail(FIDES_EINVAL, "cannot rescale a ciphertext with one tower");
-  fgb::DevCt r;
-  int rc = new_ct(ctx, A->t - 1, *A, &r);
-  if (rc) return rc;
-  r.noise_deg = A->noise_deg > 1 ? A->noise_deg - 1 : 1;
-  r.scale = A->scale / (double)c->mod[A->t - 1];
-  CK(c->rescale(A->data, A->t, r.data, c->stream), "rescale");
-  *out = register_ct(ctx, r);
+  std::vector<Pending> pd(n);
+  for (uint32_t i = 0; i < n; i++) {
+    int rc = prepare(ctx, ops[i], &pd[i]);
+    if (rc) {
+      for (uint32_t k = 0; k < i; k++) c->free_limbs(pd[k].out.data, c->stream);
+      return rc;
+    }
+  }
+  std::vector<fgb::Context::AddReq> adds;
+  std::vector<fgb::Context::MultReq> mults;
+  std::vector<fgb::Context::RescaleReq> rescales;
+  std::vector<fgb::Context::KsReq> rots;
+  const size_t NN = (size_t)c->N;
+  for (uint32_t i = 0; i < n; i++) {
+    const Pending& p = pd[i];
+    const int t = p.a->t;
+    switch (ops[i].op) {
+      case FIDES_OP_ADD:
+      case FIDES_OP_SUB:
+        adds.push_back({p.a->data, p.b->data, t, p.out.data, ops[i].op == FIDES_OP_SUB});
+        break;
+      case FIDES_OP_MULT:
+      case FIDES_OP_SQUARE:
+        mults.push_back({p.a->data, p.b->data, t, p.out.data});
+        break;
+      case FIDES_OP_RESCALE:
+        rescales.push_back({p.a->data, t, p.out.data});
+        break;
+      default:
+        rots.push_back({p.a->data + (size_t)t * NN, t, p.key, p.a->data, nullptr, p.out.data,
+                        c->galois_inverse(p.galois)});
+    }
+  }
+  cudaError_t e = c->add_batch(adds.data(), (int)adds.size(), c->stream);
+  if (e == cudaSuccess) e = c->rescale_batch(rescales.data(), (int)rescales.size(), c->stream);
+  if (e == cudaSuccess) e = c->mult_batch(mults.data(), (int)mults.size(), c->relin_key, c->stream);
+  if (e == cudaSuccess) e = c->keyswitch_batch(rots.data(), (int)rots.size(), c->stream);
+  if (e != cudaSuccess) {
+    for (uint32_t k = 0; k < n; k++) c->free_limbs(pd[k].out.data, c->stream);
+    return cuda_fail(e, "batch");
+  }
+  for (uint32_t i = 0; i < n; i++) ops[i].out = register_ct(ctx, pd[i].out);
   return FIDES_OK;
 }
 
-int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out) {
+static int one(fides_ctx* ctx, int32_t code, uint32_t a, uint32_t b, int32_t index, uint32_t* out) {
   if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
-  fgb::Context* c = ctx->c;
-  fgb::DevCt* A = find_ct(ctx, a);
-  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  auto it = c->rot_keys.find(galois);
-  if (it == c->rot_keys.end()) return fail(FIDES_ENOKEY, "no rotation key for Galois element " + std::to_string(galois));
-  if (int rc0 = check_ks_shape(ctx)) return rc0;
-  fgb::DevCt r;
-  int rc = new_ct(ctx, A->t, *A, &r);
-  if (rc) return rc;
-  CK(c->rotate(A->data, A->t, galois, it->second, r.data, c->stream), "rotate");
-  *out = register_ct(ctx, r);
-  return FIDES_OK;
+  fides_op op{code, a, b, index, 0};
+  int rc = run_batch(ctx, &op, 1);
+  if (rc == FIDES_OK) *out = op.out;
+  return rc;
 }
 
+int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
+  if (!valid_ctx(ctx) || (n && !ops)) return fail(FIDES_EINVAL, "null argument");
+  return run_batch(ctx, ops, n);
+}
+
+int fides_eval_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return one(ctx, FIDES_OP_ADD, a, b, 0, out); }
+int fides_eval_sub(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return one(ctx, FIDES_OP_SUB, a, b, 0, out); }
+int fides_eval_mult(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return one(ctx, FIDES_OP_MULT, a, b, 0, out); }
+int fides_eval_square(fides_ctx* ctx, uint32_t a, uint32_t* out) { return one(ctx, FIDES_OP_SQUARE, a, 0, 0, out); }
+int fides_rescale(fides_ctx* ctx, uint32_t a, uint32_t* out) { return one(ctx, FIDES_OP_RESCALE, a, 0, 0, out); }
 int fides_eval_rotate(fides_ctx* ctx, uint32_t a, int32_t index, uint32_t* out) {
-  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
-  return fides_eval_automorphism(ctx, a, fgb::Context::galois_for_index(ctx->c->N, index), out);
+  return one(ctx, FIDES_OP_ROTATE, a, 0, index, out);
+}
+int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out) {
+  return one(ctx, FIDES_OP_AUTOMORPHISM, a, 0, (int32_t)galois, out);
 }
 
 int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs) {
   if (!valid_ctx(ctx) || (n && (!indices || !outs))) return fail(FIDES_EINVAL, "null argument");
-  fgb::Context* c = ctx->c;
-  fgb::DevCt* A = find_ct(ctx, a);
-  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  std::vector<fgb::u64*> keys(n);
-  std::vector<uint32_t> gal(n);
-  for (uint32_t r = 0; r < n; r++) {
-    gal[r] = fgb::Context::galois_for_index(c->N, indices[r]);
-    auto it = c->rot_keys.find(gal[r]);
-    if (it == c->rot_keys.end())
-      return fail(FIDES_ENOKEY, "no rotation key for index " + std::to_string(indices[r]));
-    keys[r] = it->second;
-  }
-  if (int rc0 = check_ks_shape(ctx)) return rc0;
-  const int t = A->t;
-  const size_t P = (size_t)t * c->N;
-  CK(c->modup(A->data + P, t, c->stream), "modup");
-  for (uint32_t r = 0; r < n; r++) {
-    fgb::DevCt res;
-    int rc = new_ct(ctx, t, *A, &res);
-    if (rc) return rc;
-    CK(c->ks_from_digits(A->data + P, t, keys[r], A->data, nullptr, res.data, c->galois_inverse(gal[r]), c->stream),
-       "hoisted rotate");
-    outs[r] = register_ct(ctx, res);
-    A = find_ct(ctx, a);  // registry may have rehashed
-  }
-  return FIDES_OK;
+  std::vector<fides_op> ops(n);
+  for (uint32_t i = 0; i < n; i++) ops[i] = fides_op{FIDES_OP_ROTATE, a, 0, indices[i], 0};
+  int rc = run_batch(ctx, ops.data(), n);  // same input: one shared ModUp
+  if (rc == FIDES_OK)
+    for (uint32_t i = 0; i < n; i++) outs[i] = ops[i].out;
+  return rc;
 }
 
 }  // extern "C"

@@ -197,7 +197,7 @@ bool Context::build(const u64* roots, std::string* err) {
     c.one_sh = shoup_of(1, p);
     c.ninv = hinv((u64)N, p);
     c.ninv_sh = shoup_of(c.ninv, p);
-    c.pad = 0;
+    c.negp = 0ull - p;
   }
   d_pc = (PrimeConst*)dmalloc(sizeof(PrimeConst) * ntow);
   if (!d_pc) {
@@ -312,19 +312,12 @@ bool Context::build(const u64* roots, std::string* err) {
   crt.md_pinv = (const ulonglong2*)up(md_pinv.data(), sizeof(ulonglong2) * md_pinv.size());
   crt.rs_qinv = (const ulonglong2*)up(rs_qinv.data(), sizeof(ulonglong2) * rs_qinv.size());
 
-  const size_t L = (size_t)N * sizeof(u64);
-  ws_coeff_ = (u64*)dmalloc(L * nq);
-  ws_conv_ = (u64*)dmalloc(L * dnum * ntow);
-  ws_inner_ = (u64*)dmalloc(L * 2 * ntow);
-  ws_md_ = (u64*)dmalloc(L * 2 * nq);
-  ws_tensor_ = (u64*)dmalloc(L * 3 * nq);
-  ws_top_ = (u64*)dmalloc(L * 2);
-  ws_rs_ = (u64*)dmalloc(L * 2 * nq);
-  if (!crt.mu_qhinv || !crt.mu_qhat || !crt.md_phinv || !crt.md_phat || !crt.md_pinv || !crt.rs_qinv ||
-      !ws_coeff_ || !ws_conv_ || !ws_inner_ || !ws_md_ || !ws_tensor_ || !ws_top_ || !ws_rs_) {
+  if (!crt.mu_qhinv || !crt.mu_qhat || !crt.md_phinv || !crt.md_phat || !crt.md_pinv || !crt.rs_qinv) {
     *err = "device allocation failed";
     return false;
   }
+  ring_.N = N;
+  ring_.logN = logN;
   if (cudaDeviceSynchronize() != cudaSuccess) {
     *err = std::string("device error during context set-up: ") + cudaGetErrorString(cudaGetLastError());
     return false;
@@ -360,104 +353,258 @@ uint32_t Context::galois_for_index(int N, int32_t index) {
   return (uint32_t)g;
 }
 
-cudaError_t Context::ntt(u64* data, int npolys, int limbs, int first_prime, long long poly_stride, bool inverse,
-                         cudaStream_t s) {
-  NttBatch b{};
-  b.nseg = 1;
-  b.total_limbs = npolys * limbs;
-  NttSeg& g = b.seg[0];
-  g.data = data;
-  g.poly_stride = poly_stride;
-  g.limbs = limbs;
-  g.npolys = npolys;
-  g.limb_begin = 0;
-  for (int j = 0; j < limbs; j++) g.prime_of[j] = (uint8_t)(first_prime + j);
-  return launch_ntt(b, tabs, inverse, s);
-}
+namespace {
 
-cudaError_t Context::modup(const u64* a, int t, cudaStream_t s) {
-  const size_t L = (size_t)N;
-  const int beta = (t + alpha - 1) / alpha;
-  FGB_TRY(cudaMemcpyAsync(ws_coeff_, a, sizeof(u64) * L * t, cudaMemcpyDeviceToDevice, s));
-  FGB_TRY(ntt(ws_coeff_, 1, t, 0, 0, true, s));
-  KsDims k{N, logN, t, beta};
-  const long long cs = (long long)ntow * N;
-  FGB_TRY(launch_modup_conv(ws_coeff_, ws_conv_, cs, k, crt, d_pc, s));
+// Accumulates NTT jobs and launches whenever kMaxNttJobs are queued.
+struct NttQueue {
+  const DeviceTables& tabs;
+  bool inverse;
+  cudaStream_t s;
   NttBatch b{};
-  b.nseg = beta;
-  int begin = 0;
-  for (int d = 0; d < beta; d++) {
-    const int start = d * alpha, sz = std::min(alpha, t - start);
-    NttSeg& g = b.seg[d];
-    g.data = ws_conv_ + d * cs;
-    g.poly_stride = 0;
-    g.npolys = 1;
-    g.limbs = t - sz + np;
-    g.limb_begin = begin;
-    for (int jj = 0; jj < g.limbs; jj++)
-      g.prime_of[jj] = (uint8_t)(jj < start ? jj : (jj < t - sz ? jj + sz : nq + (jj - (t - sz))));
-    begin += g.limbs;
+  cudaError_t err = cudaSuccess;
+  NttQueue(const DeviceTables& t, bool inv, cudaStream_t st) : tabs(t), inverse(inv), s(st) {}
+  void add(const u64* src, u64* dst, long long ss, long long ds, int limbs, int npolys, const uint8_t* prime_of) {
+    if (err != cudaSuccess || limbs <= 0 || npolys <= 0) return;
+    if (b.njobs == kMaxNttJobs) flush();
+    ntt_add_job(b, src, dst, ss, ds, limbs, npolys, prime_of);
   }
-  b.total_limbs = begin;
-  FGB_TRY(launch_ntt(b, tabs, false, s));
-  digits_t_ = t;
-  return cudaSuccess;
+  void flush() {
+    if (err == cudaSuccess && b.njobs > 0) err = launch_ntt(b, tabs, inverse, s);
+    b.njobs = 0;
+    b.max_limbs = 0;
+  }
+};
+
+}  // namespace
+
+cudaError_t Context::ntt(const u64* src, u64* dst, int npolys, int limbs, int first_prime, long long poly_stride,
+                         bool inverse, cudaStream_t s) {
+  NttQueue q(tabs, inverse, s);
+  uint8_t pm[64];
+  for (int j = 0; j < limbs; j++) pm[j] = (uint8_t)(first_prime + j);
+  q.add(src, dst, poly_stride, poly_stride, limbs, npolys, pm);
+  q.flush();
+  return q.err;
 }
 
-cudaError_t Context::ks_from_digits(const u64* a, int t, const u64* key, const u64* add0, const u64* add1, u64* out,
-                                    uint32_t galois_inv, cudaStream_t s) {
-  const int beta = (t + alpha - 1) / alpha;
-  KsDims k{N, logN, t, beta};
-  const long long cs = (long long)ntow * N;
-  const int ext = t + np;
-  FGB_TRY(launch_ks_inner(a, ws_conv_, cs, key, ws_inner_, k, crt, d_pc, s));
-  // P towers of both inner products to coefficient form
+cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const size_t NN = (size_t)N;
+  // ModUp groups: requests with the same input share the digits.
+  std::vector<int> group_of(n);
+  std::vector<int> gfirst;
+  for (int i = 0; i < n; i++) {
+    int g = -1;
+    for (size_t k = 0; k < gfirst.size(); k++)
+      if (reqs[gfirst[k]].a == reqs[i].a && reqs[gfirst[k]].t == reqs[i].t) {
+        g = (int)k;
+        break;
+      }
+    if (g < 0) {
+      g = (int)gfirst.size();
+      gfirst.push_back(i);
+    }
+    group_of[i] = g;
+  }
+  const int ng = (int)gfirst.size();
+  size_t total = 0;
+  std::vector<size_t> g_off(ng), r_off(n);
+  for (int g = 0; g < ng; g++) {
+    const int t = reqs[gfirst[g]].t, beta = (t + alpha - 1) / alpha;
+    g_off[g] = total;
+    total += (size_t)t + (size_t)beta * (t + np);
+  }
+  for (int i = 0; i < n; i++) {
+    const int t = reqs[i].t;
+    r_off[i] = total;
+    total += (size_t)2 * (t + np) + (size_t)2 * t;
+  }
+  u64* ws = alloc_limbs(total, s);
+  if (!ws) return cudaErrorMemoryAllocation;
+  auto coeff_of = [&](int g) { return ws + g_off[g] * NN; };
+  auto conv_of = [&](int g) { return ws + (g_off[g] + reqs[gfirst[g]].t) * NN; };
+  auto inner_of = [&](int i) { return ws + r_off[i] * NN; };
+  auto md_of = [&](int i) { return ws + (r_off[i] + 2 * (size_t)(reqs[i].t + np)) * NN; };
+  cudaError_t err = cudaSuccess;
+  uint8_t pm[64];
+
+  // 1) INTT of every distinct input into its coefficient buffer
   {
-    NttBatch b{};
-    b.nseg = 1;
-    b.total_limbs = 2 * np;
-    NttSeg& g = b.seg[0];
-    g.data = ws_inner_ + (size_t)t * N;
-    g.poly_stride = (long long)ext * N;
-    g.limbs = np;
-    g.npolys = 2;
-    for (int j = 0; j < np; j++) g.prime_of[j] = (uint8_t)(nq + j);
-    FGB_TRY(launch_ntt(b, tabs, true, s));
+    NttQueue q(tabs, true, s);
+    for (int g = 0; g < ng; g++) {
+      const KsReq& r = reqs[gfirst[g]];
+      for (int j = 0; j < r.t; j++) pm[j] = (uint8_t)j;
+      q.add(r.a, coeff_of(g), 0, 0, r.t, 1, pm);
+    }
+    q.flush();
+    err = q.err;
   }
-  FGB_TRY(launch_moddown_conv(ws_inner_, (long long)ext * N, ws_md_, (long long)t * N, 2, k, crt, d_pc, s));
-  FGB_TRY(ntt(ws_md_, 2, t, 0, (long long)t * N, false, s));
-  FGB_TRY(launch_moddown_epilogue(ws_inner_, (long long)ext * N, ws_md_, (long long)t * N, add0, add1, out,
-                                  (long long)t * N, 2, galois_inv, k, crt, d_pc, s));
-  return cudaSuccess;
+  // 2) ModUp basis conversion, 3) NTT of the converted rows
+  for (int g0 = 0; g0 < ng && err == cudaSuccess; g0 += kMaxJobs) {
+    KsBatch kb{};
+    for (int g = g0; g < ng && kb.njobs < kMaxJobs; g++) {
+      KsJob& j = kb.jobs[kb.njobs++];
+      j = KsJob{};
+      j.a = reqs[gfirst[g]].a;
+      j.coeff = coeff_of(g);
+      j.conv = conv_of(g);
+      j.t = reqs[gfirst[g]].t;
+    }
+    err = launch_modup_conv(kb, ring_, crt, d_pc, s);
+  }
+  if (err == cudaSuccess) {
+    NttQueue q(tabs, false, s);
+    for (int g = 0; g < ng; g++) {
+      const int t = reqs[gfirst[g]].t, beta = (t + alpha - 1) / alpha;
+      for (int d = 0; d < beta; d++) {
+        const int start = d * alpha, sz = std::min(alpha, t - start), rows = t - sz + np;
+        for (int jj = 0; jj < rows; jj++)
+          pm[jj] = (uint8_t)(jj < start ? jj : (jj < t - sz ? jj + sz : nq + (jj - (t - sz))));
+        u64* c = conv_of(g) + (size_t)d * (t + np) * NN;
+        q.add(c, c, 0, 0, rows, 1, pm);
+      }
+    }
+    q.flush();
+    err = q.err;
+  }
+  // 4) inner products, 5) INTT of the P rows, 6) ModDown conversion, 7) NTT, 8) epilogue
+  for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
+    KsBatch kb{};
+    for (int i = i0; i < n && kb.njobs < kMaxJobs; i++) {
+      const KsReq& r = reqs[i];
+      KsJob& j = kb.jobs[kb.njobs++];
+      j.a = r.a;
+      j.add0 = r.add0;
+      j.add1 = r.add1;
+      j.key = r.key;
+      j.coeff = coeff_of(group_of[i]);
+      j.conv = conv_of(group_of[i]);
+      j.inner = inner_of(i);
+      j.md = md_of(i);
+      j.out = r.out;
+      j.t = r.t;
+      j.galois_inv = r.galois_inv;
+    }
+    err = launch_ks_inner(kb, ring_, crt, d_pc, s);
+    if (err != cudaSuccess) break;
+    {
+      NttQueue q(tabs, true, s);
+      for (int k = 0; k < np; k++) pm[k] = (uint8_t)(nq + k);
+      for (int b = 0; b < kb.njobs; b++) {
+        const KsJob& j = kb.jobs[b];
+        u64* p = j.inner + (size_t)j.t * NN;
+        q.add(p, p, (long long)(j.t + np) * N, (long long)(j.t + np) * N, np, 2, pm);
+      }
+      q.flush();
+      err = q.err;
+    }
+    if (err != cudaSuccess) break;
+    err = launch_moddown_conv(kb, ring_, crt, d_pc, s);
+    if (err != cudaSuccess) break;
+    {
+      NttQueue q(tabs, false, s);
+      for (int b = 0; b < kb.njobs; b++) {
+        const KsJob& j = kb.jobs[b];
+        for (int k = 0; k < j.t; k++) pm[k] = (uint8_t)k;
+        q.add(j.md, j.md, (long long)j.t * N, (long long)j.t * N, j.t, 2, pm);
+      }
+      q.flush();
+      err = q.err;
+    }
+    if (err != cudaSuccess) break;
+    err = launch_moddown_epilogue(kb, ring_, crt, d_pc, s);
+  }
+  free_limbs(ws, s);
+  return err;
 }
 
-cudaError_t Context::keyswitch(const u64* a, int t, const u64* key, const u64* add0, const u64* add1, u64* out,
-                               uint32_t galois_inv, cudaStream_t s) {
-  FGB_TRY(modup(a, t, s));
-  return ks_from_digits(a, t, key, add0, add1, out, galois_inv, s);
+cudaError_t Context::mult_batch(const MultReq* reqs, int n, const u64* rlk, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const size_t NN = (size_t)N;
+  size_t total = 0;
+  std::vector<size_t> off(n);
+  for (int i = 0; i < n; i++) {
+    off[i] = total;
+    total += (size_t)3 * reqs[i].t;
+  }
+  u64* ws = alloc_limbs(total, s);
+  if (!ws) return cudaErrorMemoryAllocation;
+  cudaError_t err = cudaSuccess;
+  for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
+    TensorBatch tb{};
+    for (int i = i0; i < n && tb.njobs < kMaxJobs; i++)
+      tb.jobs[tb.njobs++] = TensorJob{reqs[i].x, reqs[i].y, ws + off[i] * NN, reqs[i].t};
+    err = launch_tensor(tb, ring_, nq, d_pc, s);
+  }
+  if (err == cudaSuccess) {
+    std::vector<KsReq> ks(n);
+    for (int i = 0; i < n; i++) {
+      u64* d = ws + off[i] * NN;
+      const size_t P = (size_t)reqs[i].t * NN;
+      ks[i] = KsReq{d + 2 * P, reqs[i].t, rlk, d, d + P, reqs[i].out, 1u};
+    }
+    err = keyswitch_batch(ks.data(), n, s);
+  }
+  free_limbs(ws, s);
+  return err;
 }
 
-cudaError_t Context::mult(const u64* x, const u64* y, int t, const u64* rlk, u64* out, cudaStream_t s) {
-  const size_t P = (size_t)t * N;
-  FGB_TRY(launch_tensor(x, y, ws_tensor_, t, N, d_pc, s));
-  return keyswitch(ws_tensor_ + 2 * P, t, rlk, ws_tensor_, ws_tensor_ + P, out, 1, s);
+cudaError_t Context::rescale_batch(const RescaleReq* reqs, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const size_t NN = (size_t)N;
+  size_t total = 0;
+  std::vector<size_t> off(n);
+  for (int i = 0; i < n; i++) {
+    if (reqs[i].t < 2) return cudaErrorInvalidValue;
+    off[i] = total;
+    total += 2 + (size_t)2 * (reqs[i].t - 1);
+  }
+  u64* ws = alloc_limbs(total, s);
+  if (!ws) return cudaErrorMemoryAllocation;
+  cudaError_t err = cudaSuccess;
+  uint8_t pm[64];
+  for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
+    RescaleBatch rb{};
+    for (int i = i0; i < n && rb.njobs < kMaxJobs; i++) {
+      u64* top = ws + off[i] * NN;
+      rb.jobs[rb.njobs++] = RescaleJob{reqs[i].x, top, top + 2 * NN, reqs[i].out, reqs[i].t};
+    }
+    {  // top towers of both polys to coefficient form (out of place)
+      NttQueue q(tabs, true, s);
+      for (int b = 0; b < rb.njobs; b++) {
+        const RescaleJob& j = rb.jobs[b];
+        pm[0] = (uint8_t)(j.t - 1);
+        q.add(j.x + (size_t)(j.t - 1) * NN, const_cast<u64*>(j.top), (long long)j.t * N, N, 1, 2, pm);
+      }
+      q.flush();
+      err = q.err;
+    }
+    if (err == cudaSuccess) err = launch_rescale_switch(rb, ring_, nq, d_pc, s);
+    if (err == cudaSuccess) {
+      NttQueue q(tabs, false, s);
+      for (int b = 0; b < rb.njobs; b++) {
+        const RescaleJob& j = rb.jobs[b];
+        for (int k = 0; k < j.t - 1; k++) pm[k] = (uint8_t)k;
+        q.add(j.tmp, j.tmp, (long long)(j.t - 1) * N, (long long)(j.t - 1) * N, j.t - 1, 2, pm);
+      }
+      q.flush();
+      err = q.err;
+    }
+    if (err == cudaSuccess) err = launch_rescale_epilogue(rb, ring_, crt, d_pc, s);
+  }
+  free_limbs(ws, s);
+  return err;
 }
 
-cudaError_t Context::rotate(const u64* x, int t, uint32_t galois, const u64* key, u64* out, cudaStream_t s) {
-  const size_t P = (size_t)t * N;
-  return keyswitch(x + P, t, key, x, nullptr, out, galois_inverse(galois), s);
-}
-
-cudaError_t Context::rescale(const u64* x, int t, u64* out, cudaStream_t s) {
-  if (t < 2) return cudaErrorInvalidValue;
-  const size_t P = (size_t)t * N;
-  FGB_TRY(cudaMemcpyAsync(ws_top_, x + (size_t)(t - 1) * N, sizeof(u64) * N, cudaMemcpyDeviceToDevice, s));
-  FGB_TRY(cudaMemcpyAsync(ws_top_ + N, x + P + (size_t)(t - 1) * N, sizeof(u64) * N, cudaMemcpyDeviceToDevice, s));
-  FGB_TRY(ntt(ws_top_, 2, 1, t - 1, N, true, s));
-  FGB_TRY(launch_rescale_switch(ws_top_, N, ws_rs_, 2, t, N, d_pc, s));
-  FGB_TRY(ntt(ws_rs_, 2, t - 1, 0, (long long)(t - 1) * N, false, s));
-  FGB_TRY(launch_rescale_epilogue(x, (long long)P, ws_rs_, out, 2, t, N, crt, d_pc, s));
-  return cudaSuccess;
+cudaError_t Context::add_batch(const AddReq* reqs, int n, cudaStream_t s) {
+  cudaError_t err = cudaSuccess;
+  for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
+    AddBatch ab{};
+    for (int i = i0; i < n && ab.njobs < kMaxJobs; i++)
+      ab.jobs[ab.njobs++] = AddJob{reqs[i].x, reqs[i].y, reqs[i].out, reqs[i].t, reqs[i].sub ? 1 : 0};
+    err = launch_addsub(ab, ring_, nq, d_pc, s);
+  }
+  return err;
 }
 
 }  // namespace fgb

@@ -44,22 +44,47 @@ class Context {
   PrimeConst* d_pc = nullptr;
 
   // --- primitives on device memory ---
-  cudaError_t ntt(u64* data, int npolys, int limbs, int first_prime, long long poly_stride, bool inverse,
-                  cudaStream_t s);
+  cudaError_t ntt(const u64* src, u64* dst, int npolys, int limbs, int first_prime, long long poly_stride,
+                  bool inverse, cudaStream_t s);
 
-  // Key switch of a (evaluation form, t towers) with `key` ([2][dnum][ntow][N] device).  The results
-  // (ModDown(sum D b) + add0, ModDown(sum D a) + add1) are written to out [2][t][N], permuted by the
-  // automorphism whose inverse Galois element is galois_inv (1 = none).  `out` must not alias the inputs.
-  cudaError_t keyswitch(const u64* a, int t, const u64* key, const u64* add0, const u64* add1, u64* out,
-                        uint32_t galois_inv, cudaStream_t s);
-  // ModUp only (fills the conversion workspace for `t` towers of a); then per key the inner product and ModDown.
-  cudaError_t modup(const u64* a, int t, cudaStream_t s);
-  cudaError_t ks_from_digits(const u64* a, int t, const u64* key, const u64* add0, const u64* add1, u64* out,
-                             uint32_t galois_inv, cudaStream_t s);
+  // One key switch of `a` (evaluation form, t towers) with `key` ([2][dnum][ntow][N]).  Results
+  // (ModDown(sum D b) + add0, ModDown(sum D a) + add1), permuted by the automorphism whose inverse Galois
+  // element is galois_inv (1 = none), go to out [2][t][N]; out must not alias a, add0 or add1.
+  struct KsReq {
+    const u64* a;
+    int t;
+    const u64* key;
+    const u64* add0;
+    const u64* add1;
+    u64* out;
+    uint32_t galois_inv;
+  };
+  // All requests in one pipeline: requests with the same (a, t) share one ModUp (hoisting).
+  cudaError_t keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s);
 
-  cudaError_t mult(const u64* x, const u64* y, int t, const u64* rlk, u64* out, cudaStream_t s);
-  cudaError_t rescale(const u64* x, int t, u64* out, cudaStream_t s);
-  cudaError_t rotate(const u64* x, int t, uint32_t galois, const u64* key, u64* out, cudaStream_t s);
+  struct MultReq {
+    const u64* x;
+    const u64* y;
+    int t;
+    u64* out;
+  };
+  cudaError_t mult_batch(const MultReq* reqs, int n, const u64* rlk, cudaStream_t s);
+
+  struct RescaleReq {
+    const u64* x;
+    int t;
+    u64* out;
+  };
+  cudaError_t rescale_batch(const RescaleReq* reqs, int n, cudaStream_t s);
+
+  struct AddReq {
+    const u64* x;
+    const u64* y;
+    int t;
+    u64* out;
+    bool sub;
+  };
+  cudaError_t add_batch(const AddReq* reqs, int n, cudaStream_t s);
 
   // --- object registry (handles as in api/CryptoContext.hpp:233-246) ---
   std::mutex mu;
@@ -80,15 +105,7 @@ class Context {
   std::vector<void*> owned_;  // device allocations freed at destruction
   void* dmalloc(size_t bytes);
 
-  // workspace sized for t = nq
-  u64* ws_coeff_ = nullptr;  // [nq][N]
-  u64* ws_conv_ = nullptr;   // [dnum][ntow][N]
-  u64* ws_inner_ = nullptr;  // [2][ntow][N]
-  u64* ws_md_ = nullptr;     // [2][nq][N]
-  u64* ws_tensor_ = nullptr; // [3][nq][N]
-  u64* ws_top_ = nullptr;    // [2][N]
-  u64* ws_rs_ = nullptr;     // [2][nq][N]
-  int digits_t_ = 0;         // t of the digits currently held by ws_conv_
+  Ring ring_{};
 };
 
 }  // namespace fgb

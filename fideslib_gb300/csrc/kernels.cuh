@@ -1,4 +1,6 @@
-// Element-wise and basis-conversion kernels of the CKKS key-switching pipeline (launchers).
+// Job-batched kernels of the CKKS evaluation pipeline (launchers).  Every launch carries up to kMaxJobs
+// ciphertext jobs in kernel-parameter space, so a batch of ciphertexts at different levels is one launch per
+// pipeline stage; rows beyond a job's tower count exit immediately.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -6,7 +8,9 @@
 
 namespace fgb {
 
-// CRT tables resident on the device (built once per context; see Context::build_tables).
+constexpr int kMaxJobs = 64;
+
+// CRT tables resident on the device (built once per context, Context::build).
 struct CrtTables {
   int nq, np, alpha, dnum, ntow;
   // ModUp, digit d with s towers: base b = (d*alpha + s-1)*alpha
@@ -20,47 +24,82 @@ struct CrtTables {
   const ulonglong2* rs_qinv;   // [l*nq + i] = {[q_l^-1]_{q_i}, shoup}
 };
 
-struct KsDims {
+struct Ring {
   int N, logN;
-  int t;      // active Q towers
-  int beta;   // digits in use
 };
 
-// coeff: [t][N] coefficient-form input; conv: per digit d rows [t + np - s_d][N] at conv + d*conv_stride.
-cudaError_t launch_modup_conv(const u64* coeff, u64* conv, long long conv_stride, const KsDims& k,
-                              const CrtTables& c, const PrimeConst* pc, cudaStream_t s);
+// One key switch: ModUp(a) (shared by jobs with the same input), inner product with `key`, ModDown of both
+// halves, + add0/add1, automorphism scatter by galois_inv (1 = none) into out.
+struct KsJob {
+  const u64* a;      // [t][N] evaluation form (the digit's own towers are read from here)
+  const u64* add0;   // [t][N] or null
+  const u64* add1;   // [t][N] or null
+  const u64* key;    // [2][dnum][ntow][N] (0 = a vectors, 1 = b vectors)
+  const u64* coeff;  // [t][N] coefficient form of a (ModUp input)
+  u64* conv;         // digit d: conv + d*(t+np)*N, rows = the t - s_d + np converted towers
+  u64* inner;        // [2][t+np][N]
+  u64* md;           // [2][t][N]
+  u64* out;          // [2][t][N]
+  int t;
+  uint32_t galois_inv;
+};
 
-// digits: own towers are read from a_eval, converted towers from conv; key: [2][dnum][nq+np][N] (0 = a, 1 = b).
-// inner: [2][t+np][N], inner[0] = sum D*b, inner[1] = sum D*a.
-cudaError_t launch_ks_inner(const u64* a_eval, const u64* conv, long long conv_stride, const u64* key, u64* inner,
-                            const KsDims& k, const CrtTables& c, const PrimeConst* pc, cudaStream_t s);
+struct KsBatch {
+  int njobs;
+  KsJob jobs[kMaxJobs];
+};
 
-// inner P towers (coefficient form) of npolys polys laid out [poly][t+np][N]: conv_out [poly][t][N] coefficient form.
-cudaError_t launch_moddown_conv(const u64* inner, long long poly_stride_in, u64* conv_out, long long poly_stride_out,
-                                int npolys, const KsDims& k, const CrtTables& c, const PrimeConst* pc, cudaStream_t s);
+// x, y: [2][t][N] -> d: [3][t][N] = (x0y0, x0y1 + x1y0, x1y1)
+struct TensorJob {
+  const u64* x;
+  const u64* y;
+  u64* d;
+  int t;
+};
+struct TensorBatch {
+  int njobs;
+  TensorJob jobs[kMaxJobs];
+};
 
-// out[p][j][sigma(n)] = ((inner[p][j][n] - conv[p][j][n]) * P^-1 + add_p[j][n]) mod q_j, sigma = automorphism
-// scatter for the Galois element whose inverse is `galois_inv` (1 = identity).
-cudaError_t launch_moddown_epilogue(const u64* inner, long long in_stride, const u64* conv, long long conv_stride,
-                                    const u64* add0, const u64* add1, u64* out, long long out_stride, int npolys,
-                                    uint32_t galois_inv, const KsDims& k, const CrtTables& c, const PrimeConst* pc,
+// out = x +/- y over [2][t][N]
+struct AddJob {
+  const u64* x;
+  const u64* y;
+  u64* out;
+  int t;
+  int sub;
+};
+struct AddBatch {
+  int njobs;
+  AddJob jobs[kMaxJobs];
+};
+
+// Rescale of x [2][t][N]: top [2][N] holds INTT of the top towers, tmp [2][t-1][N] the switched copies.
+struct RescaleJob {
+  const u64* x;
+  const u64* top;
+  u64* tmp;
+  u64* out;
+  int t;
+};
+struct RescaleBatch {
+  int njobs;
+  RescaleJob jobs[kMaxJobs];
+};
+
+cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
+                              cudaStream_t s);
+cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
+                            cudaStream_t s);
+cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
+                                cudaStream_t s);
+cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                                     cudaStream_t s);
-
-// (x0, x1) (y0, y1) -> (x0y0, x0y1 + x1y0, x1y1); square when y == x.
-cudaError_t launch_tensor(const u64* x, const u64* y, u64* d, int t, int N, const PrimeConst* pc, cudaStream_t s);
-
-// out = x +/- y over npolys x t towers (same tower layout), element-wise.
-cudaError_t launch_addsub(const u64* x, const u64* y, u64* out, int npolys, int t, int N, bool sub,
-                          const PrimeConst* pc, cudaStream_t s);
-
-// Rescale helpers. top: [npolys][N] coefficient-form top towers (mod q_{t-1}); tmp: [npolys][t-1][N].
-cudaError_t launch_rescale_switch(const u64* top, long long top_stride, u64* tmp, int npolys, int t, int N,
-                                  const PrimeConst* pc, cudaStream_t s);
-// out[p][i] = (x[p][i] - tmp[p][i]) * q_{t-1}^-1 mod q_i, i < t-1.
-cudaError_t launch_rescale_epilogue(const u64* x, long long x_stride, const u64* tmp, u64* out, int npolys, int t,
-                                    int N, const CrtTables& c, const PrimeConst* pc, cudaStream_t s);
-
-// Evaluation-form automorphism (gather): out[brev(j)] = in[brev(((2j+1)galois mod 2N) >> 1)].
-cudaError_t launch_automorph(const u64* in, u64* out, int nlimbs, int N, int logN, uint32_t galois, cudaStream_t s);
+cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, const PrimeConst* pc,
+                                  cudaStream_t s);
+cudaError_t launch_rescale_epilogue(const RescaleBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
+                                    cudaStream_t s);
 
 }  // namespace fgb

@@ -13,8 +13,8 @@
 //     pass C  : stages on bits [3 .. 0]        (16 contiguous residues), then the store to HBM.
 //   inverse (Gentleman–Sande, bit-reversed -> natural, N^-1 applied on the way out) runs the passes in the
 //   reverse order.
-// Butterflies are Harvey-lazy: forward values live in [0, 4p), inverse in [0, 2p); outputs are reduced to
-// [0, p).  Shared memory is XOR-swizzled (word l stored at l ^ ((l >> 5) & 15)) so every pass reads and
+// Butterflies are Harvey-lazy with a cheaper quotient estimate (shoup_lazy4, products in [0, 4p)): forward
+// values live in [0, 8p), inverse in [0, 4p); outputs are reduced to [0, p).  Needs p < 2^61.  Shared memory is XOR-swizzled (word l stored at l ^ ((l >> 5) & 15)) so every pass reads and
 // writes with at most the two-wavefront minimum of 64-bit accesses.
 #include <cooperative_groups.h>
 
@@ -29,33 +29,31 @@ constexpr int kThreads = 256;
 
 __device__ __forceinline__ int swz(int l) { return l ^ ((l >> 5) & 15); }
 
-// X, Y in [0, 4p) -> X + wY, X - wY in [0, 4p).
-__device__ __forceinline__ void ct_bfly(u64& X, u64& Y, const ulonglong2& w, u64 p, u64 p2) {
-  u64 x = X >= p2 ? X - p2 : X;
-  u64 t = shoup_lazy(Y, w.x, w.y, p);
+// Forward (CT): X, Y in [0, 8p) -> X + wY, X - wY + 4p in [0, 8p)  (wY from shoup_lazy4 lies in [0, 4p)).
+__device__ __forceinline__ void ct_bfly(u64& X, u64& Y, const ulonglong2& w, u64 negp, u64 p4) {
+  const u64 x = X >= p4 ? X - p4 : X;
+  const u64 t = shoup_lazy4(Y, w.x, w.y, negp);
   X = x + t;
-  Y = x - t + p2;
+  Y = x - t + p4;
 }
 
-// X, Y in [0, 2p) -> X + Y, (X - Y) w in [0, 2p).
-__device__ __forceinline__ void gs_bfly(u64& X, u64& Y, const ulonglong2& w, u64 p, u64 p2) {
+// Inverse (GS): X, Y in [0, 4p) -> X + Y (reduced below 4p), (X - Y + 4p) w in [0, 4p).
+__device__ __forceinline__ void gs_bfly(u64& X, u64& Y, const ulonglong2& w, u64 negp, u64 p4) {
   u64 s = X + Y;
-  s = s >= p2 ? s - p2 : s;
-  u64 d = X - Y + p2;
+  s = s >= p4 ? s - p4 : s;
+  const u64 d = X - Y + p4;
   X = s;
-  Y = shoup_lazy(d, w.x, w.y, p);
+  Y = shoup_lazy4(d, w.x, w.y, negp);
 }
 
 // Radix-2^LOGR stages over x[k] = a[G*2^(LOGS+LOGR) + k*2^LOGS + low] (low < 2^LOGS).  At the sub-stage on
 // bit kb of k the pair distance is 2^(LOGS+kb), the global stage is s = LOGN-1-(LOGS+kb) and the twiddle of
 // the pair whose lower member is k has table index 2^s + G*2^(LOGR-1-kb) + (k >> (kb+1)).
 template <int LOGR, int LOGS, int LOGN>
-__device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 p,
-                                          u64 p2) {
+__device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 negp,
+                                          u64 p4) {
 #pragma unroll
   for (int kb = LOGR - 1; kb >= 0; kb--) {
-    constexpr int dummy = 0;
-    (void)dummy;
     const int s = LOGN - 1 - (LOGS + kb);
     const int nw = 1 << (LOGR - 1 - kb);
     const ulonglong2* row = tw + (1 << s) + G * nw;
@@ -63,14 +61,14 @@ __device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulon
     for (int k = 0; k < (1 << LOGR); k++) {
       if (k & (1 << kb)) continue;
       const ulonglong2 w = __ldg(row + (k >> (kb + 1)));
-      ct_bfly(x[k], x[k + (1 << kb)], w, p, p2);
+      ct_bfly(x[k], x[k + (1 << kb)], w, negp, p4);
     }
   }
 }
 
 template <int LOGR, int LOGS, int LOGN>
-__device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 p,
-                                          u64 p2) {
+__device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 negp,
+                                          u64 p4) {
 #pragma unroll
   for (int kb = 0; kb < LOGR; kb++) {
     const int s = LOGN - 1 - (LOGS + kb);
@@ -80,28 +78,30 @@ __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulon
     for (int k = 0; k < (1 << LOGR); k++) {
       if (k & (1 << kb)) continue;
       const ulonglong2 w = __ldg(row + (k >> (kb + 1)));
-      gs_bfly(x[k], x[k + (1 << kb)], w, p, p2);
+      gs_bfly(x[k], x[k + (1 << kb)], w, negp, p4);
     }
   }
 }
 
 struct LimbRef {
-  u64* ptr;
+  const u64* src;
+  u64* dst;
   int prime;
+  bool valid;
 };
 
-__device__ __forceinline__ LimbRef locate(const NttBatch& b, int limb, int N) {
-  LimbRef r{nullptr, 0};
-#pragma unroll 1
-  for (int s = 0; s < b.nseg; s++) {
-    const NttSeg& g = b.seg[s];
-    const int n = g.limbs * g.npolys;
-    if (limb >= g.limb_begin && limb < g.limb_begin + n) {
-      const int q = limb - g.limb_begin;
-      const int poly = q / g.limbs, j = q - poly * g.limbs;
-      r.ptr = g.data + poly * g.poly_stride + (long long)j * N;
-      r.prime = g.prime_of[j];
-    }
+// Job blockIdx.z, limb blockIdx.y (uniform over a cluster, so an out-of-range cluster exits as a whole
+// before any cluster barrier).
+__device__ __forceinline__ LimbRef locate(const NttBatch& b, int N) {
+  const NttJob& J = b.jobs[blockIdx.z];
+  const int q = blockIdx.y;
+  LimbRef r{nullptr, nullptr, 0, false};
+  if (q < J.limbs * J.npolys) {
+    const int poly = q / J.limbs, j = q - poly * J.limbs;
+    r.src = J.src + poly * J.src_stride + (long long)j * N;
+    r.dst = J.dst + poly * J.dst_stride + (long long)j * N;
+    r.prime = J.prime_of[j];
+    r.valid = true;
   }
   return r;
 }
@@ -117,13 +117,14 @@ struct Shape {
 };
 
 template <int LOGN>
-__global__ void __launch_bounds__(kThreads) ntt_fwd_kernel(const __grid_constant__ NttBatch b,
-                                                           const __grid_constant__ DeviceTables T, int limb0) {
+__global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_constant__ NttBatch b,
+                                                           const __grid_constant__ DeviceTables T) {
   using S = Shape<LOGN>;
   extern __shared__ __align__(16) u64 sm[];
   const int tid = threadIdx.x;
-  const LimbRef L = locate(b, limb0 + blockIdx.y, S::N);
-  const u64 p = T.pc[L.prime].p, p2 = T.pc[L.prime].p2;
+  const LimbRef L = locate(b, S::N);
+  if (!L.valid) return;
+  const u64 p = T.pc[L.prime].p, p2 = 2 * p, p4 = 4 * p, negp = T.pc[L.prime].negp;
   const ulonglong2* __restrict__ tw = T.tw_fwd + (size_t)L.prime * S::N;
   int h = 0;
 
@@ -137,10 +138,10 @@ __global__ void __launch_bounds__(kThreads) ntt_fwd_kernel(const __grid_constant
     for (int it = 0; it < IT; it++) {
       const int l = c * LPC + it * kThreads + tid;
 #pragma unroll
-      for (int hh = 0; hh < S::C; hh++) x[it][hh] = __ldg(L.ptr + hh * S::E + l);
+      for (int hh = 0; hh < S::C; hh++) x[it][hh] = __ldg(L.src + hh * S::E + l);
     }
 #pragma unroll
-    for (int it = 0; it < IT; it++) fwd_radix<S::LOGC, S::LOGE, LOGN>(x[it], 0, tw, p, p2);
+    for (int it = 0; it < IT; it++) fwd_radix<S::LOGC, S::LOGE, LOGN>(x[it], 0, tw, negp, p4);
     cl.sync();  // every CTA of the cluster is running before its shared memory is written
 #pragma unroll
     for (int it = 0; it < IT; it++) {
@@ -164,9 +165,9 @@ __global__ void __launch_bounds__(kThreads) ntt_fwd_kernel(const __grid_constant
       if constexpr (S::C > 1)
         x[k] = sm[swz(l)];
       else
-        x[k] = (l < S::E) ? __ldg(L.ptr + l) : 0ull;
+        x[k] = (l < S::E) ? __ldg(L.src + l) : 0ull;
     }
-    fwd_radix<S::LOGRA, 8, LOGN>(x, h, tw, p, p2);
+    fwd_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4);
 #pragma unroll
     for (int k = 0; k < R; k++) sm[swz(k * 256 + tid)] = x[k];
   }
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(kThreads) ntt_fwd_kernel(const __grid_constant
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    fwd_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, p, p2);
+    fwd_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -189,27 +190,28 @@ __global__ void __launch_bounds__(kThreads) ntt_fwd_kernel(const __grid_constant
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
-    fwd_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, p, p2);
-    ulonglong2* out = reinterpret_cast<ulonglong2*>(L.ptr + h * S::E + g * 16);
+    fwd_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p4);
+    ulonglong2* out = reinterpret_cast<ulonglong2*>(L.dst + h * S::E + g * 16);
 #pragma unroll
     for (int k = 0; k < 16; k += 2) {
       ulonglong2 v;
-      v.x = csub(csub(x[k], p2), p);
-      v.y = csub(csub(x[k + 1], p2), p);
+      v.x = csub(csub(csub(x[k], p4), p2), p);
+      v.y = csub(csub(csub(x[k + 1], p4), p2), p);
       out[k / 2] = v;
     }
   }
 }
 
 template <int LOGN>
-__global__ void __launch_bounds__(kThreads) ntt_inv_kernel(const __grid_constant__ NttBatch b,
-                                                           const __grid_constant__ DeviceTables T, int limb0) {
+__global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_constant__ NttBatch b,
+                                                           const __grid_constant__ DeviceTables T) {
   using S = Shape<LOGN>;
   extern __shared__ __align__(16) u64 sm[];
   const int tid = threadIdx.x;
-  const LimbRef L = locate(b, limb0 + blockIdx.y, S::N);
+  const LimbRef L = locate(b, S::N);
+  if (!L.valid) return;
   const PrimeConst& pc = T.pc[L.prime];
-  const u64 p = pc.p, p2 = pc.p2, ninv = pc.ninv, ninv_sh = pc.ninv_sh;
+  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp, ninv = pc.ninv, ninv_sh = pc.ninv_sh;
   const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
@@ -217,14 +219,14 @@ __global__ void __launch_bounds__(kThreads) ntt_inv_kernel(const __grid_constant
 #pragma unroll 1
   for (int g = tid; g < S::E / 16; g += kThreads) {  // pass C^-1
     u64 x[16];
-    const ulonglong2* in = reinterpret_cast<const ulonglong2*>(L.ptr + h * S::E + g * 16);
+    const ulonglong2* in = reinterpret_cast<const ulonglong2*>(L.src + h * S::E + g * 16);
 #pragma unroll
     for (int k = 0; k < 16; k += 2) {
       const ulonglong2 v = __ldg(in + k / 2);
       x[k] = v.x;
       x[k + 1] = v.y;
     }
-    inv_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, p, p2);
+    inv_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(g * 16 + k)] = x[k];
   }
@@ -236,7 +238,7 @@ __global__ void __launch_bounds__(kThreads) ntt_inv_kernel(const __grid_constant
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    inv_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, p, p2);
+    inv_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -250,12 +252,12 @@ __global__ void __launch_bounds__(kThreads) ntt_inv_kernel(const __grid_constant
       const int l = k * 256 + tid;
       x[k] = (l < S::E) ? sm[swz(l)] : 0ull;
     }
-    inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, p, p2);
+    inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4);
     if constexpr (S::C == 1) {
 #pragma unroll
       for (int k = 0; k < R; k++) {
         const int l = k * 256 + tid;
-        if (l < S::E) L.ptr[l] = csub(shoup_lazy(x[k], ninv, ninv_sh, p), p);
+        if (l < S::E) L.dst[l] = csub(csub(shoup_lazy4(x[k], ninv, ninv_sh, negp), p2), p);
       }
       return;
     } else {
@@ -279,9 +281,9 @@ __global__ void __launch_bounds__(kThreads) ntt_inv_kernel(const __grid_constant
         const u64* src = cl.map_shared_rank(sm, hh);
         x[hh] = src[swz(l)];
       }
-      inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, p, p2);
+      inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, negp, p4);
 #pragma unroll
-      for (int hh = 0; hh < S::C; hh++) L.ptr[hh * S::E + l] = csub(shoup_lazy(x[hh], ninv, ninv_sh, p), p);
+      for (int hh = 0; hh < S::C; hh++) L.dst[hh * S::E + l] = csub(csub(shoup_lazy4(x[hh], ninv, ninv_sh, negp), p2), p);
     }
     cl.sync();  // peers may still be reading this CTA's shared memory
   }
@@ -298,31 +300,29 @@ cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cud
     if (e != cudaSuccess) return e;
     attr_done[inverse] = true;
   }
-  for (int limb0 = 0; limb0 < b.total_limbs; limb0 += 65535) {
-    const int n = (b.total_limbs - limb0) < 65535 ? (b.total_limbs - limb0) : 65535;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(S::C, n, 1);
-    cfg.blockDim = dim3(kThreads, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = S::C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = S::C > 1 ? 1 : 0;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, b, t, limb0);
-    if (e != cudaSuccess) return e;
-    count_launch();
-  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(S::C, b.max_limbs, b.njobs);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = S::C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, b, t);
+  if (e != cudaSuccess) return e;
+  count_launch();
   return cudaSuccess;
 }
 
 }  // namespace
 
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
-  if (b.total_limbs <= 0) return cudaSuccess;
+  if (b.njobs <= 0 || b.max_limbs <= 0) return cudaSuccess;
+  if (b.njobs > kMaxNttJobs || b.max_limbs > 65535) return cudaErrorInvalidValue;
   switch (t.logN) {
     case 10: return launch_t<10>(b, t, inverse, s);
     case 11: return launch_t<11>(b, t, inverse, s);

@@ -8,33 +8,52 @@
 
 namespace fgb {
 
-// A segment is `npolys` polynomials of `limbs` towers each, tower j of poly k at data + k*poly_stride + j*N,
-// transformed modulo prime index prime_of[j].  A batch launches all limbs of all segments at once.
-struct NttSeg {
-  u64* data;
-  long long poly_stride;
+// One job = `npolys` polynomials of `limbs` towers.  Tower j of poly k is read from
+// src + k*src_stride + j*N and written to dst + k*dst_stride + j*N (src == dst: in place), modulo prime
+// index prime_of[j].  A launch carries up to kMaxNttJobs jobs in kernel-parameter space; every limb of
+// every job is one thread-block cluster.
+struct NttJob {
+  const u64* src;
+  u64* dst;
+  long long src_stride;
+  long long dst_stride;
   int limbs;
   int npolys;
-  int limb_begin;  // first global limb index of this segment (filled by the launcher)
   uint8_t prime_of[64];
 };
 
-constexpr int kMaxNttSegs = 8;
+constexpr int kMaxNttJobs = 64;
 
 struct NttBatch {
-  int nseg;
-  int total_limbs;
-  NttSeg seg[kMaxNttSegs];
+  int njobs;
+  int max_limbs;  // max over jobs of limbs * npolys (grid.y)
+  NttJob jobs[kMaxNttJobs];
 };
 
 struct DeviceTables {
-  const PrimeConst* pc;     // [ntowers]
-  const ulonglong2* tw_fwd; // [ntowers][N] {psi^brev(i), shoup}
-  const ulonglong2* tw_inv; // [ntowers][N] {psi^-brev(i), shoup}
+  const PrimeConst* pc;      // [ntowers]
+  const ulonglong2* tw_fwd;  // [ntowers][N] {psi^brev(i), shoup}
+  const ulonglong2* tw_inv;  // [ntowers][N] {psi^-brev(i), shoup}
   int logN;
 };
 
-// Host launcher: forward (inverse=false: natural -> bit-reversed evaluation order) or inverse.
+// Forward (inverse=false: coefficient -> evaluation, bit-reversed) or inverse transform of every job.
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s);
+
+// Convenience: appends a job; returns false when the batch is full.
+inline bool ntt_add_job(NttBatch& b, const u64* src, u64* dst, long long src_stride, long long dst_stride, int limbs,
+                        int npolys, const uint8_t* prime_of) {
+  if (b.njobs >= kMaxNttJobs || limbs <= 0 || npolys <= 0) return limbs <= 0 || npolys <= 0;
+  NttJob& j = b.jobs[b.njobs++];
+  j.src = src;
+  j.dst = dst;
+  j.src_stride = src_stride;
+  j.dst_stride = dst_stride;
+  j.limbs = limbs;
+  j.npolys = npolys;
+  for (int k = 0; k < limbs; k++) j.prime_of[k] = prime_of[k];
+  if (limbs * npolys > b.max_limbs) b.max_limbs = limbs * npolys;
+  return true;
+}
 
 }  // namespace fgb

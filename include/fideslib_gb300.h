@@ -118,6 +118,22 @@ int fides_eval_rotate(fides_ctx* ctx, uint32_t a, int32_t index, uint32_t* out);
 int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out);
 int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs);
 
+/* Batched evaluation: `n` independent requests (no request may consume another one's output) run together,
+ * one launch per pipeline stage for all ciphertexts of an op family, at whatever level each ciphertext is.
+ * Requests rotating the same input share its ModUp.  On success ops[i].out holds the result handle.
+ * Generalises the reference's cross-ciphertext batching (src/CKKS/LimbPartitionBatch.cu:20-600,
+ * RNSPolyBatch.cpp) to the whole key-switching pipeline. */
+enum { FIDES_OP_ADD = 1, FIDES_OP_SUB = 2, FIDES_OP_MULT = 3, FIDES_OP_SQUARE = 4, FIDES_OP_RESCALE = 5,
+       FIDES_OP_ROTATE = 6, FIDES_OP_AUTOMORPHISM = 7 };
+typedef struct {
+  int32_t op;      /* FIDES_OP_* */
+  uint32_t a;      /* first operand handle */
+  uint32_t b;      /* second operand (ADD / SUB / MULT) */
+  int32_t index;   /* rotation index (ROTATE) or Galois element (AUTOMORPHISM) */
+  uint32_t out;    /* result handle, written by the call */
+} fides_op;
+int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n);
+
 #ifdef __cplusplus
 }
 #endif

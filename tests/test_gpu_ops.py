@@ -121,3 +121,41 @@ def test_errors_are_status_codes(env):
     h1 = env.gpu.load_ciphertext(env.at(1))
     with pytest.raises(F.FidesError):
         env.gpu.rescale(h1)
+
+
+def test_batch_mixed_ops_same_alone_and_in_mix(env):
+    """fides_eval_batch over rotations (two sharing one input), mults, squares, rescales and adds at ragged
+    levels: every output equals the oracle and the same request issued alone."""
+    import fideslib_gb300 as F
+    rng = np.random.default_rng(17)
+    nq = env.nq
+    levels = [nq, max(2, nq - 1), max(2, nq // 2), 2, max(2, nq - 3), nq]
+    hs = {t: env.gpu.load_ciphertext(env.at(t), env.scale) for t in set(levels)}
+    g1, k1 = env.rot_key(1)
+    g2, k2 = env.rot_key(-5)
+    ops, expect = [], []
+    for i, t in enumerate(levels):
+        ct = env.at(t)
+        kind = i % 4
+        if kind == 0:
+            ops.append((F.OP_ROTATE, hs[t], 0, 1))
+            expect.append(env.orc.rotate(ct, g1, k1))
+            ops.append((F.OP_ROTATE, hs[t], 0, -5))  # same input: shared ModUp
+            expect.append(env.orc.rotate(ct, g2, k2))
+        elif kind == 1:
+            ops.append((F.OP_MULT, hs[t], hs[t], 0))
+            expect.append(env.orc.mult(ct, ct, env.rlk))
+        elif kind == 2:
+            ops.append((F.OP_RESCALE, hs[t], 0, 0))
+            expect.append(env.orc.rescale(ct))
+        else:
+            ops.append((F.OP_ADD, hs[t], hs[t], 0))
+            expect.append(env.orc.add(ct, ct))
+        ops.append((F.OP_SQUARE, hs[t], 0, 0))
+        expect.append(env.orc.mult(ct, ct, env.rlk))
+    outs = env.gpu.eval_batch(ops)
+    for o, e, op in zip(outs, expect, ops):
+        got = env.gpu.store_ciphertext(o)
+        assert np.array_equal(got, e), op
+        alone = env.gpu.store_ciphertext(env.gpu.eval_batch([op])[0])
+        assert np.array_equal(alone, got), op
