@@ -72,6 +72,8 @@ _SIGS = {
     "fides_eval_automorphism": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_fast_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, i32p, u32p]),
     "fides_eval_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "fides_eval_rotate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                            C.c_void_p]),
 }
 
 OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM = 1, 2, 3, 4, 5, 6, 7

@@ -58,6 +58,11 @@ int check_ks_shape(fides_ctx* ctx) {
 
 }  // namespace
 
+namespace fgb {
+// Lets other translation units of the library report through fides_last_error().
+int set_last_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace fgb
+
 extern "C" {
 
 const char* fides_last_error(void) { return g_err.c_str(); }

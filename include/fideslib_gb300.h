@@ -134,6 +134,20 @@ typedef struct {
 } fides_op;
 int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n);
 
+/* Allocation-free rotation (no counterpart in the reference).  For callers that cannot allocate device memory
+ * on their request path — a process whose GPU memory is pre-reserved by its own allocator, or a
+ * latency-critical caller that cannot pay for cudaMalloc's implicit synchronisation.  Same result as
+ * fides_eval_automorphism on the ciphertext dev_in (device u64[2][towers][N], evaluation form) with the
+ * context's rotation key for `galois`, written to dev_out (device u64[2][towers][N], must not overlap dev_in).
+ * Its key-switch workspace is a fixed 32 MiB device array inside the library (held by every GPU that loads it),
+ * so it rejects, with FIDES_EINVAL, rotations whose workspace (t + beta(t+np) + 2(t+np) + 2t limbs of 8N bytes)
+ * exceeds 32 MiB, and it calls no cudaMalloc, cudaFree or other allocating routine.  All calls share that array
+ * (it keeps the last call's contents; nothing needs it zeroed): calls whose GPU work overlaps race, so order
+ * them on one stream.  The first call on a device looks up the array's address with that device current; make
+ * it before any stream capture.  `stream` is a cudaStream_t (NULL = the context stream). */
+int fides_eval_rotate_noalloc(fides_ctx* ctx, const uint64_t* dev_in, uint32_t towers, uint32_t galois,
+                              uint64_t* dev_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
