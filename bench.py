@@ -290,6 +290,8 @@ def run_ours(args, rank, world, dist):
     b.synchronize()
     hoisted_ms = a.elapsed_time(b) / reps
 
+    served = None if args.no_served else served_bench(args, dev)
+
     # config 2: batched NTT -> INTT, 16 polys x 40 primes, kernel roofline
     ntt = ntt_bench(args, dev, stream)
     peak, peak_kind = peaks()
@@ -325,9 +327,136 @@ def run_ours(args, rank, world, dist):
                           "ops_per_s": round(32 / (hoisted_ms / 1e3), 2)},
         "ntt_cfg2": ntt["summary"],
         "roofline": ntt["roofline"],
+        "served_cfg4": served,
         "clocks": clocks,
     }
     return result
+
+
+def served_bench(args, dev):
+    """Config 4: Poisson stream of HMult 40% / HRotate 40% / Rescale 10% / Add 10% at levels U{1..29} over two
+    rings (N = 2^15 and 2^16, config-3 moduli), 1000 resident ciphertexts, relin key + 64 rotation keys per ring
+    in HBM.  Served = continuous-batching server (fides_server_*); per-op = the same server with one request at a
+    time.  Both are measured saturated (all requests queued) and under Poisson arrivals at 70% of the per-op
+    saturation rate."""
+    import numpy as np
+    import torch
+
+    import fideslib_gb300 as F
+    mods = moduli_cfg3()
+    rot_idx = [s * (k + 1) for k in range(32) for s in (1, -1)]
+    rings = []
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0x5EED0004)
+    modt = torch.tensor(mods, dtype=torch.int64, device=dev)
+    for logn in (16, 15):
+        n = 1 << logn
+        ctx = F.CryptoContext(logn, mods, NP, DNUM)
+        k = torch.randint(0, 1 << 62, (2, DNUM, NQ + NP, n), dtype=torch.int64, device=dev, generator=gen)
+        k %= modt.view(1, 1, -1, 1)
+        ctx.load_eval_mult_key_device(k.data_ptr())
+        for idx in rot_idx:
+            k = torch.randint(0, 1 << 62, (2, DNUM, NQ + NP, n), dtype=torch.int64, device=dev, generator=gen)
+            k %= modt.view(1, 1, -1, 1)
+            ctx.load_rotation_key_device(ctx.galois(idx), k.data_ptr())
+        del k
+        pool = {t: [] for t in range(1, NQ + 1)}
+        rng = np.random.default_rng(logn)
+        for _ in range(500):
+            t = NQ - int(rng.integers(1, 30))
+            x = torch.randint(0, 1 << 62, (2, t, n), dtype=torch.int64, device=dev, generator=gen)
+            x %= modt[:t].view(1, -1, 1)
+            pool[t].append(ctx.load_ciphertext_device(x.data_ptr(), t))
+        torch.cuda.synchronize()
+        rings.append((ctx, pool))
+
+    rng = np.random.default_rng(0x5EED0004)
+    nreq = 1024
+
+    def make_requests():
+        out = []
+        for _ in range(nreq):
+            r = int(rng.integers(0, 2))
+            ctx, pool = rings[r]
+            u = rng.random()
+            if u < 0.4:
+                code = F.OP_MULT
+            elif u < 0.8:
+                code = F.OP_ROTATE
+            elif u < 0.9:
+                code = F.OP_RESCALE
+            else:
+                code = F.OP_ADD
+            ts = [t for t in pool if pool[t] and (code != F.OP_RESCALE or t >= 2)]
+            t = ts[int(rng.integers(0, len(ts)))]
+            a = pool[t][int(rng.integers(0, len(pool[t])))]
+            b = pool[t][int(rng.integers(0, len(pool[t])))]
+            idx = rot_idx[int(rng.integers(0, len(rot_idx)))] if code == F.OP_ROTATE else 0
+            out.append((r, (code, a, b if code in (F.OP_MULT, F.OP_ADD) else 0, idx)))
+        return out
+
+    def run(reqs, max_batch, inflight, rate):
+        servers = [F.Server(ctx, max_batch=max_batch, max_inflight=inflight, mem_budget=24 << 30) for ctx, _ in rings]
+        warm = [servers[r].submit(*op) for r, op in reqs[:64]]
+        for (r, _), tk in zip(reqs[:64], warm):
+            servers[r].wait(tk)
+            servers[r].release(tk)
+        for sv in servers:
+            sv.reset_stats()
+        t0 = time.perf_counter()
+        gaps = rng.exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
+        due = t0
+        tickets = []
+        for (r, op), g in zip(reqs, gaps):
+            due += g
+            while rate and time.perf_counter() < due:
+                pass
+            tickets.append((r, servers[r].submit(*op)))
+        lat = []
+        for r, tk in tickets:
+            _, l = servers[r].wait(tk)
+            lat.append(l)
+            servers[r].release(tk)
+        wall = time.perf_counter() - t0
+        st = [sv.stats() for sv in servers]
+        for sv in servers:
+            sv.close()
+        lat.sort()
+        return {"ops_per_s": round(len(reqs) / wall, 1), "p50_ms": round(lat[len(lat) // 2], 3),
+                "p99_ms": round(lat[int(0.99 * (len(lat) - 1))], 3),
+                "mean_batch": round(sum(x["mean_batch"] * x["batches"] for x in st) /
+                                    max(1, sum(x["batches"] for x in st)), 2)}
+
+    reqs = make_requests()
+    per_op_sat = run(reqs, 1, 1, None)
+    served_sat = run(reqs, 64, 2, None)
+    rate = 0.7 * per_op_sat["ops_per_s"]
+    per_op_poisson = run(reqs, 1, 1, rate)
+    served_poisson = run(reqs, 64, 2, rate)
+    # single-op latency, unloaded, per op kind on the 2^16 ring
+    single = {}
+    ctx, pool = rings[0]
+    srv = F.Server(ctx, max_batch=1, max_inflight=1, mem_budget=24 << 30)
+    for name, code in (("mult", F.OP_MULT), ("rotate", F.OP_ROTATE), ("rescale", F.OP_RESCALE), ("add", F.OP_ADD)):
+        ls = []
+        for r, op in reqs:
+            if r == 0 and op[0] == code and len(ls) < 16:
+                tk = srv.submit(*op)
+                ls.append(srv.wait(tk)[1])
+                srv.release(tk)
+        ls.sort()
+        single[name] = round(ls[len(ls) // 2], 3) if ls else None
+    srv.close()
+    for ctx, _ in rings:
+        ctx.close()
+    return {"workload": "cfg4: Poisson mix HMult 40 / HRotate 40 / Rescale 10 / Add 10, levels U{1..29}, "
+                        "N in {2^15, 2^16}, 1000 resident cts, relin + 64 rotation keys per ring",
+            "requests": nreq, "saturated": {"served": served_sat, "per_op": per_op_sat,
+                                            "served_over_per_op": round(served_sat["ops_per_s"] /
+                                                                        per_op_sat["ops_per_s"], 2)},
+            "poisson_rate_req_per_s": round(rate, 1),
+            "poisson": {"served": served_poisson, "per_op": per_op_poisson},
+            "single_op_latency_ms_p50_n16": single}
 
 
 def ntt_bench(args, dev, stream):
@@ -429,6 +558,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -56,6 +56,7 @@ _SIGS = {
                                          C.c_void_p]),
     "fides_ntt_batch_host": (C.c_int, [C.c_void_p, u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
     "fides_load_eval_mult_key": (C.c_int, [C.c_void_p, u64p]),
+    "fides_load_eval_mult_key_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fides_load_rotation_key": (C.c_int, [C.c_void_p, C.c_uint32, u64p]),
     "fides_load_rotation_key_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "fides_ct_load": (C.c_int, [C.c_void_p, u64p, C.POINTER(CtMeta), u32p]),
@@ -72,6 +73,14 @@ _SIGS = {
     "fides_eval_automorphism": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_fast_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, i32p, u32p]),
     "fides_eval_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "fides_ctx_get_shape": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fides_server_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "fides_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "fides_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, u32p, C.POINTER(C.c_double)]),
+    "fides_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "fides_server_stats_get": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fides_server_reset_stats": (C.c_int, [C.c_void_p]),
+    "fides_server_destroy": (C.c_int, [C.c_void_p]),
     "fides_eval_rotate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                             C.c_void_p]),
 }
@@ -182,6 +191,9 @@ class CryptoContext:
         key = np.ascontiguousarray(key, dtype=np.uint64)
         _check(lib().fides_load_eval_mult_key(self._h, _p(key)))
 
+    def load_eval_mult_key_device(self, ptr: int):
+        _check(lib().fides_load_eval_mult_key_device(self._h, C.c_void_p(ptr)))
+
     def load_rotation_key(self, galois: int, key: np.ndarray):
         key = np.ascontiguousarray(key, dtype=np.uint64)
         _check(lib().fides_load_rotation_key(self._h, galois, _p(key)))
@@ -270,3 +282,58 @@ class CryptoContext:
 def kernel_launches() -> int:
     """Engine kernels launched by this process so far."""
     return int(lib().fides_kernel_launches())
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("max_batch", C.c_uint32), ("max_inflight_batches", C.c_uint32), ("mem_budget_bytes", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("batches", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("ops_per_s", C.c_double),
+                ("mean_batch", C.c_double)]
+
+
+class Server:
+    """Continuous-batching request server over one context (the C server's worker thread owns the context)."""
+
+    def __init__(self, ctx: CryptoContext, max_batch: int = 64, max_inflight: int = 2, mem_budget: int = 16 << 30):
+        self.ctx = ctx
+        cfg = ServerConfig(max_batch, max_inflight, mem_budget)
+        h = C.c_void_p()
+        _check(lib().fides_server_create(ctx._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def submit(self, code: int, a: int, b: int = 0, index: int = 0) -> int:
+        op = Op(code, a, b, index, 0)
+        t = C.c_uint64()
+        _check(lib().fides_server_submit(self._h, C.byref(op), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int):
+        out = C.c_uint32()
+        lat = C.c_double()
+        _check(lib().fides_server_wait(self._h, ticket, C.byref(out), C.byref(lat)))
+        return out.value, lat.value
+
+    def release(self, ticket: int):
+        _check(lib().fides_server_release(self._h, ticket))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().fides_server_stats_get(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def reset_stats(self):
+        _check(lib().fides_server_reset_stats(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fides_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

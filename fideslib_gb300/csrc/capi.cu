@@ -97,6 +97,14 @@ int fides_ctx_moduli(const fides_ctx* ctx, uint64_t* moduli, uint64_t* roots) {
   return FIDES_OK;
 }
 
+int fides_ctx_get_shape(const fides_ctx* ctx, fides_ctx_shape* shape) {
+  if (!ctx || !ctx->c || !shape) return fail(FIDES_EINVAL, "null argument");
+  const fgb::Context* c = ctx->c;
+  *shape = fides_ctx_shape{(uint32_t)c->N, (uint32_t)c->logN, (uint32_t)c->nq, (uint32_t)c->np, (uint32_t)c->dnum,
+                           (uint32_t)c->alpha};
+  return FIDES_OK;
+}
+
 uint32_t fides_galois_element(const fides_ctx* ctx, int32_t index) {
   if (!ctx || !ctx->c) return 0;
   return fgb::Context::galois_for_index(ctx->c->N, index);
@@ -167,6 +175,11 @@ static int load_key(fides_ctx* ctx, const uint64_t* key, bool device, fgb::u64**
 int fides_load_eval_mult_key(fides_ctx* ctx, const uint64_t* key) {
   if (!valid_ctx(ctx) || !key) return fail(FIDES_EINVAL, "null argument");
   return load_key(ctx, key, false, &ctx->c->relin_key);
+}
+
+int fides_load_eval_mult_key_device(fides_ctx* ctx, const uint64_t* dev_key) {
+  if (!valid_ctx(ctx) || !dev_key) return fail(FIDES_EINVAL, "null argument");
+  return load_key(ctx, dev_key, true, &ctx->c->relin_key);
 }
 
 int fides_load_rotation_key(fides_ctx* ctx, uint32_t galois, const uint64_t* key) {

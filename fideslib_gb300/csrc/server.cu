@@ -1,0 +1,283 @@
+// Continuous-batching request server over one context (C ABI in include/fideslib_gb300.h).
+//
+// The reference has no serving layer (its API runs one op per call, api/CryptoContext.cpp); this is the
+// request loop the engine was shaped for.  Clients submit independent requests from any thread; one worker
+// thread owns the context.  Whenever the GPU can take more work, the worker admits every pending request that
+// fits the memory budget (output ciphertext + key-switch workspace, counted per request) up to max_batch, runs
+// them through fides_eval_batch (one launch per pipeline stage for all of them, at their own levels), and keeps
+// up to max_inflight batches queued on the stream, so requests that arrive while a batch runs are admitted into
+// the next one as soon as slots and memory free up.  Each request's latency is stamped on the host from submit
+// to the completion of its batch's CUDA event.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/fideslib_gb300.h"
+
+namespace fgb {
+int set_last_error(int code, const char* msg);
+}
+
+namespace {
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Req {
+  fides_op op{};
+  double t_submit = 0, t_done = 0;
+  size_t footprint = 0;
+  int state = 0;  // 0 pending, 1 running, 2 done
+  int rc = 0;
+};
+
+struct InFlight {
+  cudaEvent_t ev;
+  std::vector<uint64_t> tickets;
+  size_t footprint;
+};
+
+}  // namespace
+
+struct fides_server {
+  fides_ctx* ctx = nullptr;
+  fides_server_config cfg{};
+  uint32_t N = 0, np = 0, nq = 0, alpha = 1;
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<uint64_t> pending;
+  std::unordered_map<uint64_t, Req> reqs;
+  std::vector<uint32_t> to_free;
+  std::vector<double> latencies;
+  uint64_t next_ticket = 1, batches = 0, batched_ops = 0;
+  double first_submit = -1, last_done = 0;
+  bool stop = false;
+  std::string error;
+
+  size_t footprint_of(const fides_op& op) {
+    fides_ct_meta m{};
+    if (fides_ct_meta_get(ctx, op.a, &m) != FIDES_OK) return 0;
+    const size_t S = (size_t)8 * N, t = m.towers, beta = (t + alpha - 1) / alpha;
+    size_t limbs = 2 * t;  // output
+    if (op.op == FIDES_OP_ROTATE || op.op == FIDES_OP_AUTOMORPHISM || op.op == FIDES_OP_MULT ||
+        op.op == FIDES_OP_SQUARE)
+      limbs += t + beta * (t + np) + 2 * (t + np) + 2 * t;
+    if (op.op == FIDES_OP_MULT || op.op == FIDES_OP_SQUARE) limbs += 3 * t;
+    if (op.op == FIDES_OP_RESCALE) limbs += 2 * t;
+    return limbs * S;
+  }
+
+  // Worker loop: admit -> launch (up to max_inflight batches queued) -> retire completed batches.
+  void run() {
+    cudaStream_t stream = (cudaStream_t)fides_ctx_stream(ctx);
+    std::deque<InFlight> inflight;
+    size_t inflight_bytes = 0;
+    for (;;) {
+      std::vector<uint64_t> take;
+      std::vector<uint32_t> frees;
+      bool idle_wait = false;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        if (stop && pending.empty() && inflight.empty() && to_free.empty()) break;
+        frees.swap(to_free);
+        if (!pending.empty() && inflight.size() < cfg.max_inflight_batches) {
+          size_t budget = inflight_bytes;
+          while (!pending.empty() && take.size() < cfg.max_batch) {
+            Req& r = reqs[pending.front()];
+            if (r.footprint == 0) r.footprint = footprint_of(r.op);  // context is only touched by this thread
+            const bool first = take.empty() && inflight.empty();
+            if (!first && budget + r.footprint > cfg.mem_budget_bytes) break;
+            budget += r.footprint;
+            r.state = 1;
+            take.push_back(pending.front());
+            pending.pop_front();
+          }
+        }
+        idle_wait = take.empty() && frees.empty() && inflight.empty();
+        if (idle_wait) cv_work.wait(lk, [&] { return stop || !pending.empty() || !to_free.empty(); });
+      }
+      if (idle_wait) continue;
+      for (uint32_t h : frees) fides_ct_free(ctx, h);
+      if (!take.empty()) {
+        std::vector<fides_op> ops(take.size());
+        size_t bytes = 0;
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          for (size_t i = 0; i < take.size(); i++) {
+            ops[i] = reqs[take[i]].op;
+            bytes += reqs[take[i]].footprint;
+          }
+        }
+        int rc = fides_eval_batch(ctx, ops.data(), (uint32_t)ops.size());
+        std::vector<int> rcs(ops.size(), rc);
+        if (rc != FIDES_OK && ops.size() > 1)  // one bad request must not fail its batch-mates
+          for (size_t i = 0; i < ops.size(); i++) rcs[i] = fides_eval_batch(ctx, &ops[i], 1);
+        InFlight f;
+        cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming);
+        cudaEventRecord(f.ev, stream);
+        f.tickets = take;
+        f.footprint = bytes;
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          for (size_t i = 0; i < take.size(); i++) {
+            Req& r = reqs[take[i]];
+            r.rc = rcs[i];
+            r.op.out = rcs[i] == FIDES_OK ? ops[i].out : 0;
+          }
+          batches++;
+          batched_ops += take.size();
+        }
+        inflight_bytes += bytes;
+        inflight.push_back(f);
+        continue;
+      }
+      if (inflight.empty()) continue;
+      // Retire the oldest batch.  While it runs, keep admitting new arrivals if a slot is free.
+      bool full;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        full = inflight.size() >= cfg.max_inflight_batches || stop;
+      }
+      if (!full && cudaEventQuery(inflight.front().ev) == cudaErrorNotReady) {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_work.wait_for(lk, std::chrono::microseconds(20), [&] { return !pending.empty() || !to_free.empty(); });
+        continue;
+      }
+      InFlight f = inflight.front();
+      inflight.pop_front();
+      cudaEventSynchronize(f.ev);
+      cudaEventDestroy(f.ev);
+      const double t = now_ms();
+      inflight_bytes -= f.footprint;
+      std::lock_guard<std::mutex> lk(mu);
+      for (uint64_t tk : f.tickets) {
+        Req& r = reqs[tk];
+        r.state = 2;
+        r.t_done = t;
+        latencies.push_back(t - r.t_submit);
+      }
+      last_done = t;
+      cv_done.notify_all();
+    }
+  }
+};
+
+extern "C" {
+
+int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_server** out) {
+  if (!ctx || !cfg || !out) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+  if (cfg->max_batch < 1 || cfg->max_inflight_batches < 1 || cfg->mem_budget_bytes == 0)
+    return fgb::set_last_error(FIDES_EINVAL, "max_batch, max_inflight_batches and mem_budget_bytes must be > 0");
+  fides_server* s = new fides_server();
+  s->ctx = ctx;
+  s->cfg = *cfg;
+  fides_ctx_shape shape{};
+  fides_ctx_get_shape(ctx, &shape);
+  s->N = shape.n;
+  s->nq = shape.nq;
+  s->np = shape.np;
+  s->alpha = shape.alpha ? shape.alpha : 1;
+  s->worker = std::thread([s] { s->run(); });
+  *out = s;
+  return FIDES_OK;
+}
+
+int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket) {
+  if (!s || !op || !ticket) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+  Req r;
+  r.op = *op;
+  r.op.out = 0;
+  r.t_submit = now_ms();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    const uint64_t t = s->next_ticket++;
+    s->reqs[t] = r;
+    s->pending.push_back(t);
+    if (s->first_submit < 0) s->first_submit = r.t_submit;
+    *ticket = t;
+  }
+  s->cv_work.notify_one();
+  return FIDES_OK;
+}
+
+int fides_server_wait(fides_server* s, uint64_t ticket, uint32_t* out, double* latency_ms) {
+  if (!s) return fgb::set_last_error(FIDES_EINVAL, "null server");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return fgb::set_last_error(FIDES_EINVAL, "unknown ticket");
+  s->cv_done.wait(lk, [&] { return s->reqs[ticket].state == 2; });
+  Req& r = s->reqs[ticket];
+  if (out) *out = r.op.out;
+  if (latency_ms) *latency_ms = r.t_done - r.t_submit;
+  return r.rc;
+}
+
+int fides_server_release(fides_server* s, uint64_t ticket) {
+  if (!s) return fgb::set_last_error(FIDES_EINVAL, "null server");
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end() || it->second.state != 2) return fgb::set_last_error(FIDES_EINVAL, "ticket not done");
+    if (it->second.op.out) s->to_free.push_back(it->second.op.out);
+    s->reqs.erase(it);
+  }
+  s->cv_work.notify_one();
+  return FIDES_OK;
+}
+
+int fides_server_stats_get(fides_server* s, fides_server_stats* st) {
+  if (!s || !st) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::vector<double> v = s->latencies;
+  std::sort(v.begin(), v.end());
+  *st = fides_server_stats{};
+  st->completed = v.size();
+  st->batches = s->batches;
+  if (!v.empty()) {
+    st->p50_ms = v[v.size() / 2];
+    st->p99_ms = v[std::min(v.size() - 1, (size_t)(0.99 * (double)v.size()))];
+    double sum = 0;
+    for (double x : v) sum += x;
+    st->mean_ms = sum / (double)v.size();
+    st->max_ms = v.back();
+    const double span = s->last_done - s->first_submit;
+    st->ops_per_s = span > 0 ? (double)v.size() / (span / 1e3) : 0;
+  }
+  st->mean_batch = s->batches ? (double)s->batched_ops / (double)s->batches : 0;
+  return FIDES_OK;
+}
+
+int fides_server_reset_stats(fides_server* s) {
+  if (!s) return fgb::set_last_error(FIDES_EINVAL, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->latencies.clear();
+  s->batches = s->batched_ops = 0;
+  s->first_submit = -1;
+  s->last_done = 0;
+  return FIDES_OK;
+}
+
+int fides_server_destroy(fides_server* s) {
+  if (!s) return FIDES_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  delete s;  // results that were not released stay in the context, owned by the caller
+  return FIDES_OK;
+}
+
+}  // extern "C"

@@ -79,6 +79,11 @@ int fides_synchronize(fides_ctx* ctx);
  * LimbPartition / Stream (src/CudaUtils.cuh:98-160). */
 void* fides_ctx_stream(fides_ctx* ctx);
 int fides_ctx_set_stream(fides_ctx* ctx, void* stream);
+/* Ring and basis shape of a context. */
+typedef struct {
+  uint32_t n, log_n, nq, np, dnum, alpha;
+} fides_ctx_shape;
+int fides_ctx_get_shape(const fides_ctx* ctx, fides_ctx_shape* shape);
 /* Number of engine kernels launched by this process so far (all contexts). */
 uint64_t fides_kernel_launches(void);
 
@@ -96,6 +101,7 @@ int fides_ntt_batch_host(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint32
  * src/CKKS/KeySwitchingKey.cu:19-34, RawCiphertext.cu:672-760).  The rotation key is registered under its
  * Galois element. */
 int fides_load_eval_mult_key(fides_ctx* ctx, const uint64_t* key);
+int fides_load_eval_mult_key_device(fides_ctx* ctx, const uint64_t* dev_key);
 int fides_load_rotation_key(fides_ctx* ctx, uint32_t galois, const uint64_t* key);
 int fides_load_rotation_key_device(fides_ctx* ctx, uint32_t galois, const uint64_t* dev_key);
 
@@ -147,6 +153,33 @@ int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n);
  * it before any stream capture.  `stream` is a cudaStream_t (NULL = the context stream). */
 int fides_eval_rotate_noalloc(fides_ctx* ctx, const uint64_t* dev_in, uint32_t towers, uint32_t galois,
                               uint64_t* dev_out, void* stream);
+
+/* Continuous-batching request server over one context (no counterpart in the reference, whose API runs one op
+ * per call).  One worker thread owns the context: while a server runs, use the context only through it.
+ * Clients on any thread submit independent requests (operands must be resident ciphertext handles); the worker
+ * admits every pending request that fits `mem_budget_bytes` (output + key-switch workspace per request) up to
+ * `max_batch`, runs them with fides_eval_batch, and keeps up to `max_inflight_batches` batches queued on the GPU,
+ * so arrivals during a batch join the next one.  Latency = submit to completion of the request's batch. */
+typedef struct fides_server fides_server;
+typedef struct {
+  uint32_t max_batch;
+  uint32_t max_inflight_batches;
+  uint64_t mem_budget_bytes;
+} fides_server_config;
+typedef struct {
+  uint64_t completed, batches;
+  double p50_ms, p99_ms, mean_ms, max_ms, ops_per_s, mean_batch;
+} fides_server_stats;
+int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_server** out);
+int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket);
+/* Blocks until the request finished; returns its status and result handle. */
+int fides_server_wait(fides_server* s, uint64_t ticket, uint32_t* out, double* latency_ms);
+/* Frees the request's result ciphertext (done by the worker) and forgets the ticket. */
+int fides_server_release(fides_server* s, uint64_t ticket);
+int fides_server_stats_get(fides_server* s, fides_server_stats* st);
+int fides_server_reset_stats(fides_server* s);
+/* Drains pending work and stops the worker; results not released stay in the context (caller-owned). */
+int fides_server_destroy(fides_server* s);
 
 #ifdef __cplusplus
 }
