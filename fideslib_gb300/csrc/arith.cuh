@@ -73,8 +73,34 @@ __device__ __forceinline__ u64 reduce128(u64 hi, u64 lo, const PrimeConst& c) {
   return csub(s, c.p);
 }
 
+// y mod p in [0, 4p) for any y < 2^64: the w = 1 case of shoup_lazy4 (quotient hi64(floor(2^64/p) * y) from the
+// three high partial products, remainder y + q * (2^64 - p)).
+__device__ __forceinline__ u64 reduce64_lazy4(u64 y, u64 one_sh, u64 negp) {
+  u64 r;
+  asm("{\n\t.reg .u32 y0,y1,s0,s1,n0,n1,t1,t2,q0,q1,r0,r1,c0,c1;\n\t.reg .u64 q,acc;\n\t"
+      "mov.b64 {y0,y1}, %1;\n\tmov.b64 {s0,s1}, %2;\n\tmov.b64 {n0,n1}, %3;\n\t"
+      "mul.hi.u32 t1, s1, y0;\n\tmul.hi.u32 t2, s0, y1;\n\t"
+      "add.cc.u32 c0, t1, t2;\n\taddc.u32 c1, 0, 0;\n\tmov.b64 acc, {c0,c1};\n\t"
+      "mad.wide.u32 q, s1, y1, acc;\n\tmov.b64 {q0,q1}, q;\n\t"
+      "mad.wide.u32 acc, q0, n0, %1;\n\tmov.b64 {r0,r1}, acc;\n\t"
+      "mad.lo.u32 r1, q0, n1, r1;\n\tmad.lo.u32 r1, q1, n0, r1;\n\tmov.b64 %0, {r0,r1};\n\t}"
+      : "=l"(r)
+      : "l"(y), "l"(one_sh), "l"(negp));
+  return r;
+}
+
+// z = hi*2^64 + lo reduced to [0, p): hi*[2^64 mod p] and lo each in [0, 4p), sum in [0, 8p), three corrections.
+__device__ __forceinline__ u64 reduce128_fast(u64 hi, u64 lo, const PrimeConst& c) {
+  const u64 a = shoup_lazy4(hi, c.r64, c.r64_sh, c.negp);
+  const u64 b = reduce64_lazy4(lo, c.one_sh, c.negp);
+  u64 s = a + b;
+  s = csub(s, c.p2 << 1);
+  s = csub(s, c.p2);
+  return csub(s, c.p);
+}
+
 __device__ __forceinline__ u64 mul_mod(u64 a, u64 b, const PrimeConst& c) {
-  return reduce128(mulhi(a, b), a * b, c);
+  return reduce128_fast(mulhi(a, b), a * b, c);
 }
 
 // 128-bit accumulator helpers.

@@ -61,9 +61,51 @@ __device__ __forceinline__ int conv_tower(int jj, int start, int s, int t, int n
 }
 
 // ---------------------------------------------------------------------------------------------------------
+// Basis conversion core: for one coefficient, outputs sum_{i<S} y_i * c_{i,jj} mod m_jj for jj < nout, with the
+// S inputs y_i (already multiplied by the Qhat^-1 / Phat^-1 factor) held in registers as 30-bit halves and the
+// constants c_{i,jj} staged in shared memory as 30-bit halves.  S is a compile-time constant so no multiply-add
+// is issued for absent towers.
+template <int S, class TowerOf>
+__device__ __forceinline__ void conv_rows(const uint32_t (&yl)[S], const uint32_t (&yh)[S], const uint2* cs, int nout,
+                                          u64* out, size_t stride, const PrimeConst* __restrict__ pc, TowerOf tower_of) {
+#pragma unroll 1
+  for (int jj = 0; jj < nout; jj++) {
+    u64 hi = 0, lo = 0;
+#pragma unroll
+    for (int i0 = 0; i0 < S; i0 += 16) {
+      Acc4 A{0, 0, 0, 0};
+#pragma unroll
+      for (int i = i0; i < i0 + 16 && i < S; i++) {
+        const uint2 cc = cs[i * nout + jj];
+        acc4_mac(A, yl[i], yh[i], cc.x, cc.y);
+      }
+      acc4_fold(A, hi, lo);
+    }
+    out[(size_t)jj * stride] = reduce128_fast(hi, lo, pc[tower_of(jj)]);
+  }
+}
+
+template <int S>
+__device__ __forceinline__ void modup_body(const KsJob& J, const Ring& r, const CrtTables& c,
+                                           const PrimeConst* __restrict__ pc, int d, int start, int t, int nout,
+                                           int base, const uint2* cs) {
+  const int n = blockIdx.x * kT + threadIdx.x;
+  uint32_t yl[S], yh[S];
+#pragma unroll
+  for (int i = 0; i < S; i++) {
+    const ulonglong2 w = c.mu_qhinv[base + i];
+    const u64 y = shoup(J.coeff[(size_t)(start + i) * r.N + n], w.x, w.y, pc[start + i].p);
+    yl[i] = (uint32_t)(y & kMask30);
+    yh[i] = (uint32_t)(y >> 30);
+  }
+  const int nq = c.nq;
+  conv_rows<S>(yl, yh, cs, nout, J.conv + (size_t)d * (t + c.np) * r.N + n, (size_t)r.N, pc,
+               [=](int jj) { return conv_tower(jj, start, S, t, nq); });
+}
+
 // ModUp basis conversion: grid (N/256, dnum, njobs), one thread per coefficient, all converted rows of one
 // digit.  The digit's 30-bit-sliced [Qhat_i]_{m_j} constants are staged in shared memory.
-template <int MAXS>
+template <bool WIDE>
 __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                         const PrimeConst* __restrict__ pc) {
   extern __shared__ uint2 cs[];
@@ -80,41 +122,33 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
     cs[idx] = make_uint2(src[0], src[1]);
   }
   __syncthreads();
-  const int n = blockIdx.x * kT + threadIdx.x;
-  uint32_t yl[MAXS], yh[MAXS];
-#pragma unroll
-  for (int i = 0; i < MAXS; i++) {
-    if (i < s) {
-      const ulonglong2 w = c.mu_qhinv[base + i];
-      const u64 y = shoup(J.coeff[(size_t)(start + i) * r.N + n], w.x, w.y, pc[start + i].p);
-      yl[i] = (uint32_t)(y & kMask30);
-      yh[i] = (uint32_t)(y >> 30);
-    } else {
-      yl[i] = 0;
-      yh[i] = 0;
+#define FGB_MODUP_CASE(S_) \
+  case S_:                 \
+    modup_body<S_>(J, r, c, pc, d, start, t, nout, base, cs); \
+    break;
+  if constexpr (!WIDE) {  // digits of at most 16 towers (kept separate so the common case stays register-light)
+    switch (s) {
+      FGB_MODUP_CASE(1) FGB_MODUP_CASE(2) FGB_MODUP_CASE(3) FGB_MODUP_CASE(4) FGB_MODUP_CASE(5) FGB_MODUP_CASE(6)
+      FGB_MODUP_CASE(7) FGB_MODUP_CASE(8) FGB_MODUP_CASE(9) FGB_MODUP_CASE(10) FGB_MODUP_CASE(11)
+      FGB_MODUP_CASE(12) FGB_MODUP_CASE(13) FGB_MODUP_CASE(14) FGB_MODUP_CASE(15) FGB_MODUP_CASE(16)
+      default:  // not reached: launch_modup_conv routes other sizes to the wide variant
+        break;
+    }
+  } else {
+    switch (s) {
+      FGB_MODUP_CASE(1) FGB_MODUP_CASE(2) FGB_MODUP_CASE(3) FGB_MODUP_CASE(4) FGB_MODUP_CASE(5) FGB_MODUP_CASE(6)
+      FGB_MODUP_CASE(7) FGB_MODUP_CASE(8) FGB_MODUP_CASE(9) FGB_MODUP_CASE(10) FGB_MODUP_CASE(11)
+      FGB_MODUP_CASE(12) FGB_MODUP_CASE(13) FGB_MODUP_CASE(14) FGB_MODUP_CASE(15) FGB_MODUP_CASE(16)
+      FGB_MODUP_CASE(20) FGB_MODUP_CASE(24) FGB_MODUP_CASE(28) FGB_MODUP_CASE(32)
+      default:  // not reached: launch_modup_conv rejects digit sizes without a compiled body
+        break;
     }
   }
-  u64* out = J.conv + (size_t)d * (t + c.np) * r.N + n;
-#pragma unroll 1
-  for (int jj = 0; jj < nout; jj++) {
-    u64 hi = 0, lo = 0;
-#pragma unroll
-    for (int i0 = 0; i0 < MAXS; i0 += 16) {
-      Acc4 A{0, 0, 0, 0};
-#pragma unroll
-      for (int i = i0; i < i0 + 16 && i < MAXS; i++) {
-        if (i < s) {
-          const uint2 cc = cs[i * nout + jj];
-          acc4_mac(A, yl[i], yh[i], cc.x, cc.y);
-        }
-      }
-      acc4_fold(A, hi, lo);
-    }
-    out[(size_t)jj * r.N] = reduce128(hi, lo, pc[conv_tower(jj, start, s, t, c.nq)]);
-  }
+#undef FGB_MODUP_CASE
 }
 
-// Key inner product: grid (N/256, nq+np, njobs), row j of the extended basis Q_t ∪ P.
+// Key inner product: grid (N/256, nq+np, njobs), row j of the extended basis Q_t ∪ P.  Digits and key values
+// are split into 30-bit halves and accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max).
 __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                       const PrimeConst* __restrict__ pc) {
   const KsJob& J = b.jobs[blockIdx.z];
@@ -125,7 +159,7 @@ __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ Ks
   const int n = blockIdx.x * kT + threadIdx.x;
   const size_t N = r.N;
   const int beta = (t + c.alpha - 1) / c.alpha;
-  U128 acc0{0, 0}, acc1{0, 0};
+  Acc4 A0{0, 0, 0, 0}, A1{0, 0, 0, 0};
 #pragma unroll 1
   for (int d = 0; d < beta; d++) {
     const int start = d * c.alpha;
@@ -139,22 +173,26 @@ __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ Ks
     }
     const u64 ka = J.key[((size_t)(0 * c.dnum + d) * c.ntow + tower) * N + n];
     const u64 kb = J.key[((size_t)(1 * c.dnum + d) * c.ntow + tower) * N + n];
-    mac(acc0, D, kb);
-    mac(acc1, D, ka);
+    const uint32_t dl = (uint32_t)(D & kMask30), dh = (uint32_t)(D >> 30);
+    acc4_mac(A0, dl, dh, (uint32_t)(kb & kMask30), (uint32_t)(kb >> 30));
+    acc4_mac(A1, dl, dh, (uint32_t)(ka & kMask30), (uint32_t)(ka >> 30));
   }
+  u64 h0 = 0, l0 = 0, h1 = 0, l1 = 0;
+  acc4_fold(A0, h0, l0);
+  acc4_fold(A1, h1, l1);
   const PrimeConst& P = pc[tower];
-  J.inner[(size_t)j * N + n] = reduce128(acc0.hi, acc0.lo, P);
-  J.inner[((size_t)ext + j) * N + n] = reduce128(acc1.hi, acc1.lo, P);
+  J.inner[(size_t)j * N + n] = reduce128_fast(h0, l0, P);
+  J.inner[((size_t)ext + j) * N + n] = reduce128_fast(h1, l1, P);
 }
 
 // ModDown basis conversion P -> Q_t: grid (N/256, 2, njobs); reads the (coefficient-form) P rows of inner.
-template <int MAXK>
+template <int K>
 __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                           const PrimeConst* __restrict__ pc) {
-  extern __shared__ uint2 cs[];  // [np][t]
+  extern __shared__ uint2 cs[];  // [K][t]
   const KsJob& J = b.jobs[blockIdx.z];
-  const int np = c.np, t = J.t, ext = t + np;
-  for (int idx = threadIdx.x; idx < np * t; idx += kT) {
+  const int t = J.t, ext = t + K;
+  for (int idx = threadIdx.x; idx < K * t; idx += kT) {
     const int kk = idx / t, j = idx - kk * t;
     const uint32_t* src = c.md_phat + ((size_t)kk * c.nq + j) * 2;
     cs[idx] = make_uint2(src[0], src[1]);
@@ -163,37 +201,15 @@ __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant_
   const int poly = blockIdx.y;
   const int n = blockIdx.x * kT + threadIdx.x;
   const u64* x = J.inner + ((size_t)poly * ext + t) * r.N + n;
-  uint32_t yl[MAXK], yh[MAXK];
+  uint32_t yl[K], yh[K];
 #pragma unroll
-  for (int i = 0; i < MAXK; i++) {
-    if (i < np) {
-      const ulonglong2 w = c.md_phinv[i];
-      const u64 y = shoup(x[(size_t)i * r.N], w.x, w.y, pc[c.nq + i].p);
-      yl[i] = (uint32_t)(y & kMask30);
-      yh[i] = (uint32_t)(y >> 30);
-    } else {
-      yl[i] = 0;
-      yh[i] = 0;
-    }
+  for (int i = 0; i < K; i++) {
+    const ulonglong2 w = c.md_phinv[i];
+    const u64 y = shoup(x[(size_t)i * r.N], w.x, w.y, pc[c.nq + i].p);
+    yl[i] = (uint32_t)(y & kMask30);
+    yh[i] = (uint32_t)(y >> 30);
   }
-  u64* out = J.md + (size_t)poly * t * r.N + n;
-#pragma unroll 1
-  for (int j = 0; j < t; j++) {
-    u64 hi = 0, lo = 0;
-#pragma unroll
-    for (int i0 = 0; i0 < MAXK; i0 += 16) {
-      Acc4 A{0, 0, 0, 0};
-#pragma unroll
-      for (int i = i0; i < i0 + 16 && i < MAXK; i++) {
-        if (i < np) {
-          const uint2 cc = cs[i * t + j];
-          acc4_mac(A, yl[i], yh[i], cc.x, cc.y);
-        }
-      }
-      acc4_fold(A, hi, lo);
-    }
-    out[(size_t)j * r.N] = reduce128(hi, lo, pc[j]);
-  }
+  conv_rows<K>(yl, yh, cs, t, J.md + (size_t)poly * t * r.N + n, (size_t)r.N, pc, [](int j) { return j; });
 }
 
 // out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/256, nq, 2*njobs).
@@ -292,15 +308,18 @@ int max_t(const B& b) {
 cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                               cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
+  if (c.alpha > 16 && c.alpha != 20 && c.alpha != 24 && c.alpha != 28 && c.alpha != 32) return cudaErrorInvalidValue;
+  for (int i = 0; i < b.njobs; i++) {  // partial last digits must have a compiled size
+    const int tt = b.jobs[i].t, last = tt - ((tt - 1) / c.alpha) * c.alpha;
+    if (last > 16 && last != 20 && last != 24 && last != 28 && last != 32) return cudaErrorInvalidValue;
+  }
   const int mt = max_t(b);
   const size_t smem = sizeof(uint2) * c.alpha * (mt + c.np);
   dim3 grid(r.N / kT, c.dnum, b.njobs);
   if (c.alpha <= 16)
-    modup_conv_kernel<16><<<grid, kT, smem, s>>>(b, r, c, pc);
-  else if (c.alpha <= 32)
-    modup_conv_kernel<32><<<grid, kT, smem, s>>>(b, r, c, pc);
+    modup_conv_kernel<false><<<grid, kT, smem, s>>>(b, r, c, pc);
   else
-    return cudaErrorInvalidValue;
+    modup_conv_kernel<true><<<grid, kT, smem, s>>>(b, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -319,12 +338,18 @@ cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables
   if (b.njobs <= 0) return cudaSuccess;
   const size_t smem = sizeof(uint2) * c.np * max_t(b);
   dim3 grid(r.N / kT, 2, b.njobs);
-  if (c.np <= 16)
-    moddown_conv_kernel<16><<<grid, kT, smem, s>>>(b, r, c, pc);
-  else if (c.np <= 32)
-    moddown_conv_kernel<32><<<grid, kT, smem, s>>>(b, r, c, pc);
-  else
-    return cudaErrorInvalidValue;
+  switch (c.np) {
+#define FGB_MD_CASE(K_)                                                    \
+  case K_:                                                                 \
+    moddown_conv_kernel<K_><<<grid, kT, smem, s>>>(b, r, c, pc);          \
+    break;
+    FGB_MD_CASE(1) FGB_MD_CASE(2) FGB_MD_CASE(3) FGB_MD_CASE(4) FGB_MD_CASE(5) FGB_MD_CASE(6) FGB_MD_CASE(7)
+    FGB_MD_CASE(8) FGB_MD_CASE(9) FGB_MD_CASE(10) FGB_MD_CASE(11) FGB_MD_CASE(12) FGB_MD_CASE(13)
+    FGB_MD_CASE(14) FGB_MD_CASE(15) FGB_MD_CASE(16) FGB_MD_CASE(20) FGB_MD_CASE(24) FGB_MD_CASE(32)
+#undef FGB_MD_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
   count_launch();
   return cudaGetLastError();
 }

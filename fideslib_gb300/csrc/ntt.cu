@@ -131,6 +131,10 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_const
   if constexpr (S::C > 1) {
     cg::cluster_group cl = cg::this_cluster();
     const int c = (int)cl.block_rank();
+    // "every CTA of the cluster is running" is all the first barrier has to establish (no data is exchanged
+    // yet), so it is a relaxed arrive here and a wait just before the distributed-shared-memory stores,
+    // overlapping the barrier with the loads and the first butterflies.
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
     constexpr int LPC = S::E / S::C;
     constexpr int IT = LPC / kThreads;
     u64 x[IT][S::C];
@@ -142,7 +146,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_const
     }
 #pragma unroll
     for (int it = 0; it < IT; it++) fwd_radix<S::LOGC, S::LOGE, LOGN>(x[it], 0, tw, negp, p4);
-    cl.sync();  // every CTA of the cluster is running before its shared memory is written
+    asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
 #pragma unroll
     for (int it = 0; it < IT; it++) {
       const int l = c * LPC + it * kThreads + tid;

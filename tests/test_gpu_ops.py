@@ -159,3 +159,34 @@ def test_batch_mixed_ops_same_alone_and_in_mix(env):
         assert np.array_equal(got, e), op
         alone = env.gpu.store_ciphertext(env.gpu.eval_batch([op])[0])
         assert np.array_equal(alone, got), op
+
+
+def test_batched_rotations_full_ring_cfg3(engine_lib):
+    """Config-3 shape at full size: N=2^16, 30 Q towers (60 + 29x50 bits), 10 special 60-bit primes, dnum=3.
+    Four ciphertexts at levels 0, 13, 21, 28 rotated in one batch (two of them twice, sharing a ModUp):
+    every residue bit-identical to the oracle."""
+    import fideslib_gb300 as F
+    logN = 16
+    N = 1 << logN
+    mods = O.make_moduli(logN, [60] + [50] * 29, [60] * 10)
+    gpu = F.CryptoContext(logN, mods, 10, 3)
+    orc = O.Ctx(N, 30, 10, 3, mods, threads=16)
+    rng = np.random.default_rng(0x5EED0003)
+    keys = {}
+    for idx in (1, -16, 1024):
+        g = orc.galois(idx)
+        k = np.zeros(orc.key_shape(), dtype=np.uint64)
+        for j in range(40):
+            k[:, :, j] = rng.integers(0, mods[j], (2, 3, N), dtype=np.uint64)
+        keys[idx] = (g, k)
+        gpu.load_rotation_key(g, k)
+    cts, ops = {}, []
+    for t in (30, 17, 9, 2):
+        ct = np.stack([np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(t)]) for _ in range(2)])
+        cts[t] = (ct, gpu.load_ciphertext(ct))
+    plan = [(30, 1), (30, -16), (17, 1024), (9, 1), (2, -16), (2, 1024)]
+    outs = gpu.eval_batch([(F.OP_ROTATE, cts[t][1], 0, idx) for t, idx in plan])
+    for (t, idx), o in zip(plan, outs):
+        g, k = keys[idx]
+        assert np.array_equal(gpu.store_ciphertext(o), orc.rotate(cts[t][0], g, k)), (t, idx)
+    gpu.close()
