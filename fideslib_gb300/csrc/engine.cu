@@ -371,7 +371,7 @@ struct NttQueue {
   void flush() {
     if (err == cudaSuccess && b.njobs > 0) err = launch_ntt(b, tabs, inverse, s);
     b.njobs = 0;
-    b.max_limbs = 0;
+    b.limb_begin[0] = 0;
   }
 };
 

@@ -13,6 +13,7 @@
 #include <atomic>
 
 #include "kernels.cuh"
+#include "ntt.cuh"
 
 namespace fgb {
 
@@ -109,8 +110,9 @@ template <bool WIDE>
 __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                         const PrimeConst* __restrict__ pc) {
   extern __shared__ uint2 cs[];
-  const KsJob& J = b.jobs[blockIdx.z];
-  const int t = J.t, d = blockIdx.y;
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const KsJob& J = b.jobs[z];
+  const int t = J.t, d = (int)blockIdx.y - b.row_begin[z];
   const int start = d * c.alpha;
   if (start >= t) return;
   const int s = min(c.alpha, t - start);
@@ -151,8 +153,9 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
 // are split into 30-bit halves and accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max).
 __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                       const PrimeConst* __restrict__ pc) {
-  const KsJob& J = b.jobs[blockIdx.z];
-  const int t = J.t, j = blockIdx.y;
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const KsJob& J = b.jobs[z];
+  const int t = J.t, j = (int)blockIdx.y - b.row_begin[z];
   const int ext = t + c.np;
   if (j >= ext) return;
   const int tower = j < t ? j : c.nq + (j - t);
@@ -190,7 +193,8 @@ template <int K>
 __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                           const PrimeConst* __restrict__ pc) {
   extern __shared__ uint2 cs[];  // [K][t]
-  const KsJob& J = b.jobs[blockIdx.z];
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const KsJob& J = b.jobs[z];
   const int t = J.t, ext = t + K;
   for (int idx = threadIdx.x; idx < K * t; idx += kT) {
     const int kk = idx / t, j = idx - kk * t;
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant_
     cs[idx] = make_uint2(src[0], src[1]);
   }
   __syncthreads();
-  const int poly = blockIdx.y;
+  const int poly = (int)blockIdx.y - b.row_begin[z];
   const int n = blockIdx.x * kT + threadIdx.x;
   const u64* x = J.inner + ((size_t)poly * ext + t) * r.N + n;
   uint32_t yl[K], yh[K];
@@ -215,10 +219,10 @@ __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant_
 // out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/256, nq, 2*njobs).
 __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_constant__ KsBatch b, Ring r,
                                                               CrtTables c, const PrimeConst* __restrict__ pc) {
-  const KsJob& J = b.jobs[blockIdx.z >> 1];
-  const int poly = blockIdx.z & 1;
-  const int t = J.t, j = blockIdx.y;
-  if (j >= t) return;
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const KsJob& J = b.jobs[z];
+  const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
+  const int poly = row >= t ? 1 : 0, j = row - poly * t;
   const int n = blockIdx.x * kT + threadIdx.x;
   const size_t N = r.N;
   const u64 q = pc[j].p;
@@ -239,9 +243,9 @@ __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_const
 
 __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ TensorBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
-  const TensorJob& J = b.jobs[blockIdx.z];
-  const int j = blockIdx.y;
-  if (j >= J.t) return;
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const TensorJob& J = b.jobs[z];
+  const int j = (int)blockIdx.y - b.row_begin[z];
   const size_t o = (size_t)j * r.N + blockIdx.x * kT + threadIdx.x;
   const size_t P = (size_t)J.t * r.N;
   const PrimeConst& c = pc[j];
@@ -253,9 +257,9 @@ __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ Tens
 
 __global__ void __launch_bounds__(kT) addsub_kernel(const __grid_constant__ AddBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
-  const AddJob& J = b.jobs[blockIdx.z];
-  const int j = blockIdx.y;
-  if (j >= J.t) return;
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const AddJob& J = b.jobs[z];
+  const int j = (int)blockIdx.y - b.row_begin[z];
   const u64 p = pc[j].p;
 #pragma unroll
   for (int poly = 0; poly < 2; poly++) {
@@ -267,10 +271,10 @@ __global__ void __launch_bounds__(kT) addsub_kernel(const __grid_constant__ AddB
 // OpenFHE NativeVector::SwitchModulus: values above om/2 are lifted to v - om before reduction mod nm.
 __global__ void __launch_bounds__(kT) rescale_switch_kernel(const __grid_constant__ RescaleBatch b, Ring r,
                                                             const PrimeConst* __restrict__ pc) {
-  const RescaleJob& J = b.jobs[blockIdx.z >> 1];
-  const int poly = blockIdx.z & 1;
-  const int t = J.t, i = blockIdx.y;
-  if (i >= t - 1) return;
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const RescaleJob& J = b.jobs[z];
+  const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
+  const int poly = row >= t - 1 ? 1 : 0, i = row - poly * (t - 1);
   const int n = blockIdx.x * kT + threadIdx.x;
   const PrimeConst& om = pc[t - 1];
   const PrimeConst& nm = pc[i];
@@ -284,10 +288,10 @@ __global__ void __launch_bounds__(kT) rescale_switch_kernel(const __grid_constan
 
 __global__ void __launch_bounds__(kT) rescale_epilogue_kernel(const __grid_constant__ RescaleBatch b, Ring r,
                                                               CrtTables c, const PrimeConst* __restrict__ pc) {
-  const RescaleJob& J = b.jobs[blockIdx.z >> 1];
-  const int poly = blockIdx.z & 1;
-  const int t = J.t, i = blockIdx.y;
-  if (i >= t - 1) return;
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const RescaleJob& J = b.jobs[z];
+  const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
+  const int poly = row >= t - 1 ? 1 : 0, i = row - poly * (t - 1);
   const int n = blockIdx.x * kT + threadIdx.x;
   const u64 q = pc[i].p;
   const ulonglong2 w = c.rs_qinv[(size_t)(t - 1) * c.nq + i];
@@ -303,6 +307,15 @@ int max_t(const B& b) {
   return m;
 }
 
+// Copy of a batch with row_begin filled for `rows(job)` rows per job; returns the total row count.
+template <class B, class F>
+int with_rows(const B& in, B& out, F rows) {
+  out = in;
+  out.row_begin[0] = 0;
+  for (int i = 0; i < in.njobs; i++) out.row_begin[i + 1] = out.row_begin[i] + rows(in.jobs[i]);
+  return out.row_begin[in.njobs];
+}
+
 }  // namespace
 
 cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
@@ -315,11 +328,14 @@ cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& 
   }
   const int mt = max_t(b);
   const size_t smem = sizeof(uint2) * c.alpha * (mt + c.np);
-  dim3 grid(r.N / kT, c.dnum, b.njobs);
+  KsBatch bb;
+  const int alpha = c.alpha;
+  const int rows = with_rows(b, bb, [alpha](const KsJob& j) { return (j.t + alpha - 1) / alpha; });
+  dim3 grid(r.N / kT, rows, 1);
   if (c.alpha <= 16)
-    modup_conv_kernel<false><<<grid, kT, smem, s>>>(b, r, c, pc);
+    modup_conv_kernel<false><<<grid, kT, smem, s>>>(bb, r, c, pc);
   else
-    modup_conv_kernel<true><<<grid, kT, smem, s>>>(b, r, c, pc);
+    modup_conv_kernel<true><<<grid, kT, smem, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -327,8 +343,11 @@ cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& 
 cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                             cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
-  dim3 grid(r.N / kT, max_t(b) + c.np, b.njobs);
-  ks_inner_kernel<<<grid, kT, 0, s>>>(b, r, c, pc);
+  KsBatch bb;
+  const int np = c.np;
+  const int rows = with_rows(b, bb, [np](const KsJob& j) { return j.t + np; });
+  dim3 grid(r.N / kT, rows, 1);
+  ks_inner_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -337,11 +356,13 @@ cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables
                                 cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
   const size_t smem = sizeof(uint2) * c.np * max_t(b);
-  dim3 grid(r.N / kT, 2, b.njobs);
+  KsBatch bb;
+  const int rows = with_rows(b, bb, [](const KsJob&) { return 2; });
+  dim3 grid(r.N / kT, rows, 1);
   switch (c.np) {
 #define FGB_MD_CASE(K_)                                                    \
   case K_:                                                                 \
-    moddown_conv_kernel<K_><<<grid, kT, smem, s>>>(b, r, c, pc);          \
+    moddown_conv_kernel<K_><<<grid, kT, smem, s>>>(bb, r, c, pc);          \
     break;
     FGB_MD_CASE(1) FGB_MD_CASE(2) FGB_MD_CASE(3) FGB_MD_CASE(4) FGB_MD_CASE(5) FGB_MD_CASE(6) FGB_MD_CASE(7)
     FGB_MD_CASE(8) FGB_MD_CASE(9) FGB_MD_CASE(10) FGB_MD_CASE(11) FGB_MD_CASE(12) FGB_MD_CASE(13)
@@ -357,24 +378,30 @@ cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables
 cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                                     cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
-  dim3 grid(r.N / kT, max_t(b), 2 * b.njobs);
-  moddown_epilogue_kernel<<<grid, kT, 0, s>>>(b, r, c, pc);
+  KsBatch bb;
+  const int rows = with_rows(b, bb, [](const KsJob& j) { return 2 * j.t; });
+  dim3 grid(r.N / kT, rows, 1);
+  moddown_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
-  dim3 grid(r.N / kT, max_t(b), b.njobs);
-  tensor_kernel<<<grid, kT, 0, s>>>(b, r, pc);
+  TensorBatch bb;
+  const int rows = with_rows(b, bb, [](const TensorJob& j) { return j.t; });
+  dim3 grid(r.N / kT, rows, 1);
+  tensor_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
-  dim3 grid(r.N / kT, max_t(b), b.njobs);
-  addsub_kernel<<<grid, kT, 0, s>>>(b, r, pc);
+  AddBatch bb;
+  const int rows = with_rows(b, bb, [](const AddJob& j) { return j.t; });
+  dim3 grid(r.N / kT, rows, 1);
+  addsub_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -382,10 +409,11 @@ cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeC
 cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, const PrimeConst* pc,
                                   cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
-  const int mt = max_t(b);
-  if (mt < 2) return cudaSuccess;
-  dim3 grid(r.N / kT, mt - 1, 2 * b.njobs);
-  rescale_switch_kernel<<<grid, kT, 0, s>>>(b, r, pc);
+  RescaleBatch bb;
+  const int rows = with_rows(b, bb, [](const RescaleJob& j) { return 2 * (j.t - 1); });
+  if (rows <= 0) return cudaSuccess;
+  dim3 grid(r.N / kT, rows, 1);
+  rescale_switch_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -393,10 +421,11 @@ cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, 
 cudaError_t launch_rescale_epilogue(const RescaleBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                                     cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
-  const int mt = max_t(b);
-  if (mt < 2) return cudaSuccess;
-  dim3 grid(r.N / kT, mt - 1, 2 * b.njobs);
-  rescale_epilogue_kernel<<<grid, kT, 0, s>>>(b, r, c, pc);
+  RescaleBatch bb;
+  const int rows = with_rows(b, bb, [](const RescaleJob& j) { return 2 * (j.t - 1); });
+  if (rows <= 0) return cudaSuccess;
+  dim3 grid(r.N / kT, rows, 1);
+  rescale_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }

@@ -46,6 +46,7 @@ struct KsJob {
 
 struct KsBatch {
   int njobs;
+  int row_begin[kMaxJobs + 1];  // filled by each launcher: prefix sums of that kernel's rows per job
   KsJob jobs[kMaxJobs];
 };
 
@@ -58,6 +59,7 @@ struct TensorJob {
 };
 struct TensorBatch {
   int njobs;
+  int row_begin[kMaxJobs + 1];  // filled by each launcher: prefix sums of that kernel's rows per job
   TensorJob jobs[kMaxJobs];
 };
 
@@ -71,6 +73,7 @@ struct AddJob {
 };
 struct AddBatch {
   int njobs;
+  int row_begin[kMaxJobs + 1];  // filled by each launcher: prefix sums of that kernel's rows per job
   AddJob jobs[kMaxJobs];
 };
 
@@ -84,6 +87,7 @@ struct RescaleJob {
 };
 struct RescaleBatch {
   int njobs;
+  int row_begin[kMaxJobs + 1];  // filled by each launcher: prefix sums of that kernel's rows per job
   RescaleJob jobs[kMaxJobs];
 };
 

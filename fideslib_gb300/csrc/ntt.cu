@@ -90,11 +90,11 @@ struct LimbRef {
   bool valid;
 };
 
-// Job blockIdx.z, limb blockIdx.y (uniform over a cluster, so an out-of-range cluster exits as a whole
-// before any cluster barrier).
+// Flattened limb blockIdx.y -> (job, limb of job); uniform over a cluster.
 __device__ __forceinline__ LimbRef locate(const NttBatch& b, int N) {
-  const NttJob& J = b.jobs[blockIdx.z];
-  const int q = blockIdx.y;
+  const int z = find_job(b.limb_begin, b.njobs, (int)blockIdx.y);
+  const NttJob& J = b.jobs[z];
+  const int q = (int)blockIdx.y - b.limb_begin[z];
   LimbRef r{nullptr, nullptr, 0, false};
   if (q < J.limbs * J.npolys) {
     const int poly = q / J.limbs, j = q - poly * J.limbs;
@@ -305,7 +305,7 @@ cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cud
     attr_done[inverse] = true;
   }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(S::C, b.max_limbs, b.njobs);
+  cfg.gridDim = dim3(S::C, b.limb_begin[b.njobs], 1);
   cfg.blockDim = dim3(kThreads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
@@ -325,8 +325,8 @@ cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cud
 }  // namespace
 
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
-  if (b.njobs <= 0 || b.max_limbs <= 0) return cudaSuccess;
-  if (b.njobs > kMaxNttJobs || b.max_limbs > 65535) return cudaErrorInvalidValue;
+  if (b.njobs <= 0 || b.limb_begin[b.njobs] <= 0) return cudaSuccess;
+  if (b.njobs > kMaxNttJobs || b.limb_begin[b.njobs] > 65535) return cudaErrorInvalidValue;
   switch (t.logN) {
     case 10: return launch_t<10>(b, t, inverse, s);
     case 11: return launch_t<11>(b, t, inverse, s);

@@ -26,7 +26,7 @@ constexpr int kMaxNttJobs = 64;
 
 struct NttBatch {
   int njobs;
-  int max_limbs;  // max over jobs of limbs * npolys (grid.y)
+  int limb_begin[kMaxNttJobs + 1];  // prefix sums of limbs * npolys: grid.y covers exactly the real limbs
   NttJob jobs[kMaxNttJobs];
 };
 
@@ -40,10 +40,22 @@ struct DeviceTables {
 // Forward (inverse=false: coefficient -> evaluation, bit-reversed) or inverse transform of every job.
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s);
 
+// Job owning flattened row `row` of a prefix-sum table begin[0..njobs] (uniform per block / cluster).
+__device__ __forceinline__ int find_job(const int* begin, int njobs, int row) {
+  int lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (begin[mid] <= row) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // Convenience: appends a job; returns false when the batch is full.
 inline bool ntt_add_job(NttBatch& b, const u64* src, u64* dst, long long src_stride, long long dst_stride, int limbs,
                         int npolys, const uint8_t* prime_of) {
   if (b.njobs >= kMaxNttJobs || limbs <= 0 || npolys <= 0) return limbs <= 0 || npolys <= 0;
+  if (b.njobs == 0) b.limb_begin[0] = 0;
+  b.limb_begin[b.njobs + 1] = b.limb_begin[b.njobs] + limbs * npolys;
   NttJob& j = b.jobs[b.njobs++];
   j.src = src;
   j.dst = dst;
@@ -52,7 +64,6 @@ inline bool ntt_add_job(NttBatch& b, const u64* src, u64* dst, long long src_str
   j.limbs = limbs;
   j.npolys = npolys;
   for (int k = 0; k < limbs; k++) j.prime_of[k] = prime_of[k];
-  if (limbs * npolys > b.max_limbs) b.max_limbs = limbs * npolys;
   return true;
 }
 
