@@ -492,9 +492,11 @@ def ntt_bench(args, dev, stream):
     f_ms, i_ms = statistics.mean(fwd), statistics.mean(inv)
     ach = algo / (f_ms / 1e3) / 1e9
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "ntt_fwd_traffic.json")
+    tp = os.path.join(ROOT, "profiles", "ntt_fwd_traffic.txt")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("bytes_per_launch")
+        for line in open(tp):
+            if line.startswith("bytes_per_launch:"):
+                traffic = int(line.split(":")[1])
     return {
         "summary": {"ms_ntt": round(f_ms, 4), "ms_intt": round(i_ms, 4),
                     "ntt_gbs": round(ach, 1), "intt_gbs": round(algo / (i_ms / 1e3) / 1e9, 1),

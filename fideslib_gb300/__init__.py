@@ -74,6 +74,20 @@ _SIGS = {
     "fides_eval_fast_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, i32p, u32p]),
     "fides_eval_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "fides_ctx_get_shape": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fides_pt_load": (C.c_int, [C.c_void_p, u64p, C.c_uint32, C.c_double, u32p]),
+    "fides_pt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fides_eval_mult_plain": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_add_plain": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_sub_plain": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_mult_int": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int64, u32p]),
+    "fides_eval_mult_scalar": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, C.c_double, u32p]),
+    "fides_eval_add_scalar": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, u32p]),
+    "fides_level_reduce": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_mod_raise": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_lt_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, u64p, C.POINTER(C.c_uint8),
+                                  C.c_double, u32p]),
+    "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fides_eval_linear_transform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_server_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "fides_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, u32p, C.POINTER(C.c_double)]),
@@ -262,6 +276,60 @@ class CryptoContext:
 
     def eval_automorphism(self, a: int, galois: int) -> int:
         return self._bin(lib().fides_eval_automorphism, a, galois)
+
+    # --- plaintexts, scalars, levels, bootstrap building blocks ---
+    def load_plaintext(self, pt: np.ndarray, scale: float = 1.0) -> int:
+        pt = np.ascontiguousarray(pt, dtype=np.uint64)
+        h = C.c_uint32()
+        _check(lib().fides_pt_load(self._h, _p(pt), pt.shape[0], scale, C.byref(h)))
+        return h.value
+
+    def free_plaintext(self, h: int):
+        _check(lib().fides_pt_free(self._h, h))
+
+    def _un(self, fn, *args) -> int:
+        o = C.c_uint32()
+        _check(fn(self._h, *args, C.byref(o)))
+        return o.value
+
+    def eval_mult_plain(self, a: int, pt: int) -> int:
+        return self._un(lib().fides_eval_mult_plain, a, pt)
+
+    def eval_add_plain(self, a: int, pt: int) -> int:
+        return self._un(lib().fides_eval_add_plain, a, pt)
+
+    def eval_sub_plain(self, a: int, pt: int) -> int:
+        return self._un(lib().fides_eval_sub_plain, a, pt)
+
+    def eval_mult_int(self, a: int, k: int) -> int:
+        return self._un(lib().fides_eval_mult_int, a, k)
+
+    def eval_mult_scalar(self, a: int, v: float, scale: float) -> int:
+        return self._un(lib().fides_eval_mult_scalar, a, v, scale)
+
+    def eval_add_scalar(self, a: int, v: float) -> int:
+        return self._un(lib().fides_eval_add_scalar, a, v)
+
+    def level_reduce(self, a: int, towers: int) -> int:
+        return self._un(lib().fides_level_reduce, a, towers)
+
+    def mod_raise(self, a: int, towers: int) -> int:
+        return self._un(lib().fides_mod_raise, a, towers)
+
+    def lt_create(self, bs: int, gs: int, diags: np.ndarray, present, scale: float = 1.0) -> int:
+        """diags: u64[gs*bs][towers][N] (diagonal g*bs+b pre-rotated by -g*bs); present: bool[gs*bs]."""
+        diags = np.ascontiguousarray(diags, dtype=np.uint64)
+        pres = np.ascontiguousarray(np.array(present, dtype=np.uint8))
+        h = C.c_uint32()
+        _check(lib().fides_lt_create(self._h, bs, gs, diags.shape[1], _p(diags), pres.ctypes.data_as(
+            C.POINTER(C.c_uint8)), scale, C.byref(h)))
+        return h.value
+
+    def lt_free(self, h: int):
+        _check(lib().fides_lt_free(self._h, h))
+
+    def eval_linear_transform(self, a: int, lt: int) -> int:
+        return self._un(lib().fides_eval_linear_transform, a, lt)
 
     def eval_batch(self, ops) -> list[int]:
         """ops: iterable of (op_code, a, b, index); returns result handles (one batched pipeline per op family)."""

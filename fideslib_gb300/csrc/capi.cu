@@ -1,4 +1,5 @@
 // extern "C" boundary of the engine (declarations and contract: include/fideslib_gb300.h).
+#include <cmath>
 #include <cstring>
 #include <string>
 
@@ -404,6 +405,258 @@ int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32
   if (rc == FIDES_OK)
     for (uint32_t i = 0; i < n; i++) outs[i] = ops[i].out;
   return rc;
+}
+
+
+// ---------------------------------------------------------------------------------------------------------
+// Plaintexts, scalars, level management, ModRaise and linear transforms (bootstrap building blocks)
+// ---------------------------------------------------------------------------------------------------------
+
+namespace {
+
+// Residue of round(v) mod q for |v| < 2^126, exact for the double value: v = m * 2^e with a 53-bit integer m.
+uint64_t double_residue(double v, uint64_t q) {
+  typedef unsigned __int128 u128;
+  const bool neg = v < 0;
+  double a = neg ? -v : v;
+  a = std::nearbyint(a);
+  int e = 0;
+  const double fr = std::frexp(a, &e);  // a = fr * 2^e, fr in [0.5, 1)
+  uint64_t r;
+  if (e <= 63) {
+    r = (uint64_t)a % q;
+  } else {
+    const uint64_t m = (uint64_t)std::ldexp(fr, 53);  // a = m * 2^(e-53)
+    uint64_t p2 = 1 % q, b = 2 % q;
+    for (int k = e - 53; k > 0; k >>= 1) {
+      if (k & 1) p2 = (uint64_t)((u128)p2 * b % q);
+      b = (uint64_t)((u128)b * b % q);
+    }
+    r = (uint64_t)((u128)(m % q) * p2 % q);
+  }
+  return neg && r ? q - r : r;
+}
+
+uint64_t shoup_const(uint64_t w, uint64_t q) { return (uint64_t)(((unsigned __int128)w << 64) / q); }
+
+fgb::DevPt* find_pt(fides_ctx* ctx, uint32_t h) {
+  auto it = ctx->c->pts.find(h);
+  return it == ctx->c->pts.end() ? nullptr : &it->second;
+}
+
+int scalar_op(fides_ctx* ctx, uint32_t a, const uint64_t* mul, const uint64_t* addv, fgb::DevCt meta, uint32_t* out) {
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, meta, &r);
+  if (rc) return rc;
+  fgb::ScalarBatch sb{};
+  fgb::ScalarJob& j = sb.jobs[0];
+  j.ct = A->data;
+  j.out = r.data;
+  j.t = A->t;
+  for (int k = 0; k < A->t; k++) {
+    j.mul[k] = mul[k];
+    j.mul_sh[k] = shoup_const(mul[k], c->mod[k]);
+    j.add[k] = addv[k];
+  }
+  sb.njobs = 1;
+  const fgb::Ring ring{c->N, c->logN};
+  CK(fgb::launch_scalar(sb, ring, c->d_pc, c->stream), "scalar op");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+}  // namespace
+
+int fides_pt_load(fides_ctx* ctx, const uint64_t* data, uint32_t towers, double scale, uint32_t* handle) {
+  if (!valid_ctx(ctx) || !data || !handle) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  if (towers < 1 || towers > (uint32_t)c->nq) return fail(FIDES_EINVAL, "towers out of range");
+  fgb::DevPt p;
+  p.t = (int)towers;
+  p.scale = scale;
+  p.data = c->alloc_limbs(towers, c->stream);
+  if (!p.data) return fail(FIDES_ENOMEM, "plaintext allocation failed");
+  CK(cudaMemcpyAsync(p.data, data, (size_t)towers * c->N * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream),
+     "plaintext copy");
+  const uint32_t h = c->next_handle++;
+  c->pts[h] = p;
+  *handle = h;
+  return FIDES_OK;
+}
+
+int fides_pt_free(fides_ctx* ctx, uint32_t handle) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  auto it = ctx->c->pts.find(handle);
+  if (it == ctx->c->pts.end()) return fail(FIDES_EINVAL, "unknown plaintext handle");
+  ctx->c->free_limbs(it->second.data, ctx->c->stream);
+  ctx->c->pts.erase(it);
+  return FIDES_OK;
+}
+
+static int plain_op(fides_ctx* ctx, uint32_t a, uint32_t pt, int mode, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  fgb::DevPt* P = find_pt(ctx, pt);
+  if (!A || !P) return fail(FIDES_EINVAL, "unknown ciphertext or plaintext handle");
+  if (P->t < A->t) return fail(FIDES_EINVAL, "plaintext has fewer towers than the ciphertext");
+  fgb::DevCt meta = *A;
+  if (mode == 0) {
+    meta.scale = A->scale * P->scale;
+    meta.noise_deg = A->noise_deg + 1;
+  }
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, meta, &r);
+  if (rc) return rc;
+  fgb::PtBatch pb{};
+  pb.jobs[0] = fgb::PtJob{A->data, P->data, r.data, A->t, mode};
+  pb.njobs = 1;
+  const fgb::Ring ring{c->N, c->logN};
+  CK(fgb::launch_ptop(pb, ring, c->d_pc, c->stream), "plaintext op");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_eval_mult_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) { return plain_op(ctx, a, pt, 0, out); }
+int fides_eval_add_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) { return plain_op(ctx, a, pt, 1, out); }
+int fides_eval_sub_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) { return plain_op(ctx, a, pt, 2, out); }
+
+int fides_eval_mult_int(fides_ctx* ctx, uint32_t a, int64_t k, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  uint64_t mul[64], addv[64] = {0};
+  for (int j = 0; j < A->t; j++) mul[j] = double_residue((double)k, ctx->c->mod[j]);
+  if (k > (1ll << 52) || k < -(1ll << 52))
+    for (int j = 0; j < A->t; j++) {
+      const uint64_t q = ctx->c->mod[j];
+      const uint64_t m = (uint64_t)(k < 0 ? -(k + 1) : k) % q;
+      mul[j] = k < 0 ? (q - 1 - m) % q : m;
+    }
+  return scalar_op(ctx, a, mul, addv, *A, out);
+}
+
+int fides_eval_mult_scalar(fides_ctx* ctx, uint32_t a, double v, double scale, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  uint64_t mul[64], addv[64] = {0};
+  for (int j = 0; j < A->t; j++) mul[j] = double_residue(v * scale, ctx->c->mod[j]);
+  fgb::DevCt meta = *A;
+  meta.scale = A->scale * scale;
+  meta.noise_deg = A->noise_deg + 1;
+  return scalar_op(ctx, a, mul, addv, meta, out);
+}
+
+int fides_eval_add_scalar(fides_ctx* ctx, uint32_t a, double v, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  uint64_t mul[64], addv[64];
+  for (int j = 0; j < A->t; j++) {
+    mul[j] = 1;
+    addv[j] = double_residue(v * A->scale, ctx->c->mod[j]);
+  }
+  return scalar_op(ctx, a, mul, addv, *A, out);
+}
+
+int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  if (towers < 1 || (int)towers > A->t) return fail(FIDES_EINVAL, "towers must be in [1, current towers]");
+  fgb::DevCt r;
+  int rc = new_ct(ctx, (int)towers, *A, &r);
+  if (rc) return rc;
+  const size_t row = (size_t)towers * c->N * sizeof(uint64_t);
+  CK(cudaMemcpy2DAsync(r.data, row, A->data, (size_t)A->t * c->N * sizeof(uint64_t), row, 2, cudaMemcpyDeviceToDevice,
+                       c->stream),
+     "level reduce");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_mod_raise(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  if (towers < 1 || (int)towers > c->nq) return fail(FIDES_EINVAL, "towers out of range");
+  fgb::DevCt r;
+  int rc = new_ct(ctx, (int)towers, *A, &r);
+  if (rc) return rc;
+  CK(c->mod_raise(A->data, A->t, (int)towers, r.data, c->stream), "mod raise");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, const uint64_t* diags,
+                    const uint8_t* present, double scale, uint32_t* handle) {
+  if (!valid_ctx(ctx) || !diags || !present || !handle) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  if (bs < 1 || gs < 1 || gs > (uint32_t)fgb::kMaxJobs || towers < 1 || towers > (uint32_t)c->nq)
+    return fail(FIDES_EINVAL, "need bs >= 1, 1 <= gs <= 64, 1 <= towers <= nq");
+  fgb::DevLT lt;
+  lt.bs = (int)bs;
+  lt.gs = (int)gs;
+  lt.t = (int)towers;
+  lt.scale = scale;
+  lt.present.assign(present, present + (size_t)bs * gs);
+  const size_t bytes = (size_t)bs * gs * towers * c->N * sizeof(uint64_t);
+  void* d = nullptr;
+  void* pd = nullptr;
+  CK(cudaMalloc(&d, bytes), "linear transform allocation");
+  CK(cudaMalloc(&pd, (size_t)bs * gs), "linear transform allocation");
+  lt.diags = (fgb::u64*)d;
+  lt.present_dev = (uint8_t*)pd;
+  CK(cudaMemcpyAsync(d, diags, bytes, cudaMemcpyHostToDevice, c->stream), "linear transform copy");
+  CK(cudaMemcpyAsync(pd, present, (size_t)bs * gs, cudaMemcpyHostToDevice, c->stream), "linear transform copy");
+  CK(cudaStreamSynchronize(c->stream), "linear transform copy");
+  const uint32_t h = c->next_handle++;
+  c->lts[h] = std::move(lt);
+  *handle = h;
+  return FIDES_OK;
+}
+
+int fides_lt_free(fides_ctx* ctx, uint32_t handle) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  auto it = ctx->c->lts.find(handle);
+  if (it == ctx->c->lts.end()) return fail(FIDES_EINVAL, "unknown linear transform handle");
+  cudaStreamSynchronize(ctx->c->stream);
+  cudaFree(it->second.diags);
+  cudaFree(it->second.present_dev);
+  ctx->c->lts.erase(it);
+  return FIDES_OK;
+}
+
+int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  auto it = c->lts.find(lt);
+  if (!A || it == c->lts.end()) return fail(FIDES_EINVAL, "unknown ciphertext or linear transform handle");
+  if (int rc0 = check_ks_shape(ctx)) return rc0;
+  const fgb::DevLT& L = it->second;
+  if (A->t > L.t) return fail(FIDES_EINVAL, "ciphertext has more towers than the transform's diagonals");
+  for (int b = 1; b < L.bs; b++)
+    if (!c->rot_keys.count(fgb::Context::galois_for_index(c->N, b)))
+      return fail(FIDES_ENOKEY, "missing baby-step rotation key for index " + std::to_string(b));
+  for (int g = 1; g < L.gs; g++)
+    if (!c->rot_keys.count(fgb::Context::galois_for_index(c->N, g * L.bs)))
+      return fail(FIDES_ENOKEY, "missing giant-step rotation key for index " + std::to_string(g * L.bs));
+  fgb::DevCt meta = *A;
+  meta.scale = A->scale * L.scale;
+  meta.noise_deg = A->noise_deg + 1;
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, meta, &r);
+  if (rc) return rc;
+  CK(c->linear_transform(A->data, A->t, L, r.data, c->stream), "linear transform");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
 }
 
 }  // extern "C"

@@ -112,6 +112,12 @@ Context::~Context() {
   stream = own_stream;
   for (auto& kv : cts)
     if (kv.second.data) cudaFree(kv.second.data);
+  for (auto& kv : pts)
+    if (kv.second.data) cudaFree(kv.second.data);
+  for (auto& kv : lts) {
+    if (kv.second.diags) cudaFree(kv.second.diags);
+    if (kv.second.present_dev) cudaFree(kv.second.present_dev);
+  }
   for (auto& kv : rot_keys) cudaFree(kv.second);
   if (relin_key) cudaFree(relin_key);
   for (void* p : owned_) cudaFree(p);
@@ -604,6 +610,97 @@ cudaError_t Context::add_batch(const AddReq* reqs, int n, cudaStream_t s) {
       ab.jobs[ab.njobs++] = AddJob{reqs[i].x, reqs[i].y, reqs[i].out, reqs[i].t, reqs[i].sub ? 1 : 0};
     err = launch_addsub(ab, ring_, nq, d_pc, s);
   }
+  return err;
+}
+
+cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64* out, cudaStream_t s) {
+  const size_t NN = (size_t)N, CT = (size_t)2 * t * NN;
+  const int bs = lt.bs, gs = lt.gs;
+  if (t > lt.t || gs > kMaxJobs) return cudaErrorInvalidValue;
+  std::vector<int> active;  // giant steps with at least one diagonal
+  for (int g = 0; g < gs; g++) {
+    bool any = false;
+    for (int b = 0; b < bs; b++) any = any || lt.present[(size_t)g * bs + b];
+    if (any) active.push_back(g);
+  }
+  u64* ws = alloc_limbs((size_t)2 * t * (size_t)(bs - 1 + 2 * gs), s);
+  if (!ws) return cudaErrorMemoryAllocation;
+  u64* baby = ws;                          // [bs-1] ciphertexts
+  u64* inner = ws + (size_t)(bs - 1) * CT;  // [gs]
+  u64* giant = inner + (size_t)gs * CT;     // [gs]
+  cudaError_t err = cudaSuccess;
+  {  // baby steps: rotations of x by 1..bs-1, one shared ModUp
+    std::vector<KsReq> rq;
+    for (int b = 1; b < bs; b++) {
+      const uint32_t g = galois_for_index(N, b);
+      auto it = rot_keys.find(g);
+      if (it == rot_keys.end()) err = cudaErrorInvalidValue;
+      else rq.push_back({x + (size_t)t * NN, t, it->second, x, nullptr, baby + (size_t)(b - 1) * CT, galois_inverse(g)});
+    }
+    if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
+  }
+  if (err == cudaSuccess && !active.empty()) {  // inner sums, one launch
+    DotBatch db{};
+    db.rot0 = x;
+    db.rot_base = baby;
+    db.rot_stride = (long long)CT;
+    db.pt_base = lt.diags;
+    db.pt_stride = (long long)lt.t * N;
+    db.present = lt.present_dev;
+    db.bs = bs;
+    db.t = t;
+    for (int g : active) db.jobs[db.njobs++] = DotJob{inner + (size_t)g * CT, g};
+    err = launch_ptdot(db, ring_, d_pc, s);
+  }
+  if (err == cudaSuccess) {  // giant-step rotations, one batch
+    std::vector<KsReq> rq;
+    for (int g : active) {
+      if (g == 0) continue;
+      const uint32_t gl = galois_for_index(N, g * bs);
+      auto it = rot_keys.find(gl);
+      if (it == rot_keys.end()) {
+        err = cudaErrorInvalidValue;
+        break;
+      }
+      const u64* in = inner + (size_t)g * CT;
+      rq.push_back({in + (size_t)t * NN, t, it->second, in, nullptr, giant + (size_t)(rq.size()) * CT,
+                    galois_inverse(gl)});
+    }
+    if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
+    if (err == cudaSuccess) {
+      SumBatch sb{};
+      const bool has0 = !active.empty() && active[0] == 0;
+      sb.jobs[0] = SumJob{giant, (long long)CT, (int)rq.size(), has0 ? inner : nullptr, out, t};
+      sb.njobs = 1;
+      if (!has0 && rq.empty()) err = cudaMemsetAsync(out, 0, CT * sizeof(u64), s);
+      else err = launch_sum(sb, ring_, d_pc, s);
+    }
+  }
+  free_limbs(ws, s);
+  return err;
+}
+
+cudaError_t Context::mod_raise(const u64* x, int t_in, int T, u64* out, cudaStream_t s) {
+  const size_t NN = (size_t)N;
+  u64* ws = alloc_limbs(2, s);
+  if (!ws) return cudaErrorMemoryAllocation;
+  cudaError_t err;
+  {
+    NttQueue q(tabs, true, s);
+    uint8_t pm[1] = {0};
+    q.add(x, ws, (long long)t_in * N, N, 1, 2, pm);  // tower 0 of both polys to coefficient form
+    q.flush();
+    err = q.err;
+  }
+  if (err == cudaSuccess) {
+    RaiseBatch rb{};
+    rb.jobs[0] = RaiseJob{ws, out, T};
+    rb.njobs = 1;
+    err = launch_raise_switch(rb, ring_, d_pc, s);
+  }
+  if (err == cudaSuccess) err = ntt(out, out, 2, T, 0, (long long)T * N, false, s);
+  (void)NN;
+  free_limbs(ws, s);
   return err;
 }
 

@@ -27,6 +27,22 @@ struct DevCt {
   int slots = 0;
 };
 
+struct DevPt {
+  u64* data = nullptr;  // [t][N] evaluation form
+  int t = 0;
+  double scale = 1.0;
+};
+
+// Baby-step / giant-step linear transform: diagonals laid out contiguously [gs*bs][t][N]; diagonal
+// g*bs + b is already rotated by -g*bs (the layout the reference's LT precomputation produces).
+struct DevLT {
+  u64* diags = nullptr;
+  uint8_t* present_dev = nullptr;
+  std::vector<uint8_t> present;
+  int bs = 0, gs = 0, t = 0;
+  double scale = 1.0;
+};
+
 class Context {
  public:
   ~Context();
@@ -86,11 +102,19 @@ class Context {
   };
   cudaError_t add_batch(const AddReq* reqs, int n, cudaStream_t s);
 
+  // y = sum_g rot_{g*bs}( sum_b lt.diag[g*bs+b] (.) rot_b(x) ): baby-step rotations share one ModUp, the inner
+  // sums are one pt-dot launch, the giant-step rotations one key-switch batch, the final sum one launch.
+  cudaError_t linear_transform(const u64* x, int t, const DevLT& lt, u64* out, cudaStream_t s);
+  // Raise a ciphertext's tower 0 to T towers (centred lift) — the first step of bootstrapping.
+  cudaError_t mod_raise(const u64* x, int t_in, int T, u64* out, cudaStream_t s);
+
   // --- object registry (handles as in api/CryptoContext.hpp:233-246) ---
   std::mutex mu;
   std::unordered_map<uint32_t, DevCt> cts;
   uint32_t next_handle = 1;
   std::map<uint32_t, u64*> rot_keys;  // Galois element -> key
+  std::unordered_map<uint32_t, DevPt> pts;
+  std::unordered_map<uint32_t, DevLT> lts;
   u64* relin_key = nullptr;
 
   u64* alloc_limbs(size_t nlimbs, cudaStream_t s);

@@ -300,6 +300,97 @@ __global__ void __launch_bounds__(kT) rescale_epilogue_kernel(const __grid_const
   J.out[((size_t)poly * (t - 1) + i) * r.N + n] = shoup(sub_mod(a, bb, q), w.x, w.y, q);
 }
 
+
+__global__ void __launch_bounds__(kT) ptop_kernel(const __grid_constant__ PtBatch b, Ring r,
+                                                  const PrimeConst* __restrict__ pc) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const PtJob& J = b.jobs[z];
+  const int j = (int)blockIdx.y - b.row_begin[z];
+  const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
+  const size_t o0 = (size_t)j * r.N + n, o1 = ((size_t)J.t + j) * r.N + n;
+  const PrimeConst& c = pc[j];
+  const u64 w = J.pt[(size_t)j * r.N + n];
+  if (J.mode == 0) {
+    J.out[o0] = mul_mod(J.ct[o0], w, c);
+    J.out[o1] = mul_mod(J.ct[o1], w, c);
+  } else {
+    J.out[o0] = J.mode == 1 ? add_mod(J.ct[o0], w, c.p) : sub_mod(J.ct[o0], w, c.p);
+    J.out[o1] = J.ct[o1];
+  }
+}
+
+__global__ void __launch_bounds__(kT) scalar_kernel(const __grid_constant__ ScalarBatch b, Ring r,
+                                                    const PrimeConst* __restrict__ pc) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const ScalarJob& J = b.jobs[z];
+  const int j = (int)blockIdx.y - b.row_begin[z];
+  const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
+  const u64 q = pc[j].p, w = J.mul[j], wsh = J.mul_sh[j];
+  const size_t o0 = (size_t)j * r.N + n, o1 = ((size_t)J.t + j) * r.N + n;
+  J.out[o0] = add_mod(shoup(J.ct[o0], w, wsh, q), J.add[j], q);
+  J.out[o1] = shoup(J.ct[o1], w, wsh, q);
+}
+
+// grid rows per job: 2*t (poly-major).
+__global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBatch b, Ring r,
+                                                   const PrimeConst* __restrict__ pc) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const DotJob& J = b.jobs[z];
+  const int row = (int)blockIdx.y - b.row_begin[z];
+  const int t = b.t, poly = row >= t ? 1 : 0, j = row - poly * t;
+  const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
+  const size_t co = ((size_t)poly * t + j) * r.N + n, po = (size_t)j * r.N + n;
+  u64 hi = 0, lo = 0;
+  Acc4 A{0, 0, 0, 0};
+  int terms = 0;
+#pragma unroll 1
+  for (int bb = 0; bb < b.bs; bb++) {
+    const int i = J.g * b.bs + bb;
+    if (!b.present[i]) continue;
+    const u64* ct = bb == 0 ? b.rot0 : b.rot_base + (size_t)(bb - 1) * b.rot_stride;
+    const u64 x = ct[co], w = b.pt_base[(size_t)i * b.pt_stride + po];
+    acc4_mac(A, (uint32_t)(x & kMask30), (uint32_t)(x >> 30), (uint32_t)(w & kMask30), (uint32_t)(w >> 30));
+    if (++terms == 16) {
+      acc4_fold(A, hi, lo);
+      A = Acc4{0, 0, 0, 0};
+      terms = 0;
+    }
+  }
+  acc4_fold(A, hi, lo);
+  J.out[co] = reduce128_fast(hi, lo, pc[j]);
+}
+
+__global__ void __launch_bounds__(kT) sum_kernel(const __grid_constant__ SumBatch b, Ring r,
+                                                 const PrimeConst* __restrict__ pc) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const SumJob& J = b.jobs[z];
+  const int row = (int)blockIdx.y - b.row_begin[z];
+  const int t = J.t, poly = row >= t ? 1 : 0, j = row - poly * t;
+  const size_t o = ((size_t)poly * t + j) * r.N + (size_t)blockIdx.x * kT + threadIdx.x;
+  const u64 q = pc[j].p;
+  u64 acc = J.first ? J.first[o] : 0;
+#pragma unroll 4
+  for (int k = 0; k < J.n; k++) acc = add_mod(acc, J.base[(size_t)k * J.stride + o], q);
+  J.out[o] = acc;
+}
+
+// Centred lift of tower 0 into towers 0..T-1 (OpenFHE SwitchModulus semantics, as in Rescale).
+__global__ void __launch_bounds__(kT) raise_switch_kernel(const __grid_constant__ RaiseBatch b, Ring r,
+                                                          const PrimeConst* __restrict__ pc) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const RaiseJob& J = b.jobs[z];
+  const int row = (int)blockIdx.y - b.row_begin[z];
+  const int poly = row >= J.T ? 1 : 0, i = row - poly * J.T;
+  const int n = blockIdx.x * kT + threadIdx.x;
+  const PrimeConst& om = pc[0];
+  const PrimeConst& nm = pc[i];
+  const u64 om_mod_nm = shoup(om.p, 1ull, nm.one_sh, nm.p);
+  const u64 diff = nm.p - om_mod_nm;
+  u64 v = J.top[(size_t)poly * r.N + n];
+  if (v > (om.p >> 1)) v += diff;
+  J.tmp[((size_t)poly * J.T + i) * r.N + n] = shoup(v, 1ull, nm.one_sh, nm.p);
+}
+
 template <class B>
 int max_t(const B& b) {
   int m = 0;
@@ -426,6 +517,52 @@ cudaError_t launch_rescale_epilogue(const RescaleBatch& b, const Ring& r, const 
   if (rows <= 0) return cudaSuccess;
   dim3 grid(r.N / kT, rows, 1);
   rescale_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ptop(const PtBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  PtBatch bb;
+  const int rows = with_rows(b, bb, [](const PtJob& j) { return j.t; });
+  ptop_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  ScalarBatch bb;
+  const int rows = with_rows(b, bb, [](const ScalarJob& j) { return j.t; });
+  scalar_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  DotBatch bb = b;
+  bb.row_begin[0] = 0;
+  for (int i = 0; i < b.njobs; i++) bb.row_begin[i + 1] = bb.row_begin[i] + 2 * b.t;
+  ptdot_kernel<<<dim3(r.N / kT, bb.row_begin[b.njobs], 1), kT, 0, s>>>(bb, r, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum(const SumBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  SumBatch bb;
+  const int rows = with_rows(b, bb, [](const SumJob& j) { return 2 * j.t; });
+  sum_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_raise_switch(const RaiseBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  RaiseBatch bb;
+  const int rows = with_rows(b, bb, [](const RaiseJob& j) { return 2 * j.T; });
+  raise_switch_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }

@@ -91,6 +91,89 @@ struct RescaleBatch {
   RescaleJob jobs[kMaxJobs];
 };
 
+// Plaintext op on [2][t][N]: mode 0 = multiply both polys by pt, 1 = c0 + pt, 2 = c0 - pt (c1 copied).
+struct PtJob {
+  const u64* ct;
+  const u64* pt;  // [t][N]
+  u64* out;
+  int t;
+  int mode;
+};
+struct PtBatch {
+  int njobs;
+  int row_begin[kMaxJobs + 1];
+  PtJob jobs[kMaxJobs];
+};
+
+// out[p][j] = ct[p][j] * mul[j] (+ add[j] on poly 0), per-tower constants inline.
+constexpr int kMaxScalarJobs = 16;
+struct ScalarJob {
+  const u64* ct;
+  u64* out;
+  int t;
+  u64 mul[64];
+  u64 mul_sh[64];
+  u64 add[64];
+};
+struct ScalarBatch {
+  int njobs;
+  int row_begin[kMaxScalarJobs + 1];
+  ScalarJob jobs[kMaxScalarJobs];
+};
+
+// Baby-step/giant-step inner sums: job g writes out_g[p][j] = sum_{b<bs, present} rot[b][p][j] (.) pt[g*bs+b][j]
+// with rot[b] = rot_base + b*rot_stride ([2][t][N] each, rot[0] = the input itself) and pt[i] = pt_base +
+// i*pt_stride ([>=t][N] each).
+struct DotJob {
+  u64* out;
+  int g;
+};
+struct DotBatch {
+  int njobs;
+  int row_begin[kMaxJobs + 1];
+  const u64* rot0;       // b = 0 term (the input ciphertext)
+  const u64* rot_base;   // b >= 1 terms: rot_base + (b-1)*rot_stride
+  long long rot_stride;
+  const u64* pt_base;
+  long long pt_stride;
+  const uint8_t* present;  // device [gs*bs]
+  int bs, t;
+  DotJob jobs[kMaxJobs];
+};
+
+// out = sum_k in[k] over [2][t][N] (in[k] = base + k*stride), k < n.
+struct SumJob {
+  const u64* base;
+  long long stride;
+  int n;
+  const u64* first;  // added too when non-null
+  u64* out;
+  int t;
+};
+struct SumBatch {
+  int njobs;
+  int row_begin[kMaxJobs + 1];
+  SumJob jobs[kMaxJobs];
+};
+
+// ModRaise: top [2][N] = coefficient form of tower 0 (mod q_0); tmp [2][T][N] <- centred lift into towers 0..T-1.
+struct RaiseJob {
+  const u64* top;
+  u64* tmp;
+  int T;
+};
+struct RaiseBatch {
+  int njobs;
+  int row_begin[kMaxJobs + 1];
+  RaiseJob jobs[kMaxJobs];
+};
+
+cudaError_t launch_ptop(const PtBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_sum(const SumBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_raise_switch(const RaiseBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
+
 cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                               cudaStream_t s);
 cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,

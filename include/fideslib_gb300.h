@@ -124,6 +124,33 @@ int fides_eval_rotate(fides_ctx* ctx, uint32_t a, int32_t index, uint32_t* out);
 int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out);
 int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs);
 
+/* Plaintexts (RawPlainText / LoadPlaintext, RawCiphertext.cuh:37-48, api/CryptoContext.cpp:250-269):
+ * u64[towers][N] evaluation form at scaling factor `scale`. */
+int fides_pt_load(fides_ctx* ctx, const uint64_t* data, uint32_t towers, double scale, uint32_t* handle);
+int fides_pt_free(fides_ctx* ctx, uint32_t handle);
+/* EvalMult / EvalAdd / EvalSub with a plaintext (multPt / addPt: LimbPartition.cu:654-691,
+ * src/AddSub.cu); the product's scale is the product of scales. */
+int fides_eval_mult_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out);
+int fides_eval_add_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out);
+int fides_eval_sub_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out);
+/* Multiplication by an integer (multIntScalar, src/CKKS/ApproxModEval.cu:131-136): scale unchanged. */
+int fides_eval_mult_int(fides_ctx* ctx, uint32_t a, int64_t k, uint32_t* out);
+/* Multiplication by a real constant encoded as round(v * scale) (EvalMult(ct, double)): scale *= scale. */
+int fides_eval_mult_scalar(fides_ctx* ctx, uint32_t a, double v, double scale, uint32_t* out);
+/* Adds v in every slot: round(v * ct scale) added to c0 (EvalAdd(ct, double), src/AddSub.cu scalar_add_). */
+int fides_eval_add_scalar(fides_ctx* ctx, uint32_t a, double v, uint32_t* out);
+/* Keeps the first `towers` towers (LevelReduce / SetLevel, api/CryptoContext.hpp:184). */
+int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out);
+/* ModRaise (src/CKKS/Bootstrap.cu:393-...): tower 0 of `a`, lifted (centred) to `towers` towers. */
+int fides_mod_raise(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out);
+/* Baby-step/giant-step linear transform (EvalLinearTransform, src/CKKS/LinearTransform.cu:63-256):
+ * diags = u64[gs*bs][towers][N] evaluation form, diagonal i = g*bs + b already rotated by -g*bs;
+ * present[i] = 0 marks a zero diagonal.  Needs rotation keys for 1..bs-1 and for g*bs. */
+int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, const uint64_t* diags,
+                    const uint8_t* present, double scale, uint32_t* handle);
+int fides_lt_free(fides_ctx* ctx, uint32_t handle);
+int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_t* out);
+
 /* Batched evaluation: `n` independent requests (no request may consume another one's output) run together,
  * one launch per pipeline stage for all ciphertexts of an op family, at whatever level each ciphertext is.
  * Requests rotating the same input share its ModUp.  On success ops[i].out holds the result handle.

@@ -92,6 +92,9 @@ def lib():
         L.orc_rescale.argtypes = [C.c_void_p, u64p, C.c_int, u64p]
         L.orc_add.argtypes = [C.c_void_p, u64p, u64p, C.c_int, C.c_int, u64p]
         L.orc_sub.argtypes = [C.c_void_p, u64p, u64p, C.c_int, C.c_int, u64p]
+        L.orc_plain_op.argtypes = [C.c_void_p, u64p, u64p, C.c_int, C.c_int, u64p]
+        L.orc_scalar_op.argtypes = [C.c_void_p, u64p, C.c_int, u64p, u64p, u64p]
+        L.orc_mod_raise.argtypes = [C.c_void_p, u64p, C.c_int, C.c_int, u64p]
         L.orc_rng_fill_uniform.argtypes = [C.c_void_p, C.c_uint64, u64p, C.c_int, i32p]
         L.orc_keygen_secret.argtypes = [C.c_void_p, C.c_uint64, C.c_int, i64p]
         L.orc_secret_eval.argtypes = [C.c_void_p, i64p, u64p]
@@ -285,6 +288,25 @@ class Ctx:
         out = np.zeros_like(x)
         lib().orc_sub(self._h, _p(np.ascontiguousarray(x)), _p(np.ascontiguousarray(y)), x.shape[-2],
                       x.size // (x.shape[-2] * self.N), _p(out))
+        return out
+
+    def plain_op(self, ct: np.ndarray, pt: np.ndarray, mode: int) -> np.ndarray:
+        t = ct.shape[1]
+        out = self.zeros(2, t)
+        lib().orc_plain_op(self._h, _p(np.ascontiguousarray(ct)), _p(np.ascontiguousarray(pt)), t, mode, _p(out))
+        return out
+
+    def scalar_op(self, ct: np.ndarray, mul, add) -> np.ndarray:
+        t = ct.shape[1]
+        out = self.zeros(2, t)
+        m = np.ascontiguousarray(np.array(mul, dtype=np.uint64))
+        a = np.ascontiguousarray(np.array(add, dtype=np.uint64))
+        lib().orc_scalar_op(self._h, _p(np.ascontiguousarray(ct)), t, _p(m), _p(a), _p(out))
+        return out
+
+    def mod_raise(self, ct: np.ndarray, T: int) -> np.ndarray:
+        out = self.zeros(2, T)
+        lib().orc_mod_raise(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], T, _p(out))
         return out
 
     # --- synthetic inputs ---

@@ -573,6 +573,59 @@ void orc_sub(const orc_ctx* c, const uint64_t* x, const uint64_t* y, int nl, int
 }
 
 /* ------------------------------------------------------------------------------------------------ */
+/* bootstrap building blocks — multPt / addPt (src/CKKS/LimbPartition.cu:654-691, src/AddSub.cu:10-123),  */
+/* scalar ops (ElemenwiseBatchKernels.cu Scalar_mult_, AddSub.cu scalar_add_), ModRaise                 */
+/* (src/CKKS/Bootstrap.cu:393-...: coefficient form of tower 0, SwitchModulus into every tower, NTT).   */
+/* ------------------------------------------------------------------------------------------------ */
+
+void orc_plain_op(const orc_ctx* c, const uint64_t* ct, const uint64_t* pt, int t, int mode, uint64_t* out) {
+  uint64_t N = c->N;
+  for (int j = 0; j < t; j++) {
+    uint64_t q = c->mod[j];
+    for (uint64_t k = 0; k < N; k++) {
+      size_t o0 = (size_t)j * N + k, o1 = ((size_t)t + j) * N + k;
+      uint64_t w = pt[(size_t)j * N + k];
+      if (mode == 0) {
+        out[o0] = orc_mulmod(ct[o0], w, q);
+        out[o1] = orc_mulmod(ct[o1], w, q);
+      } else {
+        out[o0] = mode == 1 ? addmod(ct[o0], w, q) : submod(ct[o0], w, q);
+        out[o1] = ct[o1];
+      }
+    }
+  }
+}
+
+void orc_scalar_op(const orc_ctx* c, const uint64_t* ct, int t, const uint64_t* mul, const uint64_t* add,
+                   uint64_t* out) {
+  uint64_t N = c->N;
+  for (int p = 0; p < 2; p++)
+    for (int j = 0; j < t; j++) {
+      uint64_t q = c->mod[j];
+      for (uint64_t k = 0; k < N; k++) {
+        size_t o = ((size_t)p * t + j) * N + k;
+        uint64_t v = orc_mulmod(ct[o], mul[j], q);
+        out[o] = p == 0 ? addmod(v, add[j], q) : v;
+      }
+    }
+}
+
+void orc_mod_raise(const orc_ctx* c, const uint64_t* ct, int t_in, int T, uint64_t* out) {
+  uint64_t N = c->N, q0 = c->mod[0];
+  uint64_t* top = (uint64_t*)malloc(sizeof(uint64_t) * N);
+  for (int p = 0; p < 2; p++) {
+    memcpy(top, ct + (size_t)p * t_in * N, sizeof(uint64_t) * N);
+    orc_ntt_inv(top, N, q0, c->itab[0]);
+    for (int j = 0; j < T; j++) {
+      uint64_t* O = out + ((size_t)p * T + j) * N;
+      for (uint64_t k = 0; k < N; k++) O[k] = switch_modulus(top[k], q0, c->mod[j]);
+      orc_ntt_fwd(O, N, c->mod[j], c->tab[j]);
+    }
+  }
+  free(top);
+}
+
+/* ------------------------------------------------------------------------------------------------ */
 /* synthetic inputs: SplitMix64 streams, ternary / sparse secrets, rounded-Gaussian errors (sigma 3.19) */
 /* ------------------------------------------------------------------------------------------------ */
 

@@ -79,6 +79,15 @@ void orc_rescale(const orc_ctx* c, const uint64_t* ct, int t, uint64_t* out);
 void orc_add(const orc_ctx* c, const uint64_t* x, const uint64_t* y, int nlimbs_per_poly, int npolys, uint64_t* out);
 void orc_sub(const orc_ctx* c, const uint64_t* x, const uint64_t* y, int nlimbs_per_poly, int npolys, uint64_t* out);
 
+/* ---- bootstrap building blocks ---- */
+/* mode 0: (c0*pt, c1*pt); 1: (c0+pt, c1); 2: (c0-pt, c1).  ct u64[2][t][N], pt u64[>=t][N]. */
+void orc_plain_op(const orc_ctx* c, const uint64_t* ct, const uint64_t* pt, int t, int mode, uint64_t* out);
+/* out[p][j] = ct[p][j]*mul[j] (+ add[j] on c0). */
+void orc_scalar_op(const orc_ctx* c, const uint64_t* ct, int t, const uint64_t* mul, const uint64_t* add,
+                   uint64_t* out);
+/* ModRaise: tower 0 of ct (u64[2][t_in][N]) lifted, centred, to T towers (out u64[2][T][N]). */
+void orc_mod_raise(const orc_ctx* c, const uint64_t* ct, int t_in, int T, uint64_t* out);
+
 /* ---- synthetic key material and messages (test inputs) ---- */
 void orc_rng_fill_uniform(const orc_ctx* c, uint64_t seed, uint64_t* x, int ntowers, const int* tower_ids);
 void orc_keygen_secret(const orc_ctx* c, uint64_t seed, int hamming_weight, int64_t* s_coeffs);
