@@ -88,6 +88,9 @@ _SIGS = {
                                   C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fides_eval_linear_transform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_chebyshev": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_double), C.c_uint32, C.c_double,
+                                       C.c_double, C.c_double, u32p]),
+    "fides_eval_double_angle": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_server_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "fides_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, u32p, C.POINTER(C.c_double)]),
@@ -330,6 +333,14 @@ class CryptoContext:
 
     def eval_linear_transform(self, a: int, lt: int) -> int:
         return self._un(lib().fides_eval_linear_transform, a, lt)
+
+    def eval_chebyshev(self, a: int, coeffs, lo: float, hi: float, const_scale: float) -> int:
+        c = np.ascontiguousarray(np.array(coeffs, dtype=np.float64))
+        return self._un(lib().fides_eval_chebyshev, a, c.ctypes.data_as(C.POINTER(C.c_double)), len(c), lo, hi,
+                        const_scale)
+
+    def eval_double_angle(self, a: int, iterations: int) -> int:
+        return self._un(lib().fides_eval_double_angle, a, iterations)
 
     def eval_batch(self, ops) -> list[int]:
         """ops: iterable of (op_code, a, b, index); returns result handles (one batched pipeline per op family)."""

@@ -151,6 +151,15 @@ int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, c
 int fides_lt_free(fides_ctx* ctx, uint32_t handle);
 int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_t* out);
 
+/* EvalChebyshevSeries (api/CryptoContext.hpp:154-156, src/CKKS/ApproxModEval.cu:138-370):
+ * p(x) = sum_k coeffs[k] T_k((2x - lo - hi)/(hi - lo)), k < n, constants encoded at const_scale.  The exact op
+ * recipe (doubling identities for T_k, level alignment by dropping towers) is documented in
+ * fideslib_gb300/csrc/poly_eval.cu.  Depth: ceil(log2(n-1)) + 1, plus 1 when [lo, hi] != [-1, 1]. */
+int fides_eval_chebyshev(fides_ctx* ctx, uint32_t a, const double* coeffs, uint32_t n, double lo, double hi,
+                         double const_scale, uint32_t* out);
+/* x <- 2x^2 - 1 applied `iterations` times (ApproxModEval.cu:724-739 double-angle iterations of EvalMod). */
+int fides_eval_double_angle(fides_ctx* ctx, uint32_t a, uint32_t iterations, uint32_t* out);
+
 /* Batched evaluation: `n` independent requests (no request may consume another one's output) run together,
  * one launch per pipeline stage for all ciphertexts of an op family, at whatever level each ciphertext is.
  * Requests rotating the same input share its ModUp.  On success ops[i].out holds the result handle.
