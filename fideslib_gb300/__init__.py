@@ -91,6 +91,7 @@ _SIGS = {
     "fides_eval_chebyshev": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                        C.c_double, C.c_double, u32p]),
     "fides_eval_double_angle": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_bootstrap": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, u32p]),
     "fides_server_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "fides_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, u32p, C.POINTER(C.c_double)]),
@@ -342,6 +343,9 @@ class CryptoContext:
     def eval_double_angle(self, a: int, iterations: int) -> int:
         return self._un(lib().fides_eval_double_angle, a, iterations)
 
+    def eval_bootstrap(self, a: int, plan: "BootstrapPlan") -> int:
+        return self._un(lib().fides_eval_bootstrap, a, C.byref(plan))
+
     def eval_batch(self, ops) -> list[int]:
         """ops: iterable of (op_code, a, b, index); returns result handles (one batched pipeline per op family)."""
         ops = list(ops)
@@ -361,6 +365,13 @@ class CryptoContext:
 def kernel_launches() -> int:
     """Engine kernels launched by this process so far."""
     return int(lib().fides_kernel_launches())
+
+
+class BootstrapPlan(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("raise_towers", C.c_uint32), ("lt_cts_re", C.c_uint32),
+                ("lt_cts_im", C.c_uint32), ("lt_stc_re", C.c_uint32), ("lt_stc_im", C.c_uint32),
+                ("cheb_coeffs", C.POINTER(C.c_double)), ("cheb_n", C.c_uint32), ("double_angle", C.c_uint32),
+                ("cheb_lo", C.c_double), ("cheb_hi", C.c_double), ("const_scale", C.c_double)]
 
 
 class ServerConfig(C.Structure):

@@ -160,6 +160,26 @@ int fides_eval_chebyshev(fides_ctx* ctx, uint32_t a, const double* coeffs, uint3
 /* x <- 2x^2 - 1 applied `iterations` times (ApproxModEval.cu:724-739 double-angle iterations of EvalMod). */
 int fides_eval_double_angle(fides_ctx* ctx, uint32_t a, uint32_t iterations, uint32_t* out);
 
+/* Bootstrapping (EvalBootstrap, api/CryptoContext.cpp:1719-1768; src/CKKS/Bootstrap.cu:169-333) with the
+ * caller's precomputation: CoeffsToSlots / SlotsToCoeffs diagonals (fides_lt_create) and the EvalMod
+ * approximation.  Steps and conventions are documented in fideslib_gb300/csrc/bootstrap.cu.  Keys needed:
+ * relinearisation, conjugation (Galois 2N-1), rotations n, 2n, ..., N/4 (sparse-slot trace) and the linear
+ * transforms' baby/giant steps. */
+typedef struct {
+  uint32_t slots;          /* n, power of two <= N/2 */
+  uint32_t raise_towers;   /* towers after ModRaise */
+  uint32_t lt_cts_re;      /* CoeffsToSlots halves: diagonals of U^-1/(2 N/2n) and -i U^-1/(2 N/2n) */
+  uint32_t lt_cts_im;
+  uint32_t lt_stc_re;      /* SlotsToCoeffs: diagonals of U and i U */
+  uint32_t lt_stc_im;
+  const double* cheb_coeffs;  /* Chebyshev approximation of cos(2 pi (r/K - 1/4) / 2^double_angle) */
+  uint32_t cheb_n;
+  uint32_t double_angle;
+  double cheb_lo, cheb_hi;    /* approximation interval in slot values r */
+  double const_scale;         /* scale for the constants of EvalMod */
+} fides_bootstrap_plan;
+int fides_eval_bootstrap(fides_ctx* ctx, uint32_t ct, const fides_bootstrap_plan* plan, uint32_t* out);
+
 /* Batched evaluation: `n` independent requests (no request may consume another one's output) run together,
  * one launch per pipeline stage for all ciphertexts of an op family, at whatever level each ciphertext is.
  * Requests rotating the same input share its ModUp.  On success ops[i].out holds the result handle.
