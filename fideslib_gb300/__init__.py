@@ -44,6 +44,7 @@ _lib = None
 _SIGS = {
     "fides_last_error": (C.c_char_p, []),
     "fides_version": (C.c_char_p, []),
+    "fides_find_primes": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint64, u64p, C.c_uint32, u64p]),
     "fides_ctx_create": (C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "fides_ctx_destroy": (C.c_int, [C.c_void_p]),
     "fides_ctx_moduli": (C.c_int, [C.c_void_p, u64p, u64p]),
@@ -86,7 +87,10 @@ _SIGS = {
     "fides_mod_raise": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_lt_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, u64p, C.POINTER(C.c_uint8),
                                   C.c_double, u32p]),
+    "fides_lt_create_strided": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
+                                          u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fides_eval_mult_monomial": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_linear_transform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_chebyshev": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                        C.c_double, C.c_double, u32p]),
@@ -320,14 +324,19 @@ class CryptoContext:
     def mod_raise(self, a: int, towers: int) -> int:
         return self._un(lib().fides_mod_raise, a, towers)
 
-    def lt_create(self, bs: int, gs: int, diags: np.ndarray, present, scale: float = 1.0) -> int:
-        """diags: u64[gs*bs][towers][N] (diagonal g*bs+b pre-rotated by -g*bs); present: bool[gs*bs]."""
+    def lt_create(self, bs: int, gs: int, diags: np.ndarray, present, scale: float = 1.0, stride: int = 1,
+                  base: int = 0) -> int:
+        """diags: u64[gs*bs][towers][N], diagonal k = g*bs+b (slot offset base + k*stride) pre-rotated by
+        -(base + g*bs*stride); present: bool[gs*bs]."""
         diags = np.ascontiguousarray(diags, dtype=np.uint64)
         pres = np.ascontiguousarray(np.array(present, dtype=np.uint8))
         h = C.c_uint32()
-        _check(lib().fides_lt_create(self._h, bs, gs, diags.shape[1], _p(diags), pres.ctypes.data_as(
-            C.POINTER(C.c_uint8)), scale, C.byref(h)))
+        _check(lib().fides_lt_create_strided(self._h, bs, gs, stride, base, diags.shape[1], _p(diags),
+                                             pres.ctypes.data_as(C.POINTER(C.c_uint8)), scale, C.byref(h)))
         return h.value
+
+    def eval_mult_monomial(self, a: int, k: int) -> int:
+        return self._un(lib().fides_eval_mult_monomial, a, k)
 
     def lt_free(self, h: int):
         _check(lib().fides_lt_free(self._h, h))

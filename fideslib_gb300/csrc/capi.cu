@@ -69,6 +69,51 @@ extern "C" {
 const char* fides_last_error(void) { return g_err.c_str(); }
 const char* fides_version(void) { return "fideslib_gb300 0.1 (sm_103a)"; }
 
+int fides_find_primes(uint32_t bits, uint32_t count, uint64_t two_n, const uint64_t* exclude, uint32_t nexclude,
+                      uint64_t* out) {
+  if (!out || bits < 2 || bits > 62 || two_n < 2) return 0;
+  typedef unsigned __int128 u128;
+  auto mulmod = [](uint64_t a, uint64_t b, uint64_t m) { return (uint64_t)((u128)a * b % m); };
+  auto powmod = [&](uint64_t a, uint64_t e, uint64_t m) {
+    uint64_t r = 1 % m;
+    for (a %= m; e; e >>= 1, a = mulmod(a, a, m))
+      if (e & 1) r = mulmod(r, a, m);
+    return r;
+  };
+  auto is_prime = [&](uint64_t n) {
+    if (n < 2) return false;
+    for (uint64_t q : {2ull, 3ull, 5ull, 7ull, 11ull, 13ull, 17ull, 19ull, 23ull, 29ull, 31ull, 37ull})
+      if (n % q == 0) return n == q;
+    uint64_t d = n - 1;
+    int r = 0;
+    while (!(d & 1)) {
+      d >>= 1;
+      r++;
+    }
+    for (uint64_t a : {2ull, 325ull, 9375ull, 28178ull, 450775ull, 9780504ull, 1795265022ull}) {
+      if (!(a %= n)) continue;
+      uint64_t x = powmod(a, d, n);
+      if (x == 1 || x == n - 1) continue;
+      bool comp = true;
+      for (int k = 1; k < r && comp; k++)
+        if ((x = mulmod(x, x, n)) == n - 1) comp = false;
+      if (comp) return false;
+    }
+    return true;
+  };
+  const uint64_t top = (1ull << bits) - 1;
+  uint64_t c = top - top % two_n + 1;
+  if (c > top) c -= two_n;
+  uint32_t found = 0;
+  for (; found < count && c > two_n; c -= two_n) {
+    bool skip = false;
+    for (uint32_t i = 0; i < nexclude && !skip; i++) skip = exclude[i] == c;
+    for (uint32_t i = 0; i < found && !skip; i++) skip = out[i] == c;
+    if (!skip && is_prime(c)) out[found++] = c;
+  }
+  return (int)found;
+}
+
 int fides_ctx_create(const fides_params* p, fides_ctx** out) {
   if (!p || !out || !p->moduli) return fail(FIDES_EINVAL, "null argument");
   int ndev = 0;
@@ -596,13 +641,21 @@ int fides_mod_raise(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out) 
 
 int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, const uint64_t* diags,
                     const uint8_t* present, double scale, uint32_t* handle) {
+  return fides_lt_create_strided(ctx, bs, gs, 1, 0, towers, diags, present, scale, handle);
+}
+
+int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
+                            const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle) {
   if (!valid_ctx(ctx) || !diags || !present || !handle) return fail(FIDES_EINVAL, "null argument");
   fgb::Context* c = ctx->c;
   if (bs < 1 || gs < 1 || gs > (uint32_t)fgb::kMaxJobs || towers < 1 || towers > (uint32_t)c->nq)
     return fail(FIDES_EINVAL, "need bs >= 1, 1 <= gs <= 64, 1 <= towers <= nq");
+  if (bs > 1 && stride == 0) return fail(FIDES_EINVAL, "stride must be nonzero");
   fgb::DevLT lt;
   lt.bs = (int)bs;
   lt.gs = (int)gs;
+  lt.stride = (int)stride;
+  lt.base = (int)base;
   lt.t = (int)towers;
   lt.scale = scale;
   lt.present.assign(present, present + (size_t)bs * gs);
@@ -642,12 +695,16 @@ int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_
   if (int rc0 = check_ks_shape(ctx)) return rc0;
   const fgb::DevLT& L = it->second;
   if (A->t > L.t) return fail(FIDES_EINVAL, "ciphertext has more towers than the transform's diagonals");
-  for (int b = 1; b < L.bs; b++)
-    if (!c->rot_keys.count(fgb::Context::galois_for_index(c->N, b)))
-      return fail(FIDES_ENOKEY, "missing baby-step rotation key for index " + std::to_string(b));
-  for (int g = 1; g < L.gs; g++)
-    if (!c->rot_keys.count(fgb::Context::galois_for_index(c->N, g * L.bs)))
-      return fail(FIDES_ENOKEY, "missing giant-step rotation key for index " + std::to_string(g * L.bs));
+  for (int32_t r : L.baby_rotations(c->N))
+    if (r && !c->rot_keys.count(fgb::Context::galois_for_index(c->N, r)))
+      return fail(FIDES_ENOKEY, "missing baby-step rotation key for index " + std::to_string(r));
+  const std::vector<int32_t> giant = L.giant_rotations(c->N);
+  for (int g = 0; g < L.gs; g++) {
+    bool any = false;
+    for (int b = 0; b < L.bs; b++) any = any || L.present[(size_t)g * L.bs + b];
+    if (any && giant[g] && !c->rot_keys.count(fgb::Context::galois_for_index(c->N, giant[g])))
+      return fail(FIDES_ENOKEY, "missing giant-step rotation key for index " + std::to_string(giant[g]));
+  }
   fgb::DevCt meta = *A;
   meta.scale = A->scale * L.scale;
   meta.noise_deg = A->noise_deg + 1;
@@ -655,6 +712,19 @@ int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_
   int rc = new_ct(ctx, A->t, meta, &r);
   if (rc) return rc;
   CK(c->linear_transform(A->data, A->t, L, r.data, c->stream), "linear transform");
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_eval_mult_monomial(fides_ctx* ctx, uint32_t a, uint32_t k, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(a));
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, *A, &r);
+  if (rc) return rc;
+  CK(c->mult_monomial(A->data, A->t, k, r.data, c->stream), "monomial multiplication");
   *out = register_ct(ctx, r);
   return FIDES_OK;
 }

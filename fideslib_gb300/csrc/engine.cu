@@ -613,10 +613,31 @@ cudaError_t Context::add_batch(const AddReq* reqs, int n, cudaStream_t s) {
   return err;
 }
 
+namespace {
+int32_t slot_mod(int64_t r, int N) {  // rotation index reduced modulo N/2 (the order of 5 modulo 2N)
+  const int64_t h = N / 2;
+  r %= h;
+  return (int32_t)(r < 0 ? r + h : r);
+}
+}  // namespace
+
+std::vector<int32_t> DevLT::baby_rotations(int N) const {
+  std::vector<int32_t> r;
+  for (int b = 1; b < bs; b++) r.push_back(slot_mod((int64_t)b * stride, N));
+  return r;
+}
+
+std::vector<int32_t> DevLT::giant_rotations(int N) const {
+  std::vector<int32_t> r;
+  for (int g = 0; g < gs; g++) r.push_back(slot_mod(base + (int64_t)g * bs * stride, N));
+  return r;
+}
+
 cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64* out, cudaStream_t s) {
   const size_t NN = (size_t)N, CT = (size_t)2 * t * NN;
   const int bs = lt.bs, gs = lt.gs;
   if (t > lt.t || gs > kMaxJobs) return cudaErrorInvalidValue;
+  const std::vector<int32_t> baby_r = lt.baby_rotations(N), giant_r = lt.giant_rotations(N);
   std::vector<int> active;  // giant steps with at least one diagonal
   for (int g = 0; g < gs; g++) {
     bool any = false;
@@ -629,13 +650,18 @@ cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64*
   u64* inner = ws + (size_t)(bs - 1) * CT;  // [gs]
   u64* giant = inner + (size_t)gs * CT;     // [gs]
   cudaError_t err = cudaSuccess;
-  {  // baby steps: rotations of x by 1..bs-1, one shared ModUp
+  {  // baby steps: rotations of x by b*stride, one shared ModUp (a zero rotation is a copy)
     std::vector<KsReq> rq;
-    for (int b = 1; b < bs; b++) {
-      const uint32_t g = galois_for_index(N, b);
+    for (int b = 1; b < bs && err == cudaSuccess; b++) {
+      u64* dst = baby + (size_t)(b - 1) * CT;
+      if (baby_r[b - 1] == 0) {
+        err = cudaMemcpyAsync(dst, x, CT * sizeof(u64), cudaMemcpyDeviceToDevice, s);
+        continue;
+      }
+      const uint32_t g = galois_for_index(N, baby_r[b - 1]);
       auto it = rot_keys.find(g);
       if (it == rot_keys.end()) err = cudaErrorInvalidValue;
-      else rq.push_back({x + (size_t)t * NN, t, it->second, x, nullptr, baby + (size_t)(b - 1) * CT, galois_inverse(g)});
+      else rq.push_back({x + (size_t)t * NN, t, it->second, x, nullptr, dst, galois_inverse(g)});
     }
     if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
   }
@@ -652,32 +678,53 @@ cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64*
     for (int g : active) db.jobs[db.njobs++] = DotJob{inner + (size_t)g * CT, g};
     err = launch_ptdot(db, ring_, d_pc, s);
   }
-  if (err == cudaSuccess) {  // giant-step rotations, one batch
+  if (err == cudaSuccess) {  // giant-step rotations, one batch; unrotated inner sums are added directly
     std::vector<KsReq> rq;
+    const u64* plain[kMaxJobs];
+    int nplain = 0;
     for (int g : active) {
-      if (g == 0) continue;
-      const uint32_t gl = galois_for_index(N, g * bs);
+      const u64* in = inner + (size_t)g * CT;
+      if (giant_r[g] == 0) {
+        plain[nplain++] = in;
+        continue;
+      }
+      const uint32_t gl = galois_for_index(N, giant_r[g]);
       auto it = rot_keys.find(gl);
       if (it == rot_keys.end()) {
         err = cudaErrorInvalidValue;
         break;
       }
-      const u64* in = inner + (size_t)g * CT;
       rq.push_back({in + (size_t)t * NN, t, it->second, in, nullptr, giant + (size_t)(rq.size()) * CT,
                     galois_inverse(gl)});
     }
     if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
     if (err == cudaSuccess) {
-      SumBatch sb{};
-      const bool has0 = !active.empty() && active[0] == 0;
-      sb.jobs[0] = SumJob{giant, (long long)CT, (int)rq.size(), has0 ? inner : nullptr, out, t};
-      sb.njobs = 1;
-      if (!has0 && rq.empty()) err = cudaMemsetAsync(out, 0, CT * sizeof(u64), s);
-      else err = launch_sum(sb, ring_, d_pc, s);
+      // rotated terms sit contiguously in `giant`; the first unrotated one is the sum's `first` operand and any
+      // further ones (offsets that coincide modulo N/2) are appended after the rotated terms
+      int n = (int)rq.size();
+      for (int i = 1; i < nplain && err == cudaSuccess; i++, n++)
+        err = cudaMemcpyAsync(giant + (size_t)n * CT, plain[i], CT * sizeof(u64), cudaMemcpyDeviceToDevice, s);
+      if (err == cudaSuccess) {
+        if (n == 0 && nplain == 0) {
+          err = cudaMemsetAsync(out, 0, CT * sizeof(u64), s);
+        } else {
+          SumBatch sb{};
+          sb.jobs[0] = SumJob{giant, (long long)CT, n, nplain ? plain[0] : nullptr, out, t};
+          sb.njobs = 1;
+          err = launch_sum(sb, ring_, d_pc, s);
+        }
+      }
     }
   }
   free_limbs(ws, s);
   return err;
+}
+
+cudaError_t Context::mult_monomial(const u64* x, int t, unsigned k, u64* out, cudaStream_t s) {
+  MonoBatch mb{};
+  mb.jobs[0] = MonoJob{x, out, t, k & (2u * N - 1)};
+  mb.njobs = 1;
+  return launch_monomial(mb, ring_, d_pc, tabs.tw_fwd, s);
 }
 
 cudaError_t Context::mod_raise(const u64* x, int t_in, int T, u64* out, cudaStream_t s) {

@@ -33,14 +33,20 @@ struct DevPt {
   double scale = 1.0;
 };
 
-// Baby-step / giant-step linear transform: diagonals laid out contiguously [gs*bs][t][N]; diagonal
-// g*bs + b is already rotated by -g*bs (the layout the reference's LT precomputation produces).
+// Baby-step / giant-step linear transform over the diagonals at slot offsets base + k*stride, k = g*bs + b:
+//   out = sum_g rot_{base + g*bs*stride}( sum_b D[g*bs + b] (.) rot_{b*stride}(x) ).
+// Diagonals are laid out contiguously [gs*bs][t][N]; D[g*bs + b] is the diagonal of offset base + k*stride
+// already rotated by -(base + g*bs*stride) (the layout the reference's LT precomputation produces).
 struct DevLT {
   u64* diags = nullptr;
   uint8_t* present_dev = nullptr;
   std::vector<uint8_t> present;
   int bs = 0, gs = 0, t = 0;
+  int stride = 1, base = 0;
   double scale = 1.0;
+  // slot-rotation indices the transform needs keys for (nonzero modulo N/2)
+  std::vector<int32_t> baby_rotations(int N) const;
+  std::vector<int32_t> giant_rotations(int N) const;
 };
 
 class Context {
@@ -105,6 +111,7 @@ class Context {
   // y = sum_g rot_{g*bs}( sum_b lt.diag[g*bs+b] (.) rot_b(x) ): baby-step rotations share one ModUp, the inner
   // sums are one pt-dot launch, the giant-step rotations one key-switch batch, the final sum one launch.
   cudaError_t linear_transform(const u64* x, int t, const DevLT& lt, u64* out, cudaStream_t s);
+  cudaError_t mult_monomial(const u64* x, int t, unsigned k, u64* out, cudaStream_t s);
   // Raise a ciphertext's tower 0 to T towers (centred lift) — the first step of bootstrapping.
   cudaError_t mod_raise(const u64* x, int t_in, int T, u64* out, cudaStream_t s);
 

@@ -331,6 +331,27 @@ __global__ void __launch_bounds__(kT) scalar_kernel(const __grid_constant__ Scal
   J.out[o1] = shoup(J.ct[o1], w, wsh, q);
 }
 
+// grid rows per job: 2*t (poly-major).  X^k at point psi^(2 brev(i) + 1) is psi^e, e = (2 brev(i) + 1) k mod 2N;
+// psi^e = tw[brev(e)] for e < N and -tw[brev(e - N)] otherwise (psi^N = -1).
+__global__ void __launch_bounds__(kT) monomial_kernel(const __grid_constant__ MonoBatch b, Ring r,
+                                                      const PrimeConst* __restrict__ pc,
+                                                      const ulonglong2* __restrict__ tw) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const MonoJob& J = b.jobs[z];
+  const int row = (int)blockIdx.y - b.row_begin[z];
+  const int j = row >= J.t ? row - J.t : row;
+  const uint32_t i = blockIdx.x * kT + threadIdx.x;
+  const uint32_t two_n_mask = 2u * r.N - 1;
+  const uint32_t e = (uint32_t)(((2ull * brev_n(i, r.logN) + 1) * J.k) & two_n_mask);
+  const uint32_t eh = e & (r.N - 1);
+  const ulonglong2 w = tw[(size_t)j * r.N + brev_n(eh, r.logN)];
+  const u64 q = pc[j].p;
+  const size_t o = (size_t)row * r.N + i;
+  u64 v = shoup(J.ct[o], w.x, w.y, q);
+  if (e >= (uint32_t)r.N && v) v = q - v;
+  J.out[o] = v;
+}
+
 // grid rows per job: 2*t (poly-major).
 __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBatch b, Ring r,
                                                    const PrimeConst* __restrict__ pc) {
@@ -535,6 +556,16 @@ cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst*
   ScalarBatch bb;
   const int rows = with_rows(b, bb, [](const ScalarJob& j) { return j.t; });
   scalar_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_monomial(const MonoBatch& b, const Ring& r, const PrimeConst* pc, const ulonglong2* tw_fwd,
+                            cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  MonoBatch bb;
+  const int rows = with_rows(b, bb, [](const MonoJob& j) { return 2 * j.t; });
+  monomial_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc, tw_fwd);
   count_launch();
   return cudaGetLastError();
 }

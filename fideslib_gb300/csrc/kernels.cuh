@@ -168,11 +168,27 @@ struct RaiseBatch {
   RaiseJob jobs[kMaxJobs];
 };
 
+// out[p][j][i] = ct[p][j][i] * X^k evaluated at the i-th evaluation point psi^(2 brev(i) + 1): multiplication by
+// the monomial X^k, 0 <= k < 2N, done pointwise in the evaluation domain (twiddles {psi^brev(e), shoup}).
+struct MonoJob {
+  const u64* ct;
+  u64* out;
+  int t;
+  unsigned k;
+};
+struct MonoBatch {
+  int njobs;
+  int row_begin[kMaxJobs + 1];
+  MonoJob jobs[kMaxJobs];
+};
+
 cudaError_t launch_ptop(const PtBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_sum(const SumBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_raise_switch(const RaiseBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_monomial(const MonoBatch& b, const Ring& r, const PrimeConst* pc, const ulonglong2* tw_fwd,
+                            cudaStream_t s);
 
 cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                               cudaStream_t s);

@@ -64,6 +64,11 @@ typedef struct {
 const char* fides_last_error(void);
 const char* fides_version(void);
 
+/* Parameter helper (the role of OpenFHE's FirstPrime/PreviousPrime in GenCryptoContext): the `count` largest
+ * primes below 2^bits that are == 1 mod two_n, skipping `exclude`.  Returns the number found. */
+int fides_find_primes(uint32_t bits, uint32_t count, uint64_t two_n, const uint64_t* exclude, uint32_t nexclude,
+                      uint64_t* out);
+
 /* Context (LoadContext, api/CryptoContext.cpp:199-249). */
 int fides_ctx_create(const fides_params* params, fides_ctx** out);
 int fides_ctx_destroy(fides_ctx* ctx);
@@ -148,8 +153,20 @@ int fides_mod_raise(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out);
  * present[i] = 0 marks a zero diagonal.  Needs rotation keys for 1..bs-1 and for g*bs. */
 int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, const uint64_t* diags,
                     const uint8_t* present, double scale, uint32_t* handle);
+/* The same over the diagonals at slot offsets base + k*stride (k = g*bs + b), the form of one level of a
+ * factored CoeffsToSlots / SlotsToCoeffs (LinearTransform(ct, rowSize, bStep, pts, stride, offset),
+ * src/CKKS/LinearTransform.cu:63; EvalCoeffsToSlots level steps, src/CKKS/CoeffsToSlots.cu:98-150):
+ *   out = sum_g rot_{base + g*bs*stride}( sum_b D[g*bs + b] (.) rot_{b*stride}(x) ),
+ * diagonal g*bs + b supplied already rotated by -(base + g*bs*stride).  Rotation keys needed: b*stride
+ * (0 < b < bs) and base + g*bs*stride for every giant step with a present diagonal (indices taken modulo N/2;
+ * a zero rotation needs no key). */
+int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
+                            const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle);
 int fides_lt_free(fides_ctx* ctx, uint32_t handle);
 int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_t* out);
+/* Multiplication by the monomial X^k (0 <= k < 2N), pointwise in the evaluation domain; X^(N/2) multiplies
+ * every slot by i (Ciphertext::multMonomial, used by the full-slot bootstrap, src/CKKS/Bootstrap.cu:262). */
+int fides_eval_mult_monomial(fides_ctx* ctx, uint32_t a, uint32_t k, uint32_t* out);
 
 /* EvalChebyshevSeries (api/CryptoContext.hpp:154-156, src/CKKS/ApproxModEval.cu:138-370):
  * p(x) = sum_k coeffs[k] T_k((2x - lo - hi)/(hi - lo)), k < n, constants encoded at const_scale.  The exact op

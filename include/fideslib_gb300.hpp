@@ -1,0 +1,193 @@
+// fideslib_gb300 — C++ host facade over the C ABI (include/fideslib_gb300.h).
+//
+// Mirrors the method names and argument meaning of the reference's fideslib::CryptoContextImpl<DCRTPoly>
+// (api/CryptoContext.hpp:43-203) for the evaluation hot path, on raw residues instead of OpenFHE objects:
+// LoadContext (the constructor), LoadCiphertext / LoadPlaintext, EvalAdd / EvalSub / EvalMult / EvalSquare,
+// EvalRotate, EvalFastRotation, Rescale, EvalChebyshevSeries, EvalBootstrap, Synchronize.  Like the reference
+// API it reports failures by throwing (fideslib_gb300::Error carries the C status code and message); the C ABI
+// underneath never throws or exits.  Ciphertext is a shared, reference-counted device handle
+// (the reference's Ciphertext<DCRTPoly> is a shared_ptr, api/Ciphertext.hpp:13-58).
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "fideslib_gb300.h"
+
+namespace fideslib_gb300 {
+
+class Error : public std::runtime_error {
+ public:
+  Error(int code, const std::string& what) : std::runtime_error(what), code_(code) {}
+  int code() const { return code_; }
+
+ private:
+  int code_;
+};
+
+inline void check(int rc) {
+  if (rc != FIDES_OK) throw Error(rc, fides_last_error());
+}
+
+struct Params {
+  uint32_t log_n = 16;
+  std::vector<uint64_t> q;  // Q primes (OpenFHE moduli)
+  std::vector<uint64_t> p;  // special primes
+  uint32_t dnum = 3;
+  std::vector<uint64_t> roots;  // optional primitive 2N-th roots for q then p (OpenFHE root_of_unity)
+  int32_t scaling_technique = FIDES_FIXEDMANUAL;
+};
+
+// The `count` largest primes < 2^bits with p == 1 mod 2N (for building synthetic parameter sets).
+inline std::vector<uint64_t> FindPrimes(uint32_t bits, uint32_t count, uint32_t log_n,
+                                        const std::vector<uint64_t>& exclude = {}) {
+  std::vector<uint64_t> out(count);
+  const int n = fides_find_primes(bits, count, 2ull << log_n, exclude.data(), (uint32_t)exclude.size(), out.data());
+  if (n != (int)count) throw Error(FIDES_EINVAL, "not enough primes of the requested size");
+  return out;
+}
+
+class CryptoContext;
+
+class Ciphertext {
+ public:
+  Ciphertext() = default;
+  uint32_t handle() const { return h_ ? h_->id : 0; }
+  explicit operator bool() const { return (bool)h_; }
+  fides_ct_meta Meta() const {
+    fides_ct_meta m{};
+    check(fides_ct_meta_get(h_->ctx, h_->id, &m));
+    return m;
+  }
+  uint32_t GetTowers() const { return Meta().towers; }
+  uint32_t GetNoiseScaleDeg() const { return Meta().noise_deg; }
+  double GetScalingFactor() const { return Meta().scale; }
+
+ private:
+  friend class CryptoContext;
+  struct Handle {
+    Handle(fides_ctx* c, uint32_t i) : ctx(c), id(i) {}
+    Handle(const Handle&) = delete;
+    Handle& operator=(const Handle&) = delete;
+    ~Handle() { fides_ct_free(ctx, id); }
+    fides_ctx* ctx;
+    uint32_t id;
+  };
+  Ciphertext(fides_ctx* ctx, uint32_t id) : h_(std::make_shared<Handle>(ctx, id)) {}
+  std::shared_ptr<Handle> h_;
+};
+
+class Plaintext {
+ public:
+  Plaintext() = default;
+  uint32_t handle() const { return h_ ? h_->id : 0; }
+
+ private:
+  friend class CryptoContext;
+  struct Handle {
+    Handle(fides_ctx* c, uint32_t i) : ctx(c), id(i) {}
+    Handle(const Handle&) = delete;
+    Handle& operator=(const Handle&) = delete;
+    ~Handle() { fides_pt_free(ctx, id); }
+    fides_ctx* ctx;
+    uint32_t id;
+  };
+  Plaintext(fides_ctx* ctx, uint32_t id) : h_(std::make_shared<Handle>(ctx, id)) {}
+  std::shared_ptr<Handle> h_;
+};
+
+class CryptoContext {
+ public:
+  // LoadContext: moduli, roots and all derived tables to the device.
+  explicit CryptoContext(const Params& prm) {
+    std::vector<uint64_t> mods(prm.q);
+    mods.insert(mods.end(), prm.p.begin(), prm.p.end());
+    fides_params p{prm.log_n, (uint32_t)prm.q.size(), (uint32_t)prm.p.size(), prm.dnum, mods.data(),
+                   prm.roots.empty() ? nullptr : prm.roots.data(), prm.scaling_technique};
+    check(fides_ctx_create(&p, &ctx_));
+    N_ = 1u << prm.log_n;
+  }
+  ~CryptoContext() { fides_ctx_destroy(ctx_); }
+  CryptoContext(const CryptoContext&) = delete;
+  CryptoContext& operator=(const CryptoContext&) = delete;
+
+  fides_ctx* raw() const { return ctx_; }
+  uint32_t GetRingDimension() const { return N_; }
+  uint32_t GetCyclotomicOrder() const { return 2 * N_; }
+
+  // Keys: u64[2][dnum][nq+np][N] (RawKeySwitchKey::r_key layout).
+  void LoadEvalMultKey(const uint64_t* key) { check(fides_load_eval_mult_key(ctx_, key)); }
+  void LoadRotationKey(int32_t index, const uint64_t* key) {
+    check(fides_load_rotation_key(ctx_, fides_galois_element(ctx_, index), key));
+  }
+  void LoadConjugationKey(const uint64_t* key) { check(fides_load_rotation_key(ctx_, 2 * N_ - 1, key)); }
+
+  // LoadCiphertext: u64[2][towers][N] evaluation form.
+  Ciphertext LoadCiphertext(const uint64_t* data, uint32_t towers, double scale, uint32_t noise_deg = 1,
+                            uint32_t slots = 0) {
+    fides_ct_meta m{towers, noise_deg, slots, 0, scale};
+    uint32_t h;
+    check(fides_ct_load(ctx_, data, &m, &h));
+    return Ciphertext(ctx_, h);
+  }
+  std::vector<uint64_t> StoreCiphertext(const Ciphertext& ct) {
+    std::vector<uint64_t> out((size_t)2 * ct.GetTowers() * N_);
+    check(fides_ct_store(ctx_, ct.handle(), out.data(), nullptr));
+    return out;
+  }
+  Plaintext LoadPlaintext(const uint64_t* data, uint32_t towers, double scale) {
+    uint32_t h;
+    check(fides_pt_load(ctx_, data, towers, scale, &h));
+    return Plaintext(ctx_, h);
+  }
+
+  Ciphertext EvalAdd(const Ciphertext& a, const Ciphertext& b) { return bin(fides_eval_add, a, b); }
+  Ciphertext EvalSub(const Ciphertext& a, const Ciphertext& b) { return bin(fides_eval_sub, a, b); }
+  Ciphertext EvalMult(const Ciphertext& a, const Ciphertext& b) { return bin(fides_eval_mult, a, b); }
+  Ciphertext EvalMult(const Ciphertext& a, const Plaintext& p) { return wrap(fides_eval_mult_plain(ctx_, a.handle(), p.handle(), &tmp_)); }
+  Ciphertext EvalAdd(const Ciphertext& a, const Plaintext& p) { return wrap(fides_eval_add_plain(ctx_, a.handle(), p.handle(), &tmp_)); }
+  Ciphertext EvalMult(const Ciphertext& a, double v, double scale) {
+    return wrap(fides_eval_mult_scalar(ctx_, a.handle(), v, scale, &tmp_));
+  }
+  Ciphertext EvalAdd(const Ciphertext& a, double v) { return wrap(fides_eval_add_scalar(ctx_, a.handle(), v, &tmp_)); }
+  Ciphertext EvalSquare(const Ciphertext& a) { return wrap(fides_eval_square(ctx_, a.handle(), &tmp_)); }
+  Ciphertext Rescale(const Ciphertext& a) { return wrap(fides_rescale(ctx_, a.handle(), &tmp_)); }
+  Ciphertext EvalRotate(const Ciphertext& a, int32_t index) {
+    return wrap(fides_eval_rotate(ctx_, a.handle(), index, &tmp_));
+  }
+  // EvalFastRotation (hoisted): one ModUp shared by every index.
+  std::vector<Ciphertext> EvalFastRotation(const Ciphertext& a, const std::vector<int32_t>& indices) {
+    std::vector<uint32_t> outs(indices.size());
+    check(fides_eval_fast_rotation(ctx_, a.handle(), (uint32_t)indices.size(), indices.data(), outs.data()));
+    std::vector<Ciphertext> r;
+    for (uint32_t h : outs) r.push_back(Ciphertext(ctx_, h));
+    return r;
+  }
+  Ciphertext EvalChebyshevSeries(const Ciphertext& a, const std::vector<double>& coeffs, double lo, double hi,
+                                 double const_scale) {
+    return wrap(fides_eval_chebyshev(ctx_, a.handle(), coeffs.data(), (uint32_t)coeffs.size(), lo, hi, const_scale,
+                                     &tmp_));
+  }
+  Ciphertext EvalBootstrap(const Ciphertext& a, const fides_bootstrap_plan& plan) {
+    return wrap(fides_eval_bootstrap(ctx_, a.handle(), &plan, &tmp_));
+  }
+  void Synchronize() { check(fides_synchronize(ctx_)); }
+
+ private:
+  Ciphertext wrap(int rc) {
+    check(rc);
+    return Ciphertext(ctx_, tmp_);
+  }
+  template <class F>
+  Ciphertext bin(F f, const Ciphertext& a, const Ciphertext& b) {
+    return wrap(f(ctx_, a.handle(), b.handle(), &tmp_));
+  }
+  fides_ctx* ctx_ = nullptr;
+  uint32_t N_ = 0;
+  uint32_t tmp_ = 0;
+};
+
+}  // namespace fideslib_gb300

@@ -42,3 +42,20 @@ def test_errors_without_gpu_are_status_codes(so):
     rc = F.lib().fides_ctx_create(ctypes.byref(prm), ctypes.byref(h))
     assert rc in (F.FIDES_ENODEV, F.FIDES_EINVAL)
     assert F.lib().fides_last_error()
+
+
+@pytest.mark.parametrize("bits,count,log_n", [(40, 5, 13), (60, 4, 16), (55, 3, 12)])
+def test_find_primes_matches_oracle(so, bits, count, log_n):
+    """Host-only helper: the `count` largest primes < 2^bits that are 1 mod 2N, as the oracle generates them,
+    and the exclusion list skips given primes."""
+    import numpy as np
+    import oracle as O
+    out = np.zeros(count, dtype=np.uint64)
+    n = F.lib().fides_find_primes(bits, count, 2 << log_n, None, 0, out.ctypes.data_as(F.u64p))
+    assert n == count
+    assert [int(x) for x in out] == O.gen_primes(bits, count, 2 << log_n)
+    ex = out[:2].copy()
+    got = np.zeros(count, dtype=np.uint64)
+    n = F.lib().fides_find_primes(bits, count, 2 << log_n, ex.ctypes.data_as(F.u64p), 2, got.ctypes.data_as(F.u64p))
+    assert n == count
+    assert [int(x) for x in got] == O.gen_primes(bits, count + 2, 2 << log_n)[2:]
