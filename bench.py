@@ -7,8 +7,9 @@ each rotated once by an index from {+-2^k}; 32 rotation keys resident in HBM.  O
 `value` is HRotate ops/s with inputs resident in HBM; `e2e` is the same through the C ABI from pinned host
 buffers (H2D of every input ciphertext, D2H of every result inside the timed region).
 
-Alongside: config 3a (one ciphertext, 32 hoisted rotations) and config 2 (batched NTT -> INTT over 16
-polynomials x 40 primes at N = 2^16), whose kernel gives the roofline object.  Inputs are seeded synthetic
+Alongside: config 3a (one ciphertext, 32 hoisted rotations), config 4 (served request stream), config 5
+(eight full-slot bootstraps in flight) and config 2 (batched NTT -> INTT over 16 polynomials x 40 primes at
+N = 2^16), whose kernel gives the roofline object.  Inputs are seeded synthetic
 residues of those shapes (random keys cost exactly what real keys cost); every working set exceeds L2.
 
 `--impl reference` times the CPU restatement of the same op (oracle/, OpenMP over towers) on this host.
@@ -291,6 +292,7 @@ def run_ours(args, rank, world, dist):
     hoisted_ms = a.elapsed_time(b) / reps
 
     served = None if args.no_served else served_bench(args, dev)
+    boot = None if args.no_bootstrap else boot_bench(args, dev)
 
     # config 2: batched NTT -> INTT, 16 polys x 40 primes, kernel roofline
     ntt = ntt_bench(args, dev, stream)
@@ -328,6 +330,7 @@ def run_ours(args, rank, world, dist):
         "ntt_cfg2": ntt["summary"],
         "roofline": ntt["roofline"],
         "served_cfg4": served,
+        "bootstrap_cfg5": boot,
         "clocks": clocks,
     }
     return result
@@ -459,6 +462,106 @@ def served_bench(args, dev):
             "single_op_latency_ms_p50_n16": single}
 
 
+def boot_bench(args, dev):
+    """Config 5: CKKS bootstrapping at N = 2^16 with 32768 full slots, level budget {3, 3} (CoeffsToSlots and
+    SlotsToCoeffs each three factors of the special FFT, 63 diagonals per factor), sparse-secret encapsulation
+    (two switch keys), EvalMod = Chebyshev degree 47 on [-12.5K, 12.5K] + 3 double angles (K = q_0 / 2^55), on
+    the config-3 moduli (ModRaise to 30 towers, 12 left after).  Eight bootstraps in flight together
+    (fides_eval_bootstrap_batch: every step one batched launch for all eight) against the same eight one at a
+    time.  Keys and diagonals are seeded random residues of the real shapes (the op sequence and its cost do not
+    depend on their values)."""
+    import numpy as np
+    import numpy.polynomial.chebyshev as Cheb
+    import torch
+
+    import fideslib_gb300 as F
+    from fideslib_gb300 import bootplan as BP
+    mods = moduli_cfg3()
+    ctx = F.CryptoContext(LOGN, mods, NP, DNUM)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0x5EED0005)
+    modt = torch.tensor(mods, dtype=torch.int64, device=dev)
+
+    def rand_key():
+        k = torch.randint(0, 1 << 62, (2, DNUM, NQ + NP, N), dtype=torch.int64, device=dev, generator=gen)
+        return k % modt.view(1, 1, -1, 1)
+
+    k = rand_key()
+    ctx.load_eval_mult_key_device(k.data_ptr())
+    ctx.load_rotation_key_device(2 * N - 1, k.data_ptr())
+    for kid in (1, 2):
+        ctx.load_switch_key_device(kid, k.data_ptr())
+    n = N // 2
+    lts = {True: [], False: []}
+    need = set()
+    diag_towers = NQ
+    for inverse in (True, False):
+        for M, stride, r in BP.factors(n, 3, inverse, scale=n / N if inverse else 1.0):
+            bs, gs, base, slots = BP.bsgs_layout(M, n, stride, r)
+            need |= BP.rotation_indices(n, N, stride, bs, gs, base, slots)
+            d = torch.randint(0, 1 << 62, (bs * gs, diag_towers, N), dtype=torch.int64, device=dev, generator=gen)
+            d %= modt[:diag_towers].view(1, -1, 1)
+            present = [s is not None for s in slots]
+            lts[inverse].append(ctx.lt_create_device(bs, gs, d.data_ptr(), diag_towers, present, 2.0 ** 50,
+                                                     stride=stride, base=base))
+            del d
+    for idx in sorted(need):
+        k = rand_key()
+        ctx.load_rotation_key_device(ctx.galois(idx), k.data_ptr())
+    del k
+    delta_m = 2.0 ** 55
+    K = mods[0] / delta_m
+    lo, hi = -12.5 * K, 12.5 * K
+    f = lambda r: np.cos(2 * np.pi * (r / K - 0.25) / 8)  # noqa: E731
+    coeffs = Cheb.chebinterpolate(lambda u: f(lo + (u + 1) * (hi - lo) / 2), 47)
+    plan = F.BootstrapPlan.make(n, NQ, lts[True], lts[False], coeffs, 3, lo, hi, 2.0 ** 50, sse_keys=(1, 2))
+    m = 8
+    hs = []
+    for _ in range(m):
+        x = torch.randint(0, 1 << 62, (2, 1, N), dtype=torch.int64, device=dev, generator=gen) % modt[0]
+        hs.append(ctx.load_ciphertext_device(x.data_ptr(), 1, scale=delta_m))
+    torch.cuda.synchronize()
+
+    def timed(fn, reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        return max(a.elapsed_time(b), (time.perf_counter() - t0) * 1e3) / reps
+
+    def batched():
+        for o in ctx.eval_bootstrap_batch(hs, plan):
+            ctx.free(o)
+
+    def one_at_a_time():
+        for h in hs:
+            ctx.free(ctx.eval_bootstrap(h, plan))
+
+    out = ctx.eval_bootstrap(hs[0], plan)
+    towers_left = ctx.meta(out).towers
+    ctx.free(out)
+    batched()
+    launches0 = F.kernel_launches()
+    batch_ms = timed(batched, 2)
+    launches = (F.kernel_launches() - launches0) // 2
+    single_ms = timed(one_at_a_time, 1)
+    ctx.close()
+    torch.cuda.synchronize()
+    return {"workload": "cfg5: bootstrap N=2^16, 32768 full slots, level budget {3,3}, sparse-secret "
+                        "encapsulation, Chebyshev 47 + 3 double angles, 8 in flight",
+            "rotation_keys": len(need) + 1, "towers_after": towers_left,
+            "batched_8": {"ms": round(batch_ms, 2), "bootstraps_per_s": round(m / (batch_ms / 1e3), 2),
+                          "gpu_launches": int(launches)},
+            "one_at_a_time_8": {"ms": round(single_ms, 2), "bootstraps_per_s": round(m / (single_ms / 1e3), 2),
+                                "ms_per_bootstrap": round(single_ms / m, 2)},
+            "batched_over_one_at_a_time": round(single_ms / batch_ms, 3)}
+
+
 def ntt_bench(args, dev, stream):
     import torch
 
@@ -561,6 +664,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-bootstrap", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))

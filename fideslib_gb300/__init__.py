@@ -90,12 +90,20 @@ _SIGS = {
     "fides_lt_create_strided": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
                                           u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fides_load_switch_key": (C.c_int, [C.c_void_p, C.c_uint32, u64p]),
+    "fides_load_switch_key_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "fides_eval_key_switch": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_mult_monomial": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_linear_transform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_eval_linear_transform_batch": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.c_uint32, u32p]),
     "fides_eval_chebyshev": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                        C.c_double, C.c_double, u32p]),
     "fides_eval_double_angle": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_bootstrap": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, u32p]),
+    "fides_eval_bootstrap_batch": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.c_void_p, u32p]),
+    "fides_eval_chebyshev_batch": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.POINTER(C.c_double), C.c_uint32,
+                                             C.c_double, C.c_double, C.c_double, u32p]),
+    "fides_eval_double_angle_batch": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.c_uint32, u32p]),
     "fides_server_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "fides_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, u32p, C.POINTER(C.c_double)]),
@@ -107,7 +115,7 @@ _SIGS = {
                                             C.c_void_p]),
 }
 
-OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM = 1, 2, 3, 4, 5, 6, 7
+OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM, OP_KEY_SWITCH = 1, 2, 3, 4, 5, 6, 7, 8
 
 
 class Op(C.Structure):
@@ -219,6 +227,16 @@ class CryptoContext:
     def load_rotation_key(self, galois: int, key: np.ndarray):
         key = np.ascontiguousarray(key, dtype=np.uint64)
         _check(lib().fides_load_rotation_key(self._h, galois, _p(key)))
+
+    def load_switch_key(self, key_id: int, key: np.ndarray):
+        key = np.ascontiguousarray(key, dtype=np.uint64)
+        _check(lib().fides_load_switch_key(self._h, key_id, _p(key)))
+
+    def load_switch_key_device(self, key_id: int, ptr: int):
+        _check(lib().fides_load_switch_key_device(self._h, key_id, C.c_void_p(ptr)))
+
+    def eval_key_switch(self, a: int, key_id: int) -> int:
+        return self._un(lib().fides_eval_key_switch, a, key_id)
 
     def load_rotation_key_device(self, galois: int, ptr: int):
         _check(lib().fides_load_rotation_key_device(self._h, galois, C.c_void_p(ptr)))
@@ -335,6 +353,21 @@ class CryptoContext:
                                              pres.ctypes.data_as(C.POINTER(C.c_uint8)), scale, C.byref(h)))
         return h.value
 
+    def eval_linear_transform_batch(self, cts, lt: int) -> list[int]:
+        a = np.ascontiguousarray(np.array(cts, dtype=np.uint32))
+        out = np.zeros(len(a), dtype=np.uint32)
+        _check(lib().fides_eval_linear_transform_batch(self._h, len(a), _p(a, u32p), lt, _p(out, u32p)))
+        return [int(x) for x in out]
+
+    def lt_create_device(self, bs: int, gs: int, ptr: int, towers: int, present, scale: float = 1.0,
+                         stride: int = 1, base: int = 0) -> int:
+        """Diagonals already in device memory (u64[gs*bs][towers][N] at ptr)."""
+        pres = np.ascontiguousarray(np.array(present, dtype=np.uint8))
+        h = C.c_uint32()
+        _check(lib().fides_lt_create_strided(self._h, bs, gs, stride, base, towers, C.cast(C.c_void_p(ptr), u64p),
+                                             pres.ctypes.data_as(C.POINTER(C.c_uint8)), scale, C.byref(h)))
+        return h.value
+
     def eval_mult_monomial(self, a: int, k: int) -> int:
         return self._un(lib().fides_eval_mult_monomial, a, k)
 
@@ -354,6 +387,23 @@ class CryptoContext:
 
     def eval_bootstrap(self, a: int, plan: "BootstrapPlan") -> int:
         return self._un(lib().fides_eval_bootstrap, a, C.byref(plan))
+
+    def _many(self, fn, cts, *args) -> list[int]:
+        a = np.ascontiguousarray(np.array(cts, dtype=np.uint32))
+        out = np.zeros(len(a), dtype=np.uint32)
+        _check(fn(self._h, len(a), _p(a, u32p), *args, _p(out, u32p)))
+        return [int(x) for x in out]
+
+    def eval_bootstrap_batch(self, cts, plan: "BootstrapPlan") -> list[int]:
+        return self._many(lib().fides_eval_bootstrap_batch, cts, C.byref(plan))
+
+    def eval_chebyshev_batch(self, cts, coeffs, lo: float, hi: float, const_scale: float) -> list[int]:
+        c = np.ascontiguousarray(np.array(coeffs, dtype=np.float64))
+        return self._many(lib().fides_eval_chebyshev_batch, cts, c.ctypes.data_as(C.POINTER(C.c_double)), len(c),
+                          lo, hi, const_scale)
+
+    def eval_double_angle_batch(self, cts, iterations: int) -> list[int]:
+        return self._many(lib().fides_eval_double_angle_batch, cts, iterations)
 
     def eval_batch(self, ops) -> list[int]:
         """ops: iterable of (op_code, a, b, index); returns result handles (one batched pipeline per op family)."""
@@ -377,10 +427,32 @@ def kernel_launches() -> int:
 
 
 class BootstrapPlan(C.Structure):
-    _fields_ = [("slots", C.c_uint32), ("raise_towers", C.c_uint32), ("lt_cts_re", C.c_uint32),
-                ("lt_cts_im", C.c_uint32), ("lt_stc_re", C.c_uint32), ("lt_stc_im", C.c_uint32),
+    _fields_ = [("slots", C.c_uint32), ("raise_towers", C.c_uint32), ("cts_count", C.c_uint32),
+                ("lt_cts", C.c_uint32 * 4), ("stc_count", C.c_uint32), ("lt_stc", C.c_uint32 * 4),
+                ("sse", C.c_uint32), ("sse_to_sparse", C.c_uint32), ("sse_to_dense", C.c_uint32),
                 ("cheb_coeffs", C.POINTER(C.c_double)), ("cheb_n", C.c_uint32), ("double_angle", C.c_uint32),
                 ("cheb_lo", C.c_double), ("cheb_hi", C.c_double), ("const_scale", C.c_double)]
+
+    @classmethod
+    def make(cls, slots: int, raise_towers: int, lt_cts, lt_stc, coeffs: np.ndarray, double_angle: int,
+             lo: float, hi: float, const_scale: float, sse_keys=None) -> "BootstrapPlan":
+        """lt_cts / lt_stc: factor handles in application order; sse_keys: (to_sparse_id, to_dense_id) or None.
+        Keeps a reference to the coefficient buffer for the plan's lifetime."""
+        c = np.ascontiguousarray(np.array(coeffs, dtype=np.float64))
+        p = cls()
+        p.slots, p.raise_towers = slots, raise_towers
+        p.cts_count, p.stc_count = len(lt_cts), len(lt_stc)
+        for i, h in enumerate(lt_cts):
+            p.lt_cts[i] = h
+        for i, h in enumerate(lt_stc):
+            p.lt_stc[i] = h
+        if sse_keys is not None:
+            p.sse, p.sse_to_sparse, p.sse_to_dense = 1, sse_keys[0], sse_keys[1]
+        p.cheb_coeffs = c.ctypes.data_as(C.POINTER(C.c_double))
+        p.cheb_n, p.double_angle = len(c), double_angle
+        p.cheb_lo, p.cheb_hi, p.const_scale = lo, hi, const_scale
+        p._coeffs = c
+        return p
 
 
 class ServerConfig(C.Structure):

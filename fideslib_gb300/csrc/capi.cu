@@ -242,6 +242,23 @@ int fides_load_rotation_key_device(fides_ctx* ctx, uint32_t galois, const uint64
   return load_key(ctx, dev_key, true, &slot);
 }
 
+// Switch keys share the rotation-key table under tagged ids that no Galois element (< 2N <= 2^17) can take.
+constexpr uint32_t kSwitchKeyTag = 0x80000000u;
+
+int fides_load_switch_key(fides_ctx* ctx, uint32_t key_id, const uint64_t* key) {
+  if (!valid_ctx(ctx) || !key) return fail(FIDES_EINVAL, "null argument");
+  if (key_id & kSwitchKeyTag) return fail(FIDES_EINVAL, "switch key id must be < 2^31");
+  fgb::u64*& slot = ctx->c->rot_keys[kSwitchKeyTag | key_id];
+  return load_key(ctx, key, false, &slot);
+}
+
+int fides_load_switch_key_device(fides_ctx* ctx, uint32_t key_id, const uint64_t* dev_key) {
+  if (!valid_ctx(ctx) || !dev_key) return fail(FIDES_EINVAL, "null argument");
+  if (key_id & kSwitchKeyTag) return fail(FIDES_EINVAL, "switch key id must be < 2^31");
+  fgb::u64*& slot = ctx->c->rot_keys[kSwitchKeyTag | key_id];
+  return load_key(ctx, dev_key, true, &slot);
+}
+
 static int ct_load_impl(fides_ctx* ctx, const uint64_t* data, const fides_ct_meta* meta, uint32_t* handle,
                         bool device) {
   if (!valid_ctx(ctx) || !data || !meta || !handle) return fail(FIDES_EINVAL, "null argument");
@@ -308,7 +325,7 @@ struct Pending {
   fgb::DevCt out;
   const fgb::DevCt* a = nullptr;
   const fgb::DevCt* b = nullptr;
-  uint32_t galois = 0;
+  uint32_t galois_inv = 1;  // automorphism applied after the key switch (1 = none)
   const fgb::u64* key = nullptr;
 };
 
@@ -348,13 +365,19 @@ static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
       meta.scale = A->scale / (double)c->mod[A->t - 1];
       break;
     case FIDES_OP_ROTATE:
-    case FIDES_OP_AUTOMORPHISM: {
-      const uint32_t g = op.op == FIDES_OP_ROTATE ? fgb::Context::galois_for_index(c->N, op.index) : (uint32_t)op.index;
+    case FIDES_OP_AUTOMORPHISM:
+    case FIDES_OP_KEY_SWITCH: {
+      const bool ks = op.op == FIDES_OP_KEY_SWITCH;
+      if (ks && ((uint32_t)op.index & kSwitchKeyTag)) return fail(FIDES_EINVAL, "switch key id must be < 2^31");
+      const uint32_t g = op.op == FIDES_OP_ROTATE ? fgb::Context::galois_for_index(c->N, op.index)
+                         : ks                     ? kSwitchKeyTag | (uint32_t)op.index
+                                                  : (uint32_t)op.index;
       auto it = c->rot_keys.find(g);
       if (it == c->rot_keys.end())
-        return fail(FIDES_ENOKEY, "no rotation key for Galois element " + std::to_string(g));
+        return fail(FIDES_ENOKEY, ks ? "no switch key with id " + std::to_string(op.index)
+                                     : "no rotation key for Galois element " + std::to_string(g));
       if (int rc = check_ks_shape(ctx)) return rc;
-      pd->galois = g;
+      pd->galois_inv = ks ? 1u : c->galois_inverse(g);
       pd->key = it->second;
       break;
     }
@@ -401,8 +424,7 @@ static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
         rescales.push_back({p.a->data, t, p.out.data});
         break;
       default:
-        rots.push_back({p.a->data + (size_t)t * NN, t, p.key, p.a->data, nullptr, p.out.data,
-                        c->galois_inverse(p.galois)});
+        rots.push_back({p.a->data + (size_t)t * NN, t, p.key, p.a->data, nullptr, p.out.data, p.galois_inv});
     }
   }
   cudaError_t e = c->add_batch(adds.data(), (int)adds.size(), c->stream);
@@ -440,6 +462,10 @@ int fides_eval_rotate(fides_ctx* ctx, uint32_t a, int32_t index, uint32_t* out) 
 }
 int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out) {
   return one(ctx, FIDES_OP_AUTOMORPHISM, a, 0, (int32_t)galois, out);
+}
+
+int fides_eval_key_switch(fides_ctx* ctx, uint32_t a, uint32_t key_id, uint32_t* out) {
+  return one(ctx, FIDES_OP_KEY_SWITCH, a, 0, (int32_t)key_id, out);
 }
 
 int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs) {
@@ -666,7 +692,7 @@ int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t st
   CK(cudaMalloc(&pd, (size_t)bs * gs), "linear transform allocation");
   lt.diags = (fgb::u64*)d;
   lt.present_dev = (uint8_t*)pd;
-  CK(cudaMemcpyAsync(d, diags, bytes, cudaMemcpyHostToDevice, c->stream), "linear transform copy");
+  CK(cudaMemcpyAsync(d, diags, bytes, cudaMemcpyDefault, c->stream), "linear transform copy");
   CK(cudaMemcpyAsync(pd, present, (size_t)bs * gs, cudaMemcpyHostToDevice, c->stream), "linear transform copy");
   CK(cudaStreamSynchronize(c->stream), "linear transform copy");
   const uint32_t h = c->next_handle++;
@@ -687,14 +713,25 @@ int fides_lt_free(fides_ctx* ctx, uint32_t handle) {
 }
 
 int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_t* out) {
-  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  return fides_eval_linear_transform_batch(ctx, 1, &a, lt, out);
+}
+
+int fides_eval_linear_transform_batch(fides_ctx* ctx, uint32_t n, const uint32_t* cts, uint32_t lt, uint32_t* outs) {
+  if (!valid_ctx(ctx) || !cts || !outs) return fail(FIDES_EINVAL, "null argument");
+  if (n == 0) return FIDES_OK;
   fgb::Context* c = ctx->c;
-  fgb::DevCt* A = find_ct(ctx, a);
   auto it = c->lts.find(lt);
-  if (!A || it == c->lts.end()) return fail(FIDES_EINVAL, "unknown ciphertext or linear transform handle");
+  if (it == c->lts.end()) return fail(FIDES_EINVAL, "unknown linear transform handle");
   if (int rc0 = check_ks_shape(ctx)) return rc0;
   const fgb::DevLT& L = it->second;
-  if (A->t > L.t) return fail(FIDES_EINVAL, "ciphertext has more towers than the transform's diagonals");
+  std::vector<fgb::DevCt*> A(n);
+  for (uint32_t i = 0; i < n; i++) {
+    A[i] = find_ct(ctx, cts[i]);
+    if (!A[i]) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(cts[i]));
+    if (A[i]->t != A[0]->t) return fail(FIDES_EINVAL, "batched transform inputs must have the same tower count");
+  }
+  const int t = A[0]->t;
+  if (t > L.t) return fail(FIDES_EINVAL, "ciphertext has more towers than the transform's diagonals");
   for (int32_t r : L.baby_rotations(c->N))
     if (r && !c->rot_keys.count(fgb::Context::galois_for_index(c->N, r)))
       return fail(FIDES_ENOKEY, "missing baby-step rotation key for index " + std::to_string(r));
@@ -705,14 +742,27 @@ int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_
     if (any && giant[g] && !c->rot_keys.count(fgb::Context::galois_for_index(c->N, giant[g])))
       return fail(FIDES_ENOKEY, "missing giant-step rotation key for index " + std::to_string(giant[g]));
   }
-  fgb::DevCt meta = *A;
-  meta.scale = A->scale * L.scale;
-  meta.noise_deg = A->noise_deg + 1;
-  fgb::DevCt r;
-  int rc = new_ct(ctx, A->t, meta, &r);
-  if (rc) return rc;
-  CK(c->linear_transform(A->data, A->t, L, r.data, c->stream), "linear transform");
-  *out = register_ct(ctx, r);
+  std::vector<fgb::DevCt> R(n);
+  std::vector<const fgb::u64*> xs(n);
+  std::vector<fgb::u64*> ys(n);
+  for (uint32_t i = 0; i < n; i++) {
+    fgb::DevCt meta = *A[i];
+    meta.scale = A[i]->scale * L.scale;
+    meta.noise_deg = A[i]->noise_deg + 1;
+    int rc = new_ct(ctx, t, meta, &R[i]);
+    if (rc) {
+      for (uint32_t k = 0; k < i; k++) c->free_limbs(R[k].data, c->stream);
+      return rc;
+    }
+    xs[i] = A[i]->data;
+    ys[i] = R[i].data;
+  }
+  const cudaError_t e = c->linear_transform_batch(xs.data(), (int)n, t, L, ys.data(), c->stream);
+  if (e != cudaSuccess) {
+    for (uint32_t k = 0; k < n; k++) c->free_limbs(R[k].data, c->stream);
+    return cuda_fail(e, "linear transform");
+  }
+  for (uint32_t i = 0; i < n; i++) outs[i] = register_ct(ctx, R[i]);
   return FIDES_OK;
 }
 

@@ -634,8 +634,14 @@ std::vector<int32_t> DevLT::giant_rotations(int N) const {
 }
 
 cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64* out, cudaStream_t s) {
+  return linear_transform_batch(&x, 1, t, lt, &out, s);
+}
+
+cudaError_t Context::linear_transform_batch(const u64* const* xs, int n, int t, const DevLT& lt, u64* const* outs,
+                                            cudaStream_t s) {
   const size_t NN = (size_t)N, CT = (size_t)2 * t * NN;
   const int bs = lt.bs, gs = lt.gs;
+  if (n <= 0) return cudaSuccess;
   if (t > lt.t || gs > kMaxJobs) return cudaErrorInvalidValue;
   const std::vector<int32_t> baby_r = lt.baby_rotations(N), giant_r = lt.giant_rotations(N);
   std::vector<int> active;  // giant steps with at least one diagonal
@@ -644,78 +650,87 @@ cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64*
     for (int b = 0; b < bs; b++) any = any || lt.present[(size_t)g * bs + b];
     if (any) active.push_back(g);
   }
-  u64* ws = alloc_limbs((size_t)2 * t * (size_t)(bs - 1 + 2 * gs), s);
+  const size_t per = (size_t)(bs - 1 + 2 * gs);  // ciphertext slots of workspace per input
+  u64* ws = alloc_limbs((size_t)2 * t * per * n, s);
   if (!ws) return cudaErrorMemoryAllocation;
-  u64* baby = ws;                          // [bs-1] ciphertexts
-  u64* inner = ws + (size_t)(bs - 1) * CT;  // [gs]
-  u64* giant = inner + (size_t)gs * CT;     // [gs]
+  auto baby = [&](int i, int b) { return ws + ((size_t)i * per + (b - 1)) * CT; };   // b = 1..bs-1
+  auto inner = [&](int i, int g) { return ws + ((size_t)i * per + (bs - 1) + g) * CT; };
+  auto giant = [&](int i, int k) { return ws + ((size_t)i * per + (bs - 1) + gs + k) * CT; };
   cudaError_t err = cudaSuccess;
-  {  // baby steps: rotations of x by b*stride, one shared ModUp (a zero rotation is a copy)
+  {  // baby steps: rotations of every input by b*stride, one shared ModUp per input (a zero rotation is a copy)
     std::vector<KsReq> rq;
-    for (int b = 1; b < bs && err == cudaSuccess; b++) {
-      u64* dst = baby + (size_t)(b - 1) * CT;
-      if (baby_r[b - 1] == 0) {
-        err = cudaMemcpyAsync(dst, x, CT * sizeof(u64), cudaMemcpyDeviceToDevice, s);
-        continue;
+    for (int i = 0; i < n && err == cudaSuccess; i++)
+      for (int b = 1; b < bs && err == cudaSuccess; b++) {
+        if (baby_r[b - 1] == 0) {
+          err = cudaMemcpyAsync(baby(i, b), xs[i], CT * sizeof(u64), cudaMemcpyDeviceToDevice, s);
+          continue;
+        }
+        const uint32_t g = galois_for_index(N, baby_r[b - 1]);
+        auto it = rot_keys.find(g);
+        if (it == rot_keys.end()) err = cudaErrorInvalidValue;
+        else rq.push_back({xs[i] + (size_t)t * NN, t, it->second, xs[i], nullptr, baby(i, b), galois_inverse(g)});
       }
-      const uint32_t g = galois_for_index(N, baby_r[b - 1]);
-      auto it = rot_keys.find(g);
-      if (it == rot_keys.end()) err = cudaErrorInvalidValue;
-      else rq.push_back({x + (size_t)t * NN, t, it->second, x, nullptr, dst, galois_inverse(g)});
-    }
     if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
   }
-  if (err == cudaSuccess && !active.empty()) {  // inner sums, one launch
+  {  // inner sums: one job per (input, active giant step), up to kMaxJobs per launch
     DotBatch db{};
-    db.rot0 = x;
-    db.rot_base = baby;
     db.rot_stride = (long long)CT;
     db.pt_base = lt.diags;
     db.pt_stride = (long long)lt.t * N;
     db.present = lt.present_dev;
     db.bs = bs;
     db.t = t;
-    for (int g : active) db.jobs[db.njobs++] = DotJob{inner + (size_t)g * CT, g};
-    err = launch_ptdot(db, ring_, d_pc, s);
-  }
-  if (err == cudaSuccess) {  // giant-step rotations, one batch; unrotated inner sums are added directly
-    std::vector<KsReq> rq;
-    const u64* plain[kMaxJobs];
-    int nplain = 0;
-    for (int g : active) {
-      const u64* in = inner + (size_t)g * CT;
-      if (giant_r[g] == 0) {
-        plain[nplain++] = in;
-        continue;
-      }
-      const uint32_t gl = galois_for_index(N, giant_r[g]);
-      auto it = rot_keys.find(gl);
-      if (it == rot_keys.end()) {
-        err = cudaErrorInvalidValue;
-        break;
-      }
-      rq.push_back({in + (size_t)t * NN, t, it->second, in, nullptr, giant + (size_t)(rq.size()) * CT,
-                    galois_inverse(gl)});
-    }
-    if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
-    if (err == cudaSuccess) {
-      // rotated terms sit contiguously in `giant`; the first unrotated one is the sum's `first` operand and any
-      // further ones (offsets that coincide modulo N/2) are appended after the rotated terms
-      int n = (int)rq.size();
-      for (int i = 1; i < nplain && err == cudaSuccess; i++, n++)
-        err = cudaMemcpyAsync(giant + (size_t)n * CT, plain[i], CT * sizeof(u64), cudaMemcpyDeviceToDevice, s);
-      if (err == cudaSuccess) {
-        if (n == 0 && nplain == 0) {
-          err = cudaMemsetAsync(out, 0, CT * sizeof(u64), s);
-        } else {
-          SumBatch sb{};
-          sb.jobs[0] = SumJob{giant, (long long)CT, n, nplain ? plain[0] : nullptr, out, t};
-          sb.njobs = 1;
-          err = launch_sum(sb, ring_, d_pc, s);
+    for (int i = 0; i < n && err == cudaSuccess; i++)
+      for (int g : active) {
+        db.jobs[db.njobs++] = DotJob{inner(i, g), xs[i], bs > 1 ? baby(i, 1) : nullptr, g};
+        if (db.njobs == kMaxJobs) {
+          err = launch_ptdot(db, ring_, d_pc, s);
+          db.njobs = 0;
+          if (err != cudaSuccess) break;
         }
       }
+    if (err == cudaSuccess && db.njobs) err = launch_ptdot(db, ring_, d_pc, s);
+  }
+  std::vector<int> nrot(n, 0);
+  std::vector<std::vector<const u64*>> plain(n);
+  if (err == cudaSuccess) {  // giant-step rotations of every input, one batch
+    std::vector<KsReq> rq;
+    for (int i = 0; i < n && err == cudaSuccess; i++)
+      for (int g : active) {
+        const u64* in = inner(i, g);
+        if (giant_r[g] == 0) {
+          plain[i].push_back(in);
+          continue;
+        }
+        const uint32_t gl = galois_for_index(N, giant_r[g]);
+        auto it = rot_keys.find(gl);
+        if (it == rot_keys.end()) {
+          err = cudaErrorInvalidValue;
+          break;
+        }
+        rq.push_back({in + (size_t)t * NN, t, it->second, in, nullptr, giant(i, nrot[i]++), galois_inverse(gl)});
+      }
+    if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
+  }
+  // sums: rotated terms sit contiguously at giant(i, 0..); the first unrotated one is the sum's `first`
+  // operand, further ones (offsets that coincide modulo N/2) are appended after the rotated terms
+  SumBatch sb{};
+  for (int i = 0; i < n && err == cudaSuccess; i++) {
+    int k = nrot[i];
+    for (size_t p = 1; p < plain[i].size() && err == cudaSuccess; p++, k++)
+      err = cudaMemcpyAsync(giant(i, k), plain[i][p], CT * sizeof(u64), cudaMemcpyDeviceToDevice, s);
+    if (err != cudaSuccess) break;
+    if (k == 0 && plain[i].empty()) {
+      err = cudaMemsetAsync(outs[i], 0, CT * sizeof(u64), s);
+      continue;
+    }
+    sb.jobs[sb.njobs++] = SumJob{giant(i, 0), (long long)CT, k, plain[i].empty() ? nullptr : plain[i][0], outs[i], t};
+    if (sb.njobs == kMaxJobs) {
+      err = launch_sum(sb, ring_, d_pc, s);
+      sb.njobs = 0;
     }
   }
+  if (err == cudaSuccess && sb.njobs) err = launch_sum(sb, ring_, d_pc, s);
   free_limbs(ws, s);
   return err;
 }

@@ -111,6 +111,9 @@ class Context {
   // y = sum_g rot_{g*bs}( sum_b lt.diag[g*bs+b] (.) rot_b(x) ): baby-step rotations share one ModUp, the inner
   // sums are one pt-dot launch, the giant-step rotations one key-switch batch, the final sum one launch.
   cudaError_t linear_transform(const u64* x, int t, const DevLT& lt, u64* out, cudaStream_t s);
+  // The same transform of n ciphertexts with t towers each, every stage batched over all of them.
+  cudaError_t linear_transform_batch(const u64* const* xs, int n, int t, const DevLT& lt, u64* const* outs,
+                                     cudaStream_t s);
   cudaError_t mult_monomial(const u64* x, int t, unsigned k, u64* out, cudaStream_t s);
   // Raise a ciphertext's tower 0 to T towers (centred lift) — the first step of bootstrapping.
   cudaError_t mod_raise(const u64* x, int t_in, int T, u64* out, cudaStream_t s);

@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBa
   for (int bb = 0; bb < b.bs; bb++) {
     const int i = J.g * b.bs + bb;
     if (!b.present[i]) continue;
-    const u64* ct = bb == 0 ? b.rot0 : b.rot_base + (size_t)(bb - 1) * b.rot_stride;
+    const u64* ct = bb == 0 ? J.rot0 : J.rot_base + (size_t)(bb - 1) * b.rot_stride;
     const u64 x = ct[co], w = b.pt_base[(size_t)i * b.pt_stride + po];
     acc4_mac(A, (uint32_t)(x & kMask30), (uint32_t)(x >> 30), (uint32_t)(w & kMask30), (uint32_t)(w >> 30));
     if (++terms == 16) {

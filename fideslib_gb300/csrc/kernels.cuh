@@ -121,18 +121,18 @@ struct ScalarBatch {
   ScalarJob jobs[kMaxScalarJobs];
 };
 
-// Baby-step/giant-step inner sums: job g writes out_g[p][j] = sum_{b<bs, present} rot[b][p][j] (.) pt[g*bs+b][j]
-// with rot[b] = rot_base + b*rot_stride ([2][t][N] each, rot[0] = the input itself) and pt[i] = pt_base +
-// i*pt_stride ([>=t][N] each).
+// Baby-step/giant-step inner sums: job (x, g) writes out[p][j] = sum_{b<bs, present} rot[b][p][j] (.) pt[g*bs+b][j]
+// with rot[0] = rot0 (the input itself), rot[b] = rot_base + (b-1)*rot_stride ([2][t][N] each) and
+// pt[i] = pt_base + i*pt_stride ([>=t][N] each).
 struct DotJob {
   u64* out;
+  const u64* rot0;
+  const u64* rot_base;
   int g;
 };
 struct DotBatch {
   int njobs;
   int row_begin[kMaxJobs + 1];
-  const u64* rot0;       // b = 0 term (the input ciphertext)
-  const u64* rot_base;   // b >= 1 terms: rot_base + (b-1)*rot_stride
   long long rot_stride;
   const u64* pt_base;
   long long pt_stride;

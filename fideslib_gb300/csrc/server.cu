@@ -70,8 +70,8 @@ struct fides_server {
     if (fides_ct_meta_get(ctx, op.a, &m) != FIDES_OK) return 0;
     const size_t S = (size_t)8 * N, t = m.towers, beta = (t + alpha - 1) / alpha;
     size_t limbs = 2 * t;  // output
-    if (op.op == FIDES_OP_ROTATE || op.op == FIDES_OP_AUTOMORPHISM || op.op == FIDES_OP_MULT ||
-        op.op == FIDES_OP_SQUARE)
+    if (op.op == FIDES_OP_ROTATE || op.op == FIDES_OP_AUTOMORPHISM || op.op == FIDES_OP_KEY_SWITCH ||
+        op.op == FIDES_OP_MULT || op.op == FIDES_OP_SQUARE)
       limbs += t + beta * (t + np) + 2 * (t + np) + 2 * t;
     if (op.op == FIDES_OP_MULT || op.op == FIDES_OP_SQUARE) limbs += 3 * t;
     if (op.op == FIDES_OP_RESCALE) limbs += 2 * t;

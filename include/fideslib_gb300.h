@@ -109,6 +109,11 @@ int fides_load_eval_mult_key(fides_ctx* ctx, const uint64_t* key);
 int fides_load_eval_mult_key_device(fides_ctx* ctx, const uint64_t* dev_key);
 int fides_load_rotation_key(fides_ctx* ctx, uint32_t galois, const uint64_t* key);
 int fides_load_rotation_key_device(fides_ctx* ctx, uint32_t galois, const uint64_t* dev_key);
+/* A key switching from one secret to another (same layout; key_id < 2^31 is the caller's name for it): the
+ * secret-switching keys of sparse-secret encapsulation (GetSecretSwitchingKey, src/CKKS/Context.cu:1091, used by
+ * src/CKKS/Bootstrap.cu:254-262 and 592-600). */
+int fides_load_switch_key(fides_ctx* ctx, uint32_t key_id, const uint64_t* key);
+int fides_load_switch_key_device(fides_ctx* ctx, uint32_t key_id, const uint64_t* dev_key);
 
 /* Ciphertexts (LoadCiphertext / GetOpenFHECipherText, api/CryptoContext.cpp:270-289,
  * RawCiphertext.cu:47-129). */
@@ -127,6 +132,8 @@ int fides_eval_square(fides_ctx* ctx, uint32_t a, uint32_t* out);
 int fides_rescale(fides_ctx* ctx, uint32_t a, uint32_t* out);
 int fides_eval_rotate(fides_ctx* ctx, uint32_t a, int32_t index, uint32_t* out);
 int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_t* out);
+/* Key switch with a key loaded by fides_load_switch_key (Ciphertext::keySwitch, src/CKKS/Ciphertext.cpp:1354). */
+int fides_eval_key_switch(fides_ctx* ctx, uint32_t a, uint32_t key_id, uint32_t* out);
 int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs);
 
 /* Plaintexts (RawPlainText / LoadPlaintext, RawCiphertext.cuh:37-48, api/CryptoContext.cpp:250-269):
@@ -150,7 +157,8 @@ int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* ou
 int fides_mod_raise(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out);
 /* Baby-step/giant-step linear transform (EvalLinearTransform, src/CKKS/LinearTransform.cu:63-256):
  * diags = u64[gs*bs][towers][N] evaluation form, diagonal i = g*bs + b already rotated by -g*bs;
- * present[i] = 0 marks a zero diagonal.  Needs rotation keys for 1..bs-1 and for g*bs. */
+ * present[i] = 0 marks a zero diagonal.  Needs rotation keys for 1..bs-1 and for g*bs.  `diags` may be host
+ * or device memory (copied into the transform). */
 int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, const uint64_t* diags,
                     const uint8_t* present, double scale, uint32_t* handle);
 /* The same over the diagonals at slot offsets base + k*stride (k = g*bs + b), the form of one level of a
@@ -164,6 +172,10 @@ int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t st
                             const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle);
 int fides_lt_free(fides_ctx* ctx, uint32_t handle);
 int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_t* out);
+/* The same transform of n ciphertexts with equal tower counts, each stage (baby-step rotations, inner sums,
+ * giant-step rotations, sums) run as one batch over all of them (the reference batches the inner sums of one
+ * ciphertext: DotProductPtInternal, src/CKKS/LinearTransform.cu:21-60). */
+int fides_eval_linear_transform_batch(fides_ctx* ctx, uint32_t n, const uint32_t* cts, uint32_t lt, uint32_t* outs);
 /* Multiplication by the monomial X^k (0 <= k < 2N), pointwise in the evaluation domain; X^(N/2) multiplies
  * every slot by i (Ciphertext::multMonomial, used by the full-slot bootstrap, src/CKKS/Bootstrap.cu:262). */
 int fides_eval_mult_monomial(fides_ctx* ctx, uint32_t a, uint32_t k, uint32_t* out);
@@ -176,19 +188,31 @@ int fides_eval_chebyshev(fides_ctx* ctx, uint32_t a, const double* coeffs, uint3
                          double const_scale, uint32_t* out);
 /* x <- 2x^2 - 1 applied `iterations` times (ApproxModEval.cu:724-739 double-angle iterations of EvalMod). */
 int fides_eval_double_angle(fides_ctx* ctx, uint32_t a, uint32_t iterations, uint32_t* out);
+/* The same two routines over m ciphertexts in lock step (one batched launch per step; the reference evaluates
+ * one ciphertext per call).  Results equal the single-ciphertext calls'. */
+int fides_eval_chebyshev_batch(fides_ctx* ctx, uint32_t m, const uint32_t* cts, const double* coeffs, uint32_t n,
+                               double lo, double hi, double const_scale, uint32_t* outs);
+int fides_eval_double_angle_batch(fides_ctx* ctx, uint32_t m, const uint32_t* cts, uint32_t iterations,
+                                  uint32_t* outs);
 
 /* Bootstrapping (EvalBootstrap, api/CryptoContext.cpp:1719-1768; src/CKKS/Bootstrap.cu:169-333) with the
- * caller's precomputation: CoeffsToSlots / SlotsToCoeffs diagonals (fides_lt_create) and the EvalMod
- * approximation.  Steps and conventions are documented in fideslib_gb300/csrc/bootstrap.cu.  Keys needed:
- * relinearisation, conjugation (Galois 2N-1), rotations n, 2n, ..., N/4 (sparse-slot trace) and the linear
- * transforms' baby/giant steps. */
+ * caller's precomputation: the CoeffsToSlots / SlotsToCoeffs factors of the level budget (one
+ * fides_lt_create_strided transform per factor), the EvalMod approximation and, for sparse-secret
+ * encapsulation, two switch keys.  Steps and conventions are documented in fideslib_gb300/csrc/bootstrap.cu.
+ * With n = slots: the CoeffsToSlots factors multiply (first applied rightmost) to Pi U_n^-1 / (N/n) and the
+ * SlotsToCoeffs factors to U_n Pi^-1, where U_n[j][k] = xi^(5^j k), xi = exp(i pi / 2n), and Pi is any slot
+ * permutation (the factored special FFT leaves bit-reversed order).  Keys needed: relinearisation,
+ * conjugation (Galois 2N-1), rotations n, 2n, ..., N/4 (sparse-slot trace), the factors' baby/giant steps. */
 typedef struct {
   uint32_t slots;          /* n, power of two <= N/2 */
   uint32_t raise_towers;   /* towers after ModRaise */
-  uint32_t lt_cts_re;      /* CoeffsToSlots halves: diagonals of U^-1/(2 N/2n) and -i U^-1/(2 N/2n) */
-  uint32_t lt_cts_im;
-  uint32_t lt_stc_re;      /* SlotsToCoeffs: diagonals of U and i U */
-  uint32_t lt_stc_im;
+  uint32_t cts_count;      /* CoeffsToSlots factors, 1..4 (the level budget) */
+  uint32_t lt_cts[4];      /* applied in this order, each followed by a rescale */
+  uint32_t stc_count;      /* SlotsToCoeffs factors, 1..4 */
+  uint32_t lt_stc[4];
+  uint32_t sse;            /* 1: sparse-secret encapsulation around ModRaise */
+  uint32_t sse_to_sparse;  /* switch-key ids (fides_load_switch_key): dense -> sparse at one tower, */
+  uint32_t sse_to_dense;   /* sparse -> dense after ModRaise */
   const double* cheb_coeffs;  /* Chebyshev approximation of cos(2 pi (r/K - 1/4) / 2^double_angle) */
   uint32_t cheb_n;
   uint32_t double_angle;
@@ -196,6 +220,10 @@ typedef struct {
   double const_scale;         /* scale for the constants of EvalMod */
 } fides_bootstrap_plan;
 int fides_eval_bootstrap(fides_ctx* ctx, uint32_t ct, const fides_bootstrap_plan* plan, uint32_t* out);
+/* m bootstraps in flight together: every step batched over all m ciphertexts (equal results to m single calls;
+ * the reference bootstraps one ciphertext per call). */
+int fides_eval_bootstrap_batch(fides_ctx* ctx, uint32_t m, const uint32_t* cts, const fides_bootstrap_plan* plan,
+                               uint32_t* outs);
 
 /* Batched evaluation: `n` independent requests (no request may consume another one's output) run together,
  * one launch per pipeline stage for all ciphertexts of an op family, at whatever level each ciphertext is.
@@ -203,12 +231,12 @@ int fides_eval_bootstrap(fides_ctx* ctx, uint32_t ct, const fides_bootstrap_plan
  * Generalises the reference's cross-ciphertext batching (src/CKKS/LimbPartitionBatch.cu:20-600,
  * RNSPolyBatch.cpp) to the whole key-switching pipeline. */
 enum { FIDES_OP_ADD = 1, FIDES_OP_SUB = 2, FIDES_OP_MULT = 3, FIDES_OP_SQUARE = 4, FIDES_OP_RESCALE = 5,
-       FIDES_OP_ROTATE = 6, FIDES_OP_AUTOMORPHISM = 7 };
+       FIDES_OP_ROTATE = 6, FIDES_OP_AUTOMORPHISM = 7, FIDES_OP_KEY_SWITCH = 8 };
 typedef struct {
   int32_t op;      /* FIDES_OP_* */
   uint32_t a;      /* first operand handle */
   uint32_t b;      /* second operand (ADD / SUB / MULT) */
-  int32_t index;   /* rotation index (ROTATE) or Galois element (AUTOMORPHISM) */
+  int32_t index;   /* rotation index (ROTATE), Galois element (AUTOMORPHISM) or switch-key id (KEY_SWITCH) */
   uint32_t out;    /* result handle, written by the call */
 } fides_op;
 int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n);

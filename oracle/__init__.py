@@ -95,6 +95,7 @@ def lib():
         L.orc_plain_op.argtypes = [C.c_void_p, u64p, u64p, C.c_int, C.c_int, u64p]
         L.orc_scalar_op.argtypes = [C.c_void_p, u64p, C.c_int, u64p, u64p, u64p]
         L.orc_mod_raise.argtypes = [C.c_void_p, u64p, C.c_int, C.c_int, u64p]
+        L.orc_mult_monomial.argtypes = [C.c_void_p, u64p, C.c_int, C.c_uint32, u64p]
         L.orc_rng_fill_uniform.argtypes = [C.c_void_p, C.c_uint64, u64p, C.c_int, i32p]
         L.orc_keygen_secret.argtypes = [C.c_void_p, C.c_uint64, C.c_int, i64p]
         L.orc_secret_eval.argtypes = [C.c_void_p, i64p, u64p]
@@ -309,6 +310,15 @@ class Ctx:
         lib().orc_mod_raise(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], T, _p(out))
         return out
 
+    def mult_monomial(self, ct: np.ndarray, k: int) -> np.ndarray:
+        out = self.zeros(2, ct.shape[1])
+        lib().orc_mult_monomial(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], k, _p(out))
+        return out
+
+    def key_switch(self, ct: np.ndarray, key: np.ndarray) -> np.ndarray:
+        """(c0, c1) -> (c0 + KS(c1)_0, KS(c1)_1): a rotation with the identity automorphism."""
+        return self.rotate(ct, 1, key)
+
     # --- synthetic inputs ---
     def uniform(self, seed: int, ntowers: int, tower_ids=None) -> np.ndarray:
         out = self.zeros(ntowers)
@@ -324,6 +334,13 @@ class Ctx:
     def relin_key(self, seed: int, s: np.ndarray) -> np.ndarray:
         k = np.zeros(self.key_shape(), dtype=np.uint64)
         lib().orc_relin_keygen(self._h, seed, _p(s, i64p), _p(k))
+        return k
+
+    def switch_key(self, seed: int, s_from: np.ndarray, s_to: np.ndarray) -> np.ndarray:
+        """Key switching ciphertexts under s_from to s_to."""
+        k = np.zeros(self.key_shape(), dtype=np.uint64)
+        lib().orc_ksk_gen(self._h, seed, _p(np.ascontiguousarray(s_from), i64p),
+                          _p(np.ascontiguousarray(s_to), i64p), _p(k))
         return k
 
     def rot_key(self, seed: int, s: np.ndarray, galois: int) -> np.ndarray:

@@ -625,6 +625,33 @@ void orc_mod_raise(const orc_ctx* c, const uint64_t* ct, int t_in, int T, uint64
   free(top);
 }
 
+/* Multiplication by X^k (0 <= k < 2N) as a negacyclic shift of the coefficients (X^N = -1): the definition
+ * behind Ciphertext::multMonomial (src/CKKS/Bootstrap.cu:262), computed in the coefficient domain so that it
+ * checks the evaluation-domain product independently. */
+void orc_mult_monomial(const orc_ctx* c, const uint64_t* ct, int t, uint32_t k, uint64_t* out) {
+  uint64_t N = c->N;
+  k &= (uint32_t)(2 * N - 1);
+  uint64_t* a = (uint64_t*)malloc(sizeof(uint64_t) * N);
+  for (int p = 0; p < 2; p++)
+    for (int j = 0; j < t; j++) {
+      const uint64_t q = c->mod[j];
+      memcpy(a, ct + ((size_t)p * t + j) * N, sizeof(uint64_t) * N);
+      orc_ntt_inv(a, N, q, c->itab[j]);
+      uint64_t* O = out + ((size_t)p * t + j) * N;
+      for (uint64_t i = 0; i < N; i++) {
+        uint64_t e = (i + k) % (2 * N);
+        uint64_t v = a[i];
+        if (e >= N) {
+          e -= N;
+          v = v ? q - v : 0;
+        }
+        O[e] = v;
+      }
+      orc_ntt_fwd(O, N, q, c->tab[j]);
+    }
+  free(a);
+}
+
 /* ------------------------------------------------------------------------------------------------ */
 /* synthetic inputs: SplitMix64 streams, ternary / sparse secrets, rounded-Gaussian errors (sigma 3.19) */
 /* ------------------------------------------------------------------------------------------------ */

@@ -87,6 +87,8 @@ void orc_scalar_op(const orc_ctx* c, const uint64_t* ct, int t, const uint64_t* 
                    uint64_t* out);
 /* ModRaise: tower 0 of ct (u64[2][t_in][N]) lifted, centred, to T towers (out u64[2][T][N]). */
 void orc_mod_raise(const orc_ctx* c, const uint64_t* ct, int t_in, int T, uint64_t* out);
+/* ct * X^k (0 <= k < 2N), by a negacyclic coefficient shift. */
+void orc_mult_monomial(const orc_ctx* c, const uint64_t* ct, int t, uint32_t k, uint64_t* out);
 
 /* ---- synthetic key material and messages (test inputs) ---- */
 void orc_rng_fill_uniform(const orc_ctx* c, uint64_t seed, uint64_t* x, int ntowers, const int* tower_ids);

@@ -1,127 +1,148 @@
-"""End-to-end CKKS bootstrapping on the GPU (fides_eval_bootstrap).
+"""End-to-end CKKS bootstrapping on the GPU (fides_eval_bootstrap / fides_eval_bootstrap_batch).
 
-Ring N=2^12 with 16 sparse slots, sparse ternary secret (Hamming weight 32), q_0 of 60 bits and 19 further
-45-bit towers, 4 special primes, dnum 5.  The CoeffsToSlots / SlotsToCoeffs diagonals are computed here for the
-slot order of the encoder (slot j <-> zeta^(5^j)) and encoded by the oracle, the way the reference receives its
-bootstrap plaintexts from OpenFHE.  The output is checked residue-for-residue against an op-for-op oracle replay
-of the documented bootstrap recipe, and its decrypted slots against the input message."""
+Ring N=2^12, q_0 of 60 bits and 55-bit towers, 4 special primes of 60 bits (P above every digit's modulus).
+Two shapes: 16 sparse slots with a one-factor level budget, and 2048 full slots with the level budget {3, 3}
+and sparse-secret encapsulation (main secret of Hamming weight 192, encapsulated under weight 32).  The
+CoeffsToSlots / SlotsToCoeffs factors come from the factored special FFT (tests/boot_plan.py) and are encoded by
+the oracle, the way the reference receives its bootstrap plaintexts from OpenFHE.  Every output residue is
+checked against an op-for-op oracle replay of the recipe documented in fideslib_gb300/csrc/bootstrap.cu, and
+the decrypted slots against the input message (precision stated).  A batch of bootstraps in flight together
+must give exactly the single-call results."""
 import numpy as np
 import numpy.polynomial.chebyshev as C
 import pytest
 
 import oracle as O
+from tests import boot_plan as BP
 from tests.replay import Sim
 
 pytestmark = pytest.mark.gpu
 
-LOGN, NQ, NP, DNUM, SLOTS = 12, 20, 4, 5, 16
-DELTA_M, DELTA_PT = 2.0 ** 55, 2.0 ** 55  # towers of 55 bits; q_0 / DELTA_M = 32 keeps the EvalMod gain small
-BS = GS = 4
+LOGN = 12
+N = 1 << LOGN
+NQ, NP, DNUM = 22, 4, 6  # digits of 4 towers (<= 220 bits) under P = 240 bits
+DELTA_M = DELTA_PT = 2.0 ** 55  # q_0 / DELTA_M = 32 keeps the EvalMod gain small
 R_DOUBLE = 3
 CHEB_DEG = 47
 B_RANGE = 12.5
 
 
-def slot_matrix(n):
-    zeta = np.exp(1j * np.pi / (2 * n))
-    rows = [pow(5, j, 4 * n) for j in range(n)]
-    return np.array([[zeta ** ((r * i) % (4 * n)) for i in range(n)] for r in rows])
+class Setup:
+    def __init__(self, slots, budget, sse, seed):
+        import fideslib_gb300 as F
+        self.F, self.slots = F, slots
+        self.mods = O.make_moduli(LOGN, [60] + [55] * (NQ - 1), [60] * NP)
+        self.gpu = F.CryptoContext(LOGN, self.mods, NP, DNUM)
+        self.orc = orc = O.Ctx(N, NQ, NP, DNUM, self.mods, threads=16)
+        self.s = orc.secret(seed, hamming_weight=192 if sse else 32)
+        self.rlk = orc.relin_key(seed + 1, self.s)
+        self.gpu.load_eval_mult_key(self.rlk)
+        self.sse = None
+        if sse:
+            s_sparse = orc.secret(seed + 2, hamming_weight=32)
+            self.sse = (orc.switch_key(seed + 3, self.s, s_sparse), orc.switch_key(seed + 4, s_sparse, self.s))
+            self.gpu.load_switch_key(10, self.sse[0])
+            self.gpu.load_switch_key(11, self.sse[1])
+        self.cts = [BP.Factor(orc, M, slots, stride, r, NQ, DELTA_PT)
+                    for M, stride, r in BP.factors(slots, budget[0], inverse=True, scale=slots / N)]
+        self.stc = [BP.Factor(orc, M, slots, stride, r, NQ, DELTA_PT)
+                    for M, stride, r in BP.factors(slots, budget[1], inverse=False)]
+        need = set()
+        for f in self.cts + self.stc:
+            need |= f.rotations(slots, N)
+        r = slots
+        while r < N // 2:
+            need.add(r)
+            r <<= 1
+        self.keys = {}
+        for i, idx in enumerate(sorted(need)):
+            g = orc.galois(idx)
+            self.keys[idx] = (g, orc.rot_key(seed + 100 + i, self.s, g))
+            self.gpu.load_rotation_key(g, self.keys[idx][1])
+        self.conj = (2 * N - 1, orc.rot_key(seed + 7, self.s, 2 * N - 1))
+        self.gpu.load_rotation_key(*self.conj)
+        self.K = self.mods[0] / DELTA_M
+        self.lo, self.hi = -B_RANGE * self.K, B_RANGE * self.K
+        f = lambda r: np.cos(2 * np.pi * (r / self.K - 0.25) / 2 ** R_DOUBLE)  # noqa: E731
+        lo, hi = self.lo, self.hi
+        self.coeffs = C.chebinterpolate(lambda u: f(lo + (u + 1) * (hi - lo) / 2), CHEB_DEG)
+        self.plan = F.BootstrapPlan.make(slots, NQ, [f.create(self.gpu, DELTA_PT) for f in self.cts],
+                                         [f.create(self.gpu, DELTA_PT) for f in self.stc], self.coeffs, R_DOUBLE,
+                                         self.lo, self.hi, DELTA_PT, sse_keys=(10, 11) if sse else None)
+
+    def message(self, seed):
+        rng = np.random.default_rng(seed)
+        z = (rng.uniform(-1, 1, self.slots) + 1j * rng.uniform(-1, 1, self.slots)) * 0.5
+        return z, self.orc.encrypt(seed, self.s, self.orc.encode(z, DELTA_M, 1))
+
+    def replay(self, ct):
+        """The recipe of fideslib_gb300/csrc/bootstrap.cu on the oracle, op for op."""
+        orc, sim = self.orc, Sim(self.orc, self.mods, self.rlk)
+        x = ct
+        if self.sse:
+            x = orc.key_switch(np.ascontiguousarray(x[:, :1]), self.sse[0])
+        x = orc.mod_raise(x, NQ)
+        if self.sse:
+            x = orc.key_switch(x, self.sse[1])
+        r = self.slots
+        while r < N // 2:
+            x = orc.add(x, orc.rotate(x, *self.keys[r]))
+            r <<= 1
+        v = (x, DELTA_M)
+        for f in self.cts:
+            v = sim.rescale((f.replay(orc, v[0], self.keys, N), v[1] * DELTA_PT))
+        c = orc.rotate(v[0], *self.conj)
+        halves = [(orc.add(v[0], c), v[1]), (orc.mult_monomial(orc.sub(v[0], c), 3 * N // 2), v[1])]
+        modded = []
+        for h in halves:
+            y = sim.chebyshev(h, list(self.coeffs), self.lo, self.hi, DELTA_PT)
+            for _ in range(R_DOUBLE):
+                y = sim.add_scalar(sim.mult_int(sim.rescale(sim.mult(y, y)), 2), -1.0)
+            modded.append(sim.rescale(sim.mult_scalar(y, self.K / (2 * np.pi), DELTA_PT)))
+        w = (orc.add(modded[0][0], orc.mult_monomial(modded[1][0], N // 2)), modded[0][1])
+        for f in self.stc:
+            w = sim.rescale((f.replay(orc, w[0], self.keys, N), w[1] * DELTA_PT))
+        return w
+
+    def precision(self, got, scale, z):
+        dec = self.orc.decode(self.orc.decrypt(self.s, got), scale, self.slots)
+        err = np.abs(dec - z).max()
+        return err, -np.log2(err)
 
 
-def diagonals(M):
-    n = M.shape[0]
-    return np.array([[M[j, (j + i) % n] for j in range(n)] for i in range(n)])
-
-
-def encode_lt(orc, M, towers):
-    d = diagonals(M)
-    out = np.zeros((BS * GS, towers, 1 << LOGN), dtype=np.uint64)
-    for g in range(GS):
-        for b in range(BS):
-            i = g * BS + b
-            out[i] = orc.encode(np.roll(d[i], g * BS), DELTA_PT, towers)
-    return out
-
-
-def lt_replay(orc, keys, ct, diags):
-    baby = [ct] + [orc.rotate(ct, *keys[b]) for b in range(1, BS)]
-    total = None
-    for g in range(GS):
-        inner = None
-        for b in range(BS):
-            term = orc.plain_op(baby[b], diags[g * BS + b], 0)
-            inner = term if inner is None else orc.add(inner, term)
-        if g > 0:
-            inner = orc.rotate(inner, *keys[g * BS])
-        total = inner if total is None else orc.add(total, inner)
-    return total
-
-
-def test_bootstrap_end_to_end(engine_lib):
-    import fideslib_gb300 as F
-    N = 1 << LOGN
-    mods = O.make_moduli(LOGN, [60] + [55] * (NQ - 1), [60] * NP)
-    gpu = F.CryptoContext(LOGN, mods, NP, DNUM)
-    orc = O.Ctx(N, NQ, NP, DNUM, mods, threads=16)
-    s = orc.secret(0x5EED0005, hamming_weight=32)
-    rlk = orc.relin_key(1, s)
-    gpu.load_eval_mult_key(rlk)
-    keys = {}
-    for idx in [1, 2, 3, 4, 8, 12] + [SLOTS << k for k in range(20) if (SLOTS << k) < N // 2]:
-        g = orc.galois(idx)
-        keys[idx] = (g, orc.rot_key(100 + idx, s, g))
-        gpu.load_rotation_key(g, keys[idx][1])
-    conj = (2 * N - 1, orc.rot_key(7, s, 2 * N - 1))
-    gpu.load_rotation_key(*conj)
-
-    U = slot_matrix(SLOTS)
-    A = np.linalg.inv(U) / (N // (2 * SLOTS))
-    mats = {"cts_re": A / 2, "cts_im": -0.5j * A, "stc_re": U, "stc_im": 1j * U}
-    enc = {k: encode_lt(orc, M, NQ) for k, M in mats.items()}
-    lts = {k: gpu.lt_create(BS, GS, v, np.ones(BS * GS, dtype=bool), DELTA_PT) for k, v in enc.items()}
-
-    K = mods[0] / DELTA_M
-    lo, hi = -B_RANGE * K, B_RANGE * K
-    f = lambda r: np.cos(2 * np.pi * (r / K - 0.25) / 2 ** R_DOUBLE)  # noqa: E731
-    coeffs = C.chebinterpolate(lambda u: f(lo + (u + 1) * (hi - lo) / 2), CHEB_DEG)
-    cbuf = np.ascontiguousarray(coeffs)
-    plan = F.BootstrapPlan(SLOTS, NQ, lts["cts_re"], lts["cts_im"], lts["stc_re"], lts["stc_im"],
-                           cbuf.ctypes.data_as(F.C.POINTER(F.C.c_double)), len(cbuf), R_DOUBLE, lo, hi, DELTA_PT)
-
-    rng = np.random.default_rng(77)
-    z = (rng.uniform(-1, 1, SLOTS) + 1j * rng.uniform(-1, 1, SLOTS)) * 0.5
-    ct = orc.encrypt(5, s, orc.encode(z, DELTA_M, 1))
-    h = gpu.load_ciphertext(ct, DELTA_M)
-    out = gpu.eval_bootstrap(h, plan)
+def check(setup, z, ct):
+    gpu = setup.gpu
+    out = gpu.eval_bootstrap(gpu.load_ciphertext(ct, DELTA_M), setup.plan)
     got = gpu.store_ciphertext(out)
     meta = gpu.meta(out)
-
-    # op-for-op oracle replay of the recipe in fideslib_gb300/csrc/bootstrap.cu
-    sim = Sim(orc, mods, rlk)
-    x = orc.mod_raise(ct, NQ)
-    r = SLOTS
-    while r < N // 2:
-        x = orc.add(x, orc.rotate(x, *keys[r]))
-        r <<= 1
-    halves = []
-    for name in ("cts_re", "cts_im"):
-        y = lt_replay(orc, keys, x, enc[name])
-        y = orc.add(y, orc.rotate(y, *conj))
-        halves.append(sim.rescale((y, DELTA_M * DELTA_PT)))
-    mods_out = []
-    for v in halves:
-        c = sim.chebyshev(v, list(coeffs), lo, hi, DELTA_PT)
-        for _ in range(R_DOUBLE):
-            c = sim.add_scalar(sim.mult_int(sim.rescale(sim.mult(c, c)), 2), -1.0)
-        mods_out.append(sim.rescale(sim.mult_scalar(c, K / (2 * np.pi), DELTA_PT)))
-    a = lt_replay(orc, keys, mods_out[0][0], enc["stc_re"])
-    b = lt_replay(orc, keys, mods_out[1][0], enc["stc_im"])
-    ref, ref_scale = sim.rescale((orc.add(a, b), mods_out[0][1] * DELTA_PT))
+    ref, ref_scale = setup.replay(ct)
     assert np.array_equal(got, ref)
     assert abs(meta.scale / ref_scale - 1) < 1e-9
-
-    dec = orc.decode(orc.decrypt(s, got), meta.scale, SLOTS)
-    err = np.abs(dec - z).max()
-    print(f"bootstrap: {meta.towers} towers left, max slot error {err:.3e} ({-np.log2(err):.1f} bits)")
-    assert meta.towers == NQ - 14
+    err, bits = setup.precision(got, meta.scale, z)
+    print(f"bootstrap n={setup.slots}: {meta.towers} towers left, max slot error {err:.3e} ({bits:.1f} bits)")
     assert err < 1e-3, err
+    return got, meta
+
+
+def test_bootstrap_sparse_slots():
+    st = Setup(slots=16, budget=(1, 1), sse=False, seed=0x5EED0005)
+    z, ct = st.message(77)
+    _, meta = check(st, z, ct)
+    assert meta.towers == NQ - 1 - 8 - R_DOUBLE - 1 - 1
+
+
+def test_bootstrap_full_slots_level_budget_sse_and_batch():
+    st = Setup(slots=N // 2, budget=(3, 3), sse=True, seed=0x5EED0015)
+    z, ct = st.message(78)
+    got, meta = check(st, z, ct)
+    assert meta.towers == NQ - 3 - 8 - R_DOUBLE - 1 - 3
+    # three bootstraps in flight together: the first equals the single call, the others decrypt to their inputs
+    z2, ct2 = st.message(79)
+    z3, ct3 = st.message(80)
+    gpu = st.gpu
+    hs = [gpu.load_ciphertext(c, DELTA_M) for c in (ct, ct2, ct3)]
+    outs = gpu.eval_bootstrap_batch(hs, st.plan)
+    assert np.array_equal(gpu.store_ciphertext(outs[0]), got)
+    for o, zz in zip(outs[1:], (z2, z3)):
+        err, bits = st.precision(gpu.store_ciphertext(o), gpu.meta(o).scale, zz)
+        assert err < 1e-3, err
