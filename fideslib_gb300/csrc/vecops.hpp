@@ -99,6 +99,10 @@ inline int mult_scalar(Scope& sc, const V& a, const std::vector<double>& v, doub
 inline int mult_scalar(Scope& sc, const V& a, double v, double scale, V& out) {
   return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_mult_scalar(sc.ctx, a[i], v, scale, o); });
 }
+// Per-element constant scales: element i gets round(v * scale[i]) and scale *= scale[i].
+inline int mult_scalar_at(Scope& sc, const V& a, double v, const std::vector<double>& scale, V& out) {
+  return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_mult_scalar(sc.ctx, a[i], v, scale[i], o); });
+}
 inline int add_scalar(Scope& sc, const V& a, double v, V& out) {
   return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_add_scalar(sc.ctx, a[i], v, o); });
 }
@@ -124,6 +128,12 @@ inline int drop_to(Scope& sc, const V& a, const std::vector<uint32_t>& t, V& out
     sc.keep(V{out[i]});
   }
   return FIDES_OK;
+}
+
+inline std::vector<double> scales(fides_ctx* ctx, const V& a) {
+  std::vector<double> s(a.size());
+  for (size_t i = 0; i < a.size(); i++) s[i] = scale_of(ctx, a[i]);
+  return s;
 }
 
 inline std::vector<uint32_t> towers(fides_ctx* ctx, const V& a) {

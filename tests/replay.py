@@ -46,28 +46,99 @@ class Sim:
     def sub(self, a, b):
         return (self.orc.sub(a[0], b[0]), a[1])
 
-    def chebyshev(self, x, c, lo, hi, cs):
-        d = len(c) - 1
-        T = [None] * (d + 1)
-        if lo == -1.0 and hi == 1.0:
-            T[1] = x
-        else:
-            u = self.rescale(self.mult_scalar(x, 2.0 / (hi - lo), cs))
-            T[1] = self.add_scalar(u, -(hi + lo) / (hi - lo))
-        for k in range(2, d + 1):
-            if k % 2 == 0:
-                m2 = self.mult_int(self.rescale(self.mult(T[k // 2], T[k // 2])), 2)
-                T[k] = self.add_scalar(m2, -1.0)
-            else:
-                A, B = T[(k - 1) // 2], T[(k + 1) // 2]
-                t = min(self.t(A), self.t(B))
-                m2 = self.mult_int(self.rescale(self.mult(self.drop(A, t), self.drop(B, t))), 2)
-                T[k] = self.sub(m2, self.drop(T[1], self.t(m2)))
-        tmin = min(self.t(T[k]) for k in range(1, d + 1) if c[k] != 0)
+    def _align(self, a, b):
+        t = min(self.t(a), self.t(b))
+        return self.drop(a, t), self.drop(b, t)
+
+    def _next_t(self, T, k):
+        if k % 2 == 0:
+            return self.add_scalar(self.mult_int(self.rescale(self.mult(T[k // 2], T[k // 2])), 2), -1.0)
+        A, B = self._align(T[(k - 1) // 2], T[(k + 1) // 2])
+        m2 = self.mult_int(self.rescale(self.mult(A, B)), 2)
+        t1 = self.drop(T[1], self.t(m2) + 1)
+        f = m2[1] * float(self.mods[self.t(m2)]) / t1[1]
+        return self.sub(m2, self.rescale(self.mult_scalar(t1, 1.0, f)))
+
+    def _leaf_towers(self, T, c):
+        ks = [k for k in range(1, len(c)) if c[k] != 0]
+        return min(self.t(T[k]) for k in ks) - 1 if ks else None
+
+    @staticmethod
+    def _split(c):
+        M = len(c) // 2
+        q, r = [0.0] * M, list(c[:M])
+        q[0] = c[M]
+        for j in range(1, M):
+            q[j] = 2.0 * c[M + j]
+            r[M - j] -= c[M + j]
+        return q, r
+
+    def _node_towers(self, T, G, c, i):
+        if i == 0:
+            return self._leaf_towers(T, c)
+        q, r = self._split(c)
+        tq, tr = self._node_towers(T, G, q, i - 1), self._node_towers(T, G, r, i - 1)
+        tg = self.t(G[i - 1])
+        tp = min(tq, tg) - 1 if tq is not None else (tg - 1 if q[0] != 0.0 else None)
+        if tp is None:
+            return tr
+        return tp if tr is None else min(tp, tr)
+
+    def _leaf(self, T, c, target):
+        tl = self._leaf_towers(T, c)
         acc = None
-        for k in range(1, d + 1):
+        for k in range(1, len(c)):
             if c[k] == 0:
                 continue
-            term = self.mult_scalar(self.drop(T[k], tmin), c[k], cs)
+            X = self.drop(T[k], tl + 1)
+            term = self.mult_scalar(X, c[k], target * float(self.mods[tl]) / X[1])
             acc = term if acc is None else self.add(acc, term)
-        return self.add_scalar(self.rescale(acc), c[0])
+        return (self.rescale(acc) if acc is not None else None), c[0]
+
+    def _node(self, T, G, c, i, target):
+        if i == 0:
+            return self._leaf(T, c, target)
+        q, r = self._split(c)
+        Gm = G[i - 1]
+        tg, sg = self.t(Gm), Gm[1]
+        prod = None
+        if any(x != 0.0 for x in q[1:]):
+            tq = self._node_towers(T, G, q, i - 1)
+            Qct, Qc = self._node(T, G, q, i - 1, target * float(self.mods[min(tq, tg) - 1]) / sg)
+            X = self.add_scalar(Qct, Qc) if Qc != 0.0 else Qct
+            X, Gd = self._align(X, Gm)
+            prod = self.rescale(self.mult(X, Gd))
+        elif q[0] != 0.0:
+            prod = self.rescale(self.mult_scalar(Gm, q[0], target * float(self.mods[tg - 1]) / sg))
+        Rct, Rc = self._node(T, G, r, i - 1, target)
+        if prod is None:
+            return Rct, Rc
+        if Rct is None:
+            return prod, Rc
+        pd, rd = self._align(prod, Rct)
+        return self.add(pd, rd), Rc
+
+    def chebyshev(self, x, c, lo, hi, cs):
+        """Baby-step/giant-step Chebyshev evaluation in the engine's op order (fideslib_gb300/csrc/poly_eval.cu)."""
+        d = len(c) - 1
+        if lo == -1.0 and hi == 1.0:
+            t1 = x
+        else:
+            u = self.rescale(self.mult_scalar(x, 2.0 / (hi - lo), cs))
+            t1 = self.add_scalar(u, -(hi + lo) / (hi - lo))
+        lb = max(1, int(np.floor(np.log2(d + 1) / 2.0 + 0.5)))
+        bs = 1 << lb
+        m = 0
+        while (bs << m) <= d:
+            m += 1
+        top = bs if m > 0 else bs - 1
+        T = [None, t1] + [None] * (top - 1)
+        for k in range(2, top + 1):
+            T[k] = self._next_t(T, k)
+        G = [T[bs]] if m > 0 else []
+        for i in range(1, m):
+            G.append(self.add_scalar(self.mult_int(self.rescale(self.mult(G[i - 1], G[i - 1])), 2), -1.0))
+        cc = list(c) + [0.0] * ((bs << m) - len(c))
+        ct, c0 = self._node(T, G, cc, m, t1[1])
+        assert ct is not None
+        return self.add_scalar(ct, c0)

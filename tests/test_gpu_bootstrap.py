@@ -110,7 +110,7 @@ class Setup:
         return err, -np.log2(err)
 
 
-def check(setup, z, ct):
+def check(setup, z, ct, tol):
     gpu = setup.gpu
     out = gpu.eval_bootstrap(gpu.load_ciphertext(ct, DELTA_M), setup.plan)
     got = gpu.store_ciphertext(out)
@@ -120,22 +120,22 @@ def check(setup, z, ct):
     assert abs(meta.scale / ref_scale - 1) < 1e-9
     err, bits = setup.precision(got, meta.scale, z)
     print(f"bootstrap n={setup.slots}: {meta.towers} towers left, max slot error {err:.3e} ({bits:.1f} bits)")
-    assert err < 1e-3, err
+    assert err < tol, err
     return got, meta
 
 
 def test_bootstrap_sparse_slots():
     st = Setup(slots=16, budget=(1, 1), sse=False, seed=0x5EED0005)
     z, ct = st.message(77)
-    _, meta = check(st, z, ct)
-    assert meta.towers == NQ - 1 - 8 - R_DOUBLE - 1 - 1
+    _, meta = check(st, z, ct, 1e-3)
+    assert meta.towers >= 2
 
 
 def test_bootstrap_full_slots_level_budget_sse_and_batch():
     st = Setup(slots=N // 2, budget=(3, 3), sse=True, seed=0x5EED0015)
     z, ct = st.message(78)
-    got, meta = check(st, z, ct)
-    assert meta.towers == NQ - 3 - 8 - R_DOUBLE - 1 - 3
+    got, meta = check(st, z, ct, 2e-5)
+    assert meta.towers >= 2
     # three bootstraps in flight together: the first equals the single call, the others decrypt to their inputs
     z2, ct2 = st.message(79)
     z3, ct3 = st.message(80)
@@ -145,4 +145,4 @@ def test_bootstrap_full_slots_level_budget_sse_and_batch():
     assert np.array_equal(gpu.store_ciphertext(outs[0]), got)
     for o, zz in zip(outs[1:], (z2, z3)):
         err, bits = st.precision(gpu.store_ciphertext(o), gpu.meta(o).scale, zz)
-        assert err < 1e-3, err
+        assert err < 2e-5, err
