@@ -13,9 +13,12 @@
 //     pass C  : stages on bits [3 .. 0]        (16 contiguous residues), then the store to HBM.
 //   inverse (Gentleman–Sande, bit-reversed -> natural, N^-1 applied on the way out) runs the passes in the
 //   reverse order.
+// For N = 2^13 .. 2^16 the forward transform uses a radix-16 variant of the same cluster layout (ntt16_fwd_kernel
+// below: four radix-16 passes, 16 residues per thread, three CTAs per SM).
 // Butterflies are Harvey-lazy with a cheaper quotient estimate (shoup_lazy4, products in [0, 4p)): forward
-// values live in [0, 8p), inverse in [0, 4p); outputs are reduced to [0, p).  Needs p < 2^61.  Shared memory is XOR-swizzled (word l stored at l ^ ((l >> 5) & 15)) so every pass reads and
-// writes with at most the two-wavefront minimum of 64-bit accesses.
+// values live in [0, 8p), inverse in [0, 4p); outputs are reduced to [0, p).  Needs p < 2^61.  Shared memory is
+// XOR-swizzled (word l stored at l ^ ((l >> 5) & 15)) so every pass reads and writes with at most the
+// two-wavefront minimum of 64-bit accesses.
 #include <cooperative_groups.h>
 
 #include "ntt.cuh"
@@ -293,6 +296,143 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
   }
 }
 
+// ---- forward, N = 2^13 .. 2^16: radix-16 passes, 16 residues per thread ----
+//
+// Same cluster layout (C = N/8192 CTAs of 8192 residues, 64 KiB of shared memory each), but every pass works
+// on 16-residue groups, so a thread holds 16 residues (not 32) at a time: 256 threads per CTA each take two
+// groups per pass, and with 64 registers a thread three CTAs share an SM (24 warps; 8-CTA clusters then also
+// pack a 19-SM GPC almost fully).  Passes (forward; the inverse runs them in reverse order):
+//   X : bits [LOGN-1 .. 12] (LOGX = LOGN - 12 bits; the top LOGC of them cross CTAs via distributed shared
+//       memory, bit 12 is inside the CTA) on columns l' in [0, 4096) of CTA c's share;
+//   A : bits [11 .. 8]   (16 residues at stride 256),
+//   B : bits [7 .. 4]    (16 residues at stride 16),
+//   C : bits [3 .. 0]    (16 contiguous residues), then the store to HBM.
+// The profile of this kernel shows the ALU pipe (64-bit compares, selects and adds of the lazy reductions) as the
+// busiest unit; occupancy (16, 24 or 32 warps per SM) barely moves its time.
+constexpr int kThreads16 = 256;
+constexpr int kGroups16 = 512 / kThreads16;  // 16-residue groups per thread and pass
+
+template <int LOGN>
+struct Shape16 {
+  static constexpr int N = 1 << LOGN;
+  static constexpr int E = 8192;
+  static constexpr int LOGC = LOGN - 13;
+  static constexpr int C = 1 << LOGC;
+  static constexpr int LOGX = LOGN - 12;
+  static constexpr int GX = (16 >> LOGX) * kGroups16;  // phase-X groups per thread
+  static constexpr int COLS = 4096 / C;                // phase-X columns per CTA
+};
+
+template <int LOGN>
+__global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_constant__ NttBatch b,
+                                                                 const __grid_constant__ DeviceTables T) {
+  using S = Shape16<LOGN>;
+  extern __shared__ __align__(16) u64 sm[];
+  const int tid = threadIdx.x;
+  const LimbRef L = locate(b, S::N);
+  if (!L.valid) return;
+  const u64 p = T.pc[L.prime].p, p2 = 2 * p, p4 = 4 * p, negp = T.pc[L.prime].negp;
+  const ulonglong2* __restrict__ tw = T.tw_fwd + (size_t)L.prime * S::N;
+  int h = 0;
+  if constexpr (S::C > 1) {
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+    h = (int)cg::this_cluster().block_rank();
+  }
+  {  // phase X
+    constexpr int R = 1 << S::LOGX;
+#pragma unroll 1
+    for (int q = 0; q < S::GX; q++) {
+      const int col = h * S::COLS + q * kThreads16 + tid;
+      u64 x[R];
+#pragma unroll
+      for (int k = 0; k < R; k++) x[k] = __ldg(L.src + k * 4096 + col);
+      fwd_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4);
+      if constexpr (S::C > 1) {
+        if (q == 0) asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
+        cg::cluster_group cl = cg::this_cluster();
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+          u64* dst = cl.map_shared_rank(sm, k >> 1);
+          dst[swz((k & 1) * 4096 + col)] = x[k];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; k++) sm[swz(k * 4096 + col)] = x[k];
+      }
+    }
+    if constexpr (S::C > 1)
+      cg::this_cluster().sync();
+    else
+      __syncthreads();
+  }
+#pragma unroll 1
+  for (int g = tid; g < 512; g += kThreads16) {  // pass A
+    const int b12 = g >> 8, low = g & 255;
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(b12 * 4096 + k * 256 + low)];
+    fwd_radix<4, 8, LOGN>(x, h * 2 + b12, tw, negp, p4);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(b12 * 4096 + k * 256 + low)] = x[k];
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int g = tid; g < 512; g += kThreads16) {  // pass B
+    const int low = g & 15, high = g >> 4;
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
+    fwd_radix<4, 4, LOGN>(x, h * 32 + high, tw, negp, p4);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int g = tid; g < 512; g += kThreads16) {  // pass C
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
+    fwd_radix<4, 0, LOGN>(x, h * 512 + g, tw, negp, p4);
+    ulonglong2* out = reinterpret_cast<ulonglong2*>(L.dst + h * S::E + g * 16);
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+      ulonglong2 v;
+      v.x = csub(csub(csub(x[k], p4), p2), p);
+      v.y = csub(csub(csub(x[k + 1], p4), p2), p);
+      out[k / 2] = v;
+    }
+  }
+}
+
+template <int LOGN>
+cudaError_t launch16_fwd(const NttBatch& b, const DeviceTables& t, cudaStream_t s) {
+  using S = Shape16<LOGN>;
+  auto kern = ntt16_fwd_kernel<LOGN>;
+  static bool attr_done = false;
+  const size_t smem = sizeof(u64) * S::E;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(S::C, b.limb_begin[b.njobs], 1);
+  cfg.blockDim = dim3(kThreads16, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = S::C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, b, t);
+  if (e != cudaSuccess) return e;
+  count_launch();
+  return cudaSuccess;
+}
+
 template <int LOGN>
 cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape<LOGN>;
@@ -331,10 +471,12 @@ cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, c
     case 10: return launch_t<10>(b, t, inverse, s);
     case 11: return launch_t<11>(b, t, inverse, s);
     case 12: return launch_t<12>(b, t, inverse, s);
-    case 13: return launch_t<13>(b, t, inverse, s);
-    case 14: return launch_t<14>(b, t, inverse, s);
-    case 15: return launch_t<15>(b, t, inverse, s);
-    case 16: return launch_t<16>(b, t, inverse, s);
+    // measured on GB300 (640 limbs at N = 2^16): the radix-16 forward is 5% faster than the radix-32/16 one; a
+    // radix-16 inverse of the same shape (pull or push exchange) was 3% slower than the radix-32/16 inverse
+    case 13: return inverse ? launch_t<13>(b, t, true, s) : launch16_fwd<13>(b, t, s);
+    case 14: return inverse ? launch_t<14>(b, t, true, s) : launch16_fwd<14>(b, t, s);
+    case 15: return inverse ? launch_t<15>(b, t, true, s) : launch16_fwd<15>(b, t, s);
+    case 16: return inverse ? launch_t<16>(b, t, true, s) : launch16_fwd<16>(b, t, s);
     default: return cudaErrorInvalidValue;
   }
 }
