@@ -464,27 +464,31 @@ def served_bench(args, dev):
 
 def boot_bench(args, dev):
     """Config 5: CKKS bootstrapping at N = 2^16 with 32768 full slots, level budget {3, 3} (CoeffsToSlots and
-    SlotsToCoeffs each three factors of the special FFT, 63 diagonals per factor), sparse-secret encapsulation
-    (two switch keys), EvalMod = Chebyshev degree 47 on [-12.5K, 12.5K] + 3 double angles (K = q_0 / 2^55), on
-    the config-3 moduli (ModRaise to 30 towers, 12 left after).  Eight bootstraps in flight together
-    (fides_eval_bootstrap_batch: every step one batched launch for all eight) against the same eight one at a
-    time.  Keys and diagonals are seeded random residues of the real shapes (the op sequence and its cost do not
-    depend on their values)."""
+    SlotsToCoeffs each three factors of the special FFT, up to 63 diagonals per factor, encoded on the GPU),
+    sparse-secret encapsulation (two switch keys), EvalMod = Chebyshev degree 47 on [-12.5K, 12.5K] + 3 double
+    angles (K = q_0 / 2^55).  Moduli as in the N = 2^16 bootstrap precision test: q_0 of 60 bits, 24 towers of
+    55 bits (scale 2^55), 5 special primes of 60 bits, dnum 5.  Eight bootstraps in flight together
+    (fides_eval_bootstrap_batch: every step one batched launch for all eight), the same eight one at a time, and
+    the eight submitted as requests to the continuous-batching server.  Keys are seeded random residues of the
+    real shape (a key switch costs the same on any residues)."""
     import numpy as np
     import numpy.polynomial.chebyshev as Cheb
     import torch
 
     import fideslib_gb300 as F
     from fideslib_gb300 import bootplan as BP
-    mods = moduli_cfg3()
-    ctx = F.CryptoContext(LOGN, mods, NP, DNUM)
+    nq, npr, dnum = 25, 5, 5
+    mods = gen_primes_host(60, 1, 2 * N)
+    mods += gen_primes_host(55, nq - 1, 2 * N, exclude=mods)
+    mods += gen_primes_host(60, npr, 2 * N, exclude=mods)
+    ctx = F.CryptoContext(LOGN, mods, npr, dnum)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     gen = torch.Generator(device=dev)
     gen.manual_seed(0x5EED0005)
     modt = torch.tensor(mods, dtype=torch.int64, device=dev)
 
     def rand_key():
-        k = torch.randint(0, 1 << 62, (2, DNUM, NQ + NP, N), dtype=torch.int64, device=dev, generator=gen)
+        k = torch.randint(0, 1 << 62, (2, dnum, nq + npr, N), dtype=torch.int64, device=dev, generator=gen)
         return k % modt.view(1, 1, -1, 1)
 
     k = rand_key()
@@ -493,34 +497,30 @@ def boot_bench(args, dev):
     for kid in (1, 2):
         ctx.load_switch_key_device(kid, k.data_ptr())
     n = N // 2
+    delta = 2.0 ** 55
     lts = {True: [], False: []}
     need = set()
-    diag_towers = NQ
     for inverse in (True, False):
         for M, stride, r in BP.factors(n, 3, inverse, scale=n / N if inverse else 1.0):
             bs, gs, base, slots = BP.bsgs_layout(M, n, stride, r)
             need |= BP.rotation_indices(n, N, stride, bs, gs, base, slots)
-            d = torch.randint(0, 1 << 62, (bs * gs, diag_towers, N), dtype=torch.int64, device=dev, generator=gen)
-            d %= modt[:diag_towers].view(1, -1, 1)
             present = [s is not None for s in slots]
-            lts[inverse].append(ctx.lt_create_device(bs, gs, d.data_ptr(), diag_towers, present, 2.0 ** 50,
-                                                     stride=stride, base=base))
-            del d
+            diag = np.array([x if x is not None else np.zeros(n) for x in slots])
+            lts[inverse].append(ctx.lt_create_slots(bs, gs, diag, present, delta, nq, stride=stride, base=base))
     for idx in sorted(need):
         k = rand_key()
         ctx.load_rotation_key_device(ctx.galois(idx), k.data_ptr())
     del k
-    delta_m = 2.0 ** 55
-    K = mods[0] / delta_m
+    K = mods[0] / delta
     lo, hi = -12.5 * K, 12.5 * K
     f = lambda r: np.cos(2 * np.pi * (r / K - 0.25) / 8)  # noqa: E731
     coeffs = Cheb.chebinterpolate(lambda u: f(lo + (u + 1) * (hi - lo) / 2), 47)
-    plan = F.BootstrapPlan.make(n, NQ, lts[True], lts[False], coeffs, 3, lo, hi, 2.0 ** 50, sse_keys=(1, 2))
+    plan = F.BootstrapPlan.make(n, nq, lts[True], lts[False], coeffs, 3, lo, hi, delta, sse_keys=(1, 2))
     m = 8
     hs = []
     for _ in range(m):
         x = torch.randint(0, 1 << 62, (2, 1, N), dtype=torch.int64, device=dev, generator=gen) % modt[0]
-        hs.append(ctx.load_ciphertext_device(x.data_ptr(), 1, scale=delta_m))
+        hs.append(ctx.load_ciphertext_device(x.data_ptr(), 1, scale=delta))
     torch.cuda.synchronize()
 
     def timed(fn, reps):
@@ -550,16 +550,30 @@ def boot_bench(args, dev):
     batch_ms = timed(batched, 2)
     launches = (F.kernel_launches() - launches0) // 2
     single_ms = timed(one_at_a_time, 1)
+    # the same eight as requests to the continuous-batching server (admitted together, one bootstrap batch)
+    srv = F.Server(ctx, max_batch=m, max_inflight=1, mem_budget=200 << 30)
+    srv.set_bootstrap_plan(plan)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tickets = [srv.submit(F.OP_BOOTSTRAP, h) for h in hs]
+    lat = sorted(srv.wait(t)[1] for t in tickets)
+    served_ms = (time.perf_counter() - t0) * 1e3
+    for t in tickets:
+        srv.release(t)
+    srv.close()
     ctx.close()
     torch.cuda.synchronize()
     return {"workload": "cfg5: bootstrap N=2^16, 32768 full slots, level budget {3,3}, sparse-secret "
-                        "encapsulation, Chebyshev 47 + 3 double angles, 8 in flight",
+                        "encapsulation, Chebyshev 47 + 3 double angles, 8 in flight; q_0 60 bits + 24 x 55-bit "
+                        "towers, 5 x 60-bit special primes, dnum 5; diagonals encoded on the GPU",
             "rotation_keys": len(need) + 1, "towers_after": towers_left,
             "batched_8": {"ms": round(batch_ms, 2), "bootstraps_per_s": round(m / (batch_ms / 1e3), 2),
                           "gpu_launches": int(launches)},
             "one_at_a_time_8": {"ms": round(single_ms, 2), "bootstraps_per_s": round(m / (single_ms / 1e3), 2),
                                 "ms_per_bootstrap": round(single_ms / m, 2)},
-            "batched_over_one_at_a_time": round(single_ms / batch_ms, 3)}
+            "batched_over_one_at_a_time": round(single_ms / batch_ms, 3),
+            "served_8": {"ms": round(served_ms, 2), "bootstraps_per_s": round(m / (served_ms / 1e3), 2),
+                         "latency_ms_p50": round(lat[len(lat) // 2], 2), "latency_ms_max": round(lat[-1], 2)}}
 
 
 def ntt_bench(args, dev, stream):

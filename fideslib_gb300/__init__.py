@@ -90,6 +90,13 @@ _SIGS = {
     "fides_lt_create_strided": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
                                           u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fides_pt_encode": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32, C.c_double,
+                                  C.c_uint32, u32p]),
+    "fides_pt_decode": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "fides_pt_store": (C.c_int, [C.c_void_p, C.c_uint32, u64p]),
+    "fides_lt_create_slots": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_uint8),
+                                        C.c_uint32, C.c_double, u32p]),
     "fides_load_switch_key": (C.c_int, [C.c_void_p, C.c_uint32, u64p]),
     "fides_load_switch_key_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "fides_eval_key_switch": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
@@ -106,6 +113,7 @@ _SIGS = {
     "fides_eval_double_angle_batch": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.c_uint32, u32p]),
     "fides_server_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "fides_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "fides_server_set_bootstrap_plan": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fides_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, u32p, C.POINTER(C.c_double)]),
     "fides_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fides_server_stats_get": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -115,7 +123,7 @@ _SIGS = {
                                             C.c_void_p]),
 }
 
-OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM, OP_KEY_SWITCH = 1, 2, 3, 4, 5, 6, 7, 8
+OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM, OP_KEY_SWITCH, OP_BOOTSTRAP = range(1, 10)
 
 
 class Op(C.Structure):
@@ -368,6 +376,40 @@ class CryptoContext:
                                              pres.ctypes.data_as(C.POINTER(C.c_uint8)), scale, C.byref(h)))
         return h.value
 
+    def encode(self, z, scale: float, towers: int) -> int:
+        """Plaintext handle: the slot vector z (complex, length a power of two <= N/2) encoded on the GPU."""
+        z = np.asarray(z, dtype=np.complex128)
+        re, im = np.ascontiguousarray(z.real), np.ascontiguousarray(z.imag)
+        h = C.c_uint32()
+        dp = C.POINTER(C.c_double)
+        _check(lib().fides_pt_encode(self._h, re.ctypes.data_as(dp), im.ctypes.data_as(dp), len(z), scale, towers,
+                                     C.byref(h)))
+        return h.value
+
+    def decode(self, pt: int, slots: int) -> np.ndarray:
+        re, im = np.zeros(slots), np.zeros(slots)
+        dp = C.POINTER(C.c_double)
+        _check(lib().fides_pt_decode(self._h, pt, slots, re.ctypes.data_as(dp), im.ctypes.data_as(dp)))
+        return re + 1j * im
+
+    def store_plaintext(self, pt: int, towers: int) -> np.ndarray:
+        out = np.zeros((towers, self.N), dtype=np.uint64)
+        _check(lib().fides_pt_store(self._h, pt, _p(out)))
+        return out
+
+    def lt_create_slots(self, bs: int, gs: int, diags, present, scale: float, towers: int, stride: int = 1,
+                        base: int = 0) -> int:
+        """diags: complex [bs*gs][slots] (rows of absent diagonals ignored), encoded on the GPU."""
+        d = np.asarray(diags, dtype=np.complex128)
+        re, im = np.ascontiguousarray(d.real), np.ascontiguousarray(d.imag)
+        pres = np.ascontiguousarray(np.array(present, dtype=np.uint8))
+        h = C.c_uint32()
+        dp = C.POINTER(C.c_double)
+        _check(lib().fides_lt_create_slots(self._h, bs, gs, stride, base, towers, re.ctypes.data_as(dp),
+                                           im.ctypes.data_as(dp), pres.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                           d.shape[1], scale, C.byref(h)))
+        return h.value
+
     def eval_mult_monomial(self, a: int, k: int) -> int:
         return self._un(lib().fides_eval_mult_monomial, a, k)
 
@@ -474,6 +516,9 @@ class Server:
         h = C.c_void_p()
         _check(lib().fides_server_create(ctx._h, C.byref(cfg), C.byref(h)))
         self._h = h
+
+    def set_bootstrap_plan(self, plan: "BootstrapPlan"):
+        _check(lib().fides_server_set_bootstrap_plan(self._h, C.byref(plan)))
 
     def submit(self, code: int, a: int, b: int = 0, index: int = 0) -> int:
         op = Op(code, a, b, index, 0)

@@ -558,6 +558,17 @@ int fides_pt_load(fides_ctx* ctx, const uint64_t* data, uint32_t towers, double 
   return FIDES_OK;
 }
 
+int fides_pt_store(fides_ctx* ctx, uint32_t handle, uint64_t* data) {
+  if (!valid_ctx(ctx) || !data) return fail(FIDES_EINVAL, "null argument");
+  fgb::DevPt* P = find_pt(ctx, handle);
+  if (!P) return fail(FIDES_EINVAL, "unknown plaintext handle");
+  CK(cudaMemcpyAsync(data, P->data, (size_t)P->t * ctx->c->N * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                     ctx->c->stream),
+     "plaintext copy");
+  CK(cudaStreamSynchronize(ctx->c->stream), "plaintext copy");
+  return FIDES_OK;
+}
+
 int fides_pt_free(fides_ctx* ctx, uint32_t handle) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
   auto it = ctx->c->pts.find(handle);

@@ -6,8 +6,9 @@
 // fits the memory budget (output ciphertext + key-switch workspace, counted per request) up to max_batch, runs
 // them through fides_eval_batch (one launch per pipeline stage for all of them, at their own levels), and keeps
 // up to max_inflight batches queued on the stream, so requests that arrive while a batch runs are admitted into
-// the next one as soon as slots and memory free up.  Each request's latency is stamped on the host from submit
-// to the completion of its batch's CUDA event.
+// the next one as soon as slots and memory free up.  Bootstrap requests (FIDES_OP_BOOTSTRAP, with the plan set
+// by fides_server_set_bootstrap_plan) admitted together run as one fides_eval_bootstrap_batch.  Each request's
+// latency is stamped on the host from submit to the completion of its batch's CUDA event.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,6 +53,9 @@ struct InFlight {
 struct fides_server {
   fides_ctx* ctx = nullptr;
   fides_server_config cfg{};
+  bool has_plan = false;
+  fides_bootstrap_plan plan{};  // cheb_coeffs points into coeffs
+  std::vector<double> coeffs;
   uint32_t N = 0, np = 0, nq = 0, alpha = 1;
   std::thread worker;
   std::mutex mu;
@@ -75,6 +79,8 @@ struct fides_server {
       limbs += t + beta * (t + np) + 2 * (t + np) + 2 * t;
     if (op.op == FIDES_OP_MULT || op.op == FIDES_OP_SQUARE) limbs += 3 * t;
     if (op.op == FIDES_OP_RESCALE) limbs += 2 * t;
+    if (op.op == FIDES_OP_BOOTSTRAP)  // estimate: the largest stage holds about 64 ciphertexts at raise_towers
+      limbs = (size_t)64 * 2 * plan.raise_towers;
     return limbs * S;
   }
 
@@ -119,10 +125,36 @@ struct fides_server {
             bytes += reqs[take[i]].footprint;
           }
         }
-        int rc = fides_eval_batch(ctx, ops.data(), (uint32_t)ops.size());
-        std::vector<int> rcs(ops.size(), rc);
-        if (rc != FIDES_OK && ops.size() > 1)  // one bad request must not fail its batch-mates
-          for (size_t i = 0; i < ops.size(); i++) rcs[i] = fides_eval_batch(ctx, &ops[i], 1);
+        // bootstrap requests go through fides_eval_bootstrap_batch (all of them in flight together), the rest
+        // through fides_eval_batch
+        std::vector<size_t> bi, oi;
+        for (size_t i = 0; i < ops.size(); i++) (ops[i].op == FIDES_OP_BOOTSTRAP ? bi : oi).push_back(i);
+        std::vector<int> rcs(ops.size(), FIDES_OK);
+        if (!oi.empty()) {
+          std::vector<fides_op> sub(oi.size());
+          for (size_t k = 0; k < oi.size(); k++) sub[k] = ops[oi[k]];
+          const int rc = fides_eval_batch(ctx, sub.data(), (uint32_t)sub.size());
+          for (size_t k = 0; k < oi.size(); k++) {
+            if (rc != FIDES_OK && sub.size() > 1)  // one bad request must not fail its batch-mates
+              rcs[oi[k]] = fides_eval_batch(ctx, &sub[k], 1);
+            else
+              rcs[oi[k]] = rc;
+            ops[oi[k]].out = sub[k].out;
+          }
+        }
+        if (!bi.empty()) {
+          std::vector<uint32_t> in(bi.size()), outs(bi.size(), 0);
+          for (size_t k = 0; k < bi.size(); k++) in[k] = ops[bi[k]].a;
+          const int rc = has_plan ? fides_eval_bootstrap_batch(ctx, (uint32_t)in.size(), in.data(), &plan, outs.data())
+                                  : fgb::set_last_error(FIDES_EINVAL, "no bootstrap plan set on the server");
+          for (size_t k = 0; k < bi.size(); k++) {
+            if (rc != FIDES_OK && has_plan && bi.size() > 1)
+              rcs[bi[k]] = fides_eval_bootstrap(ctx, in[k], &plan, &outs[k]);
+            else
+              rcs[bi[k]] = rc;
+            ops[bi[k]].out = outs[k];
+          }
+        }
         InFlight f;
         cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming);
         cudaEventRecord(f.ev, stream);
@@ -190,6 +222,17 @@ int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_se
   s->alpha = shape.alpha ? shape.alpha : 1;
   s->worker = std::thread([s] { s->run(); });
   *out = s;
+  return FIDES_OK;
+}
+
+int fides_server_set_bootstrap_plan(fides_server* s, const fides_bootstrap_plan* plan) {
+  if (!s || !plan || !plan->cheb_coeffs || plan->cheb_n == 0) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (!s->pending.empty()) return fgb::set_last_error(FIDES_EINVAL, "set the plan before submitting requests");
+  s->coeffs.assign(plan->cheb_coeffs, plan->cheb_coeffs + plan->cheb_n);
+  s->plan = *plan;
+  s->plan.cheb_coeffs = s->coeffs.data();
+  s->has_plan = true;
   return FIDES_OK;
 }
 

@@ -180,6 +180,23 @@ int fides_eval_linear_transform_batch(fides_ctx* ctx, uint32_t n, const uint32_t
  * every slot by i (Ciphertext::multMonomial, used by the full-slot bootstrap, src/CKKS/Bootstrap.cu:262). */
 int fides_eval_mult_monomial(fides_ctx* ctx, uint32_t a, uint32_t k, uint32_t* out);
 
+/* CKKS encoding on the GPU (OpenFHE MakeCKKSPackedPlaintext, which the reference runs on the CPU before
+ * LoadPlaintext, api/CryptoContext.cpp:488-535): slots = n values re[k] + i im[k] (host; im may be null), n a power
+ * of two <= N/2, encoded at `scale` into `towers` towers (sparse packings replicate with period n).  FP64 special
+ * FFT on the device; every |round(scale * coefficient)| must be < 2^62 (FIDES_EINVAL otherwise). */
+int fides_pt_encode(fides_ctx* ctx, const double* re, const double* im, uint32_t slots, double scale, uint32_t towers,
+                    uint32_t* handle);
+/* Decoding of a plaintext's first n slots at its scale (CKKSPackedEncoding::Decode): coefficients are rebuilt from
+ * towers 0 and 1, so |round(scale * coefficient)| must stay below q_0 q_1 / 2 (q_0 / 2 with one tower). */
+int fides_pt_decode(fides_ctx* ctx, uint32_t pt, uint32_t slots, double* re, double* im);
+/* Copies a plaintext's residues (u64[towers][N], evaluation form) to host memory. */
+int fides_pt_store(fides_ctx* ctx, uint32_t pt, uint64_t* data);
+/* fides_lt_create_strided with the diagonals given as slot vectors (re/im [bs*gs][slots], host) and encoded on
+ * the GPU at `scale` into `towers` towers: the whole bootstrap precomputation stays on the device. */
+int fides_lt_create_slots(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
+                          const double* re, const double* im, const uint8_t* present, uint32_t slots, double scale,
+                          uint32_t* handle);
+
 /* EvalChebyshevSeries (api/CryptoContext.hpp:154-156, src/CKKS/ApproxModEval.cu:138-370):
  * p(x) = sum_k coeffs[k] T_k((2x - lo - hi)/(hi - lo)), k < n, constants encoded at const_scale.  The exact op
  * recipe (doubling identities for T_k, level alignment by dropping towers) is documented in
@@ -231,7 +248,8 @@ int fides_eval_bootstrap_batch(fides_ctx* ctx, uint32_t m, const uint32_t* cts, 
  * Generalises the reference's cross-ciphertext batching (src/CKKS/LimbPartitionBatch.cu:20-600,
  * RNSPolyBatch.cpp) to the whole key-switching pipeline. */
 enum { FIDES_OP_ADD = 1, FIDES_OP_SUB = 2, FIDES_OP_MULT = 3, FIDES_OP_SQUARE = 4, FIDES_OP_RESCALE = 5,
-       FIDES_OP_ROTATE = 6, FIDES_OP_AUTOMORPHISM = 7, FIDES_OP_KEY_SWITCH = 8 };
+       FIDES_OP_ROTATE = 6, FIDES_OP_AUTOMORPHISM = 7, FIDES_OP_KEY_SWITCH = 8,
+       FIDES_OP_BOOTSTRAP = 9 /* request server only (fides_server_set_bootstrap_plan) */ };
 typedef struct {
   int32_t op;      /* FIDES_OP_* */
   uint32_t a;      /* first operand handle */
@@ -272,6 +290,9 @@ typedef struct {
   double p50_ms, p99_ms, mean_ms, max_ms, ops_per_s, mean_batch;
 } fides_server_stats;
 int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_server** out);
+/* Bootstrap requests (FIDES_OP_BOOTSTRAP, operand a) use this plan (copied, with its coefficients); requests
+ * admitted together run as one fides_eval_bootstrap_batch.  Set it before submitting. */
+int fides_server_set_bootstrap_plan(fides_server* s, const fides_bootstrap_plan* plan);
 int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket);
 /* Blocks until the request finished; returns its status and result handle. */
 int fides_server_wait(fides_server* s, uint64_t ticket, uint32_t* out, double* latency_ms);

@@ -146,3 +146,23 @@ def test_bootstrap_full_slots_level_budget_sse_and_batch():
     for o, zz in zip(outs[1:], (z2, z3)):
         err, bits = st.precision(gpu.store_ciphertext(o), gpu.meta(o).scale, zz)
         assert err < 2e-5, err
+
+
+def test_bootstrap_requests_through_the_server():
+    """Bootstrap requests submitted to the continuous-batching server run in flight together and give exactly the
+    single-call results."""
+    st = Setup(slots=N // 2, budget=(3, 3), sse=True, seed=0x5EED0025)
+    gpu, F = st.gpu, st.F
+    msgs = [st.message(90 + i) for i in range(3)]
+    hs = [gpu.load_ciphertext(ct, DELTA_M) for _, ct in msgs]
+    singles = [gpu.store_ciphertext(gpu.eval_bootstrap(h, st.plan)) for h in hs]
+    srv = F.Server(gpu, max_batch=8, max_inflight=1, mem_budget=64 << 30)
+    srv.set_bootstrap_plan(st.plan)
+    tickets = [srv.submit(F.OP_BOOTSTRAP, h) for h in hs]
+    outs = [srv.wait(t)[0] for t in tickets]
+    stats = srv.stats()
+    srv.close()  # unreleased results stay in the context, owned by the caller
+    got = [gpu.store_ciphertext(o) for o in outs]
+    for g, ref in zip(got, singles):
+        assert np.array_equal(g, ref)
+    assert stats["completed"] == 3
