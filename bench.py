@@ -227,6 +227,15 @@ def run_ours(args, rank, world, dist):
             dist.barrier()
         return ms, launches
 
+    if args.profile_step:  # warm-up batched steps plus exactly one, for an ncu launch list of the headline step
+        for _ in range(args.warmup):
+            step_batched()
+        torch.cuda.synchronize()
+        l0 = F.kernel_launches()
+        step_batched()
+        torch.cuda.synchronize()
+        return {"profile_step": True, "warmup": args.warmup, "launches_per_step": F.kernel_launches() - l0}
+
     per_op_ms, _ = timed(step_per_op, args.steps)
     with Clocks(dev.index) as clk:
         ms, launches = timed(step_batched, args.steps)
@@ -328,6 +337,7 @@ def run_ours(args, rank, world, dist):
         "hoisted_cfg3a": {"ms_for_32_rotations": round(hoisted_ms, 4),
                           "ops_per_s": round(32 / (hoisted_ms / 1e3), 2)},
         "ntt_cfg2": ntt["summary"],
+        "ntt_autotune_n16": ctx.ntt_tuning(),
         "roofline": ntt["roofline"],
         "served_cfg4": served,
         "bootstrap_cfg5": boot,
@@ -679,6 +689,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-bootstrap", action="store_true")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="set up the headline workload, run --warmup batched steps and one more, print the launch "
+                         "count and exit (the command profiled for the per-kernel launch list)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -696,7 +709,7 @@ def main():
         dist = D
     res = run_ours(args, rank, world, dist)
     if rank == 0:
-        if world == 1 and not args.no_cpu_baseline:
+        if world == 1 and not args.no_cpu_baseline and not args.profile_step:
             threads = os.cpu_count() or 1
             v = cpu_rotations(4, threads, 42)
             res["cpu_baseline"] = {"value": round(v, 4), "unit": "HRotate ops/s", "cores": threads, "kind": "port",

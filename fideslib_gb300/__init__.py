@@ -90,6 +90,8 @@ _SIGS = {
     "fides_lt_create_strided": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
                                           u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fides_ctx_ntt_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32]),
     "fides_pt_encode": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                   C.c_uint32, u32p]),
     "fides_pt_decode": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -375,6 +377,16 @@ class CryptoContext:
         _check(lib().fides_lt_create_strided(self._h, bs, gs, stride, base, towers, C.cast(C.c_void_p(ptr), u64p),
                                              pres.ctypes.data_as(C.POINTER(C.c_uint8)), scale, C.byref(h)))
         return h.value
+
+    def ntt_tuning(self) -> dict:
+        """The forward-NTT variant the autotuner chose at creation and the two variants' times (ms / 64 limbs)."""
+        v = C.c_int32()
+        ms = (C.c_float * 2)()
+        _check(lib().fides_ctx_ntt_tuning(self._h, C.byref(v), ms))
+        return {"fwd_variant": v.value, "ms_per_64_limbs": [round(ms[0], 4), round(ms[1], 4)]}
+
+    def set_ntt_variant(self, fwd_variant: int):
+        _check(lib().fides_ctx_ntt_tuning_set(self._h, fwd_variant))
 
     def encode(self, z, scale: float, towers: int) -> int:
         """Plaintext handle: the slot vector z (complex, length a power of two <= N/2) encoded on the GPU."""

@@ -69,6 +69,25 @@ extern "C" {
 const char* fides_last_error(void) { return g_err.c_str(); }
 const char* fides_version(void) { return "fideslib_gb300 0.1 (sm_103a)"; }
 
+int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  if (fwd_variant) *fwd_variant = ctx->c->tabs.fwd_variant;
+  if (ms) {
+    ms[0] = ctx->c->ntt_tune_ms[0];
+    ms[1] = ctx->c->ntt_tune_ms[1];
+  }
+  return FIDES_OK;
+}
+
+int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  if (fwd_variant != 0 && fwd_variant != 1) return fail(FIDES_EINVAL, "forward variant must be 0 or 1");
+  if (ctx->c->logN < 13 && fwd_variant == 0) return fail(FIDES_EINVAL, "the radix-16 forward needs N >= 2^13");
+  cudaStreamSynchronize(ctx->c->stream);
+  ctx->c->tabs.fwd_variant = fwd_variant;
+  return FIDES_OK;
+}
+
 int fides_find_primes(uint32_t bits, uint32_t count, uint64_t two_n, const uint64_t* exclude, uint32_t nexclude,
                       uint64_t* out) {
   if (!out || bits < 2 || bits > 62 || two_n < 2) return 0;

@@ -328,6 +328,10 @@ bool Context::build(const u64* roots, std::string* err) {
     *err = std::string("device error during context set-up: ") + cudaGetErrorString(cudaGetLastError());
     return false;
   }
+  if (tune_ntt(tabs, own_stream, ntt_tune_ms) != cudaSuccess) {  // pick the forward NTT kernel for this ring
+    *err = std::string("NTT tuning failed: ") + cudaGetErrorString(cudaGetLastError());
+    return false;
+  }
   return true;
 }
 

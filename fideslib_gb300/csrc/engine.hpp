@@ -62,6 +62,7 @@ class Context {
   cudaStream_t own_stream = nullptr;  // the context's own stream
 
   DeviceTables tabs{};
+  float ntt_tune_ms[2] = {-1.f, -1.f};  // forward NTT variants timed by tune_ntt (ms per 64 limbs)
   CrtTables crt{};
   PrimeConst* d_pc = nullptr;
 

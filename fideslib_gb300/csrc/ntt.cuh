@@ -35,10 +35,16 @@ struct DeviceTables {
   const ulonglong2* tw_fwd;  // [ntowers][N] {psi^brev(i), shoup}
   const ulonglong2* tw_inv;  // [ntowers][N] {psi^-brev(i), shoup}
   int logN;
+  int fwd_variant = 0;  // forward kernel for N >= 2^13: 0 = radix-16 (three CTAs/SM), 1 = radix-32/16 (tune_ntt)
 };
 
 // Forward (inverse=false: coefficient -> evaluation, bit-reversed) or inverse transform of every job.
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s);
+
+// Autotuner: times the forward kernel variants on a 64-limb scratch batch of this ring (device memory from the
+// stream-ordered pool, synchronising `s`) and stores the faster one in t.fwd_variant.  The per-variant times
+// (ms per 64 limbs) are written to ms[0..1] when ms is non-null (a variant that does not apply gets -1).
+cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms);
 
 // Job owning flattened row `row` of a prefix-sum table begin[0..njobs] (uniform per block / cluster).
 __device__ __forceinline__ int find_job(const int* begin, int njobs, int row) {

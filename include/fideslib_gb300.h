@@ -64,6 +64,13 @@ typedef struct {
 const char* fides_last_error(void);
 const char* fides_version(void);
 
+/* The NTT autotuner's choice for this ring (no counterpart in the reference, whose NTT kernel is fixed at build
+ * time): at context creation both forward kernels are timed on 64 scratch limbs and the faster one is used.
+ * fwd_variant 0 = radix-16 passes (three CTAs per SM), 1 = radix-32/16 passes; ms[0..1] = their times in ms
+ * (-1 where a single kernel applies, N < 2^13). */
+int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms);
+/* Overrides the autotuner's choice (both variants give identical residues). */
+int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant);
 /* Parameter helper (the role of OpenFHE's FirstPrime/PreviousPrime in GenCryptoContext): the `count` largest
  * primes below 2^bits that are == 1 mod two_n, skipping `exclude`.  Returns the number found. */
 int fides_find_primes(uint32_t bits, uint32_t count, uint64_t two_n, const uint64_t* exclude, uint32_t nexclude,

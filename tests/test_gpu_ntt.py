@@ -76,3 +76,22 @@ def test_batched_ntt_full_size_config(engine_lib):
     assert np.array_equal(fwd.reshape(640, N), ref)
     back = ctx.ntt_host(fwd, 0, inverse=True)
     assert np.array_equal(back, data)
+
+
+@pytest.mark.parametrize("logN", [13, 14, 15, 16])
+def test_both_forward_variants_and_autotuner(engine_lib, logN):
+    """The autotuner picked one of the two forward kernels with both timed; each variant, forced, gives the
+    oracle's residues (edge values included)."""
+    N = 1 << logN
+    ctx, mods = make_ctx(logN, 2, bits=60)
+    tune = ctx.ntt_tuning()
+    assert tune["fwd_variant"] in (0, 1) and min(tune["ms_per_64_limbs"]) > 0
+    rng = np.random.default_rng(logN + 100)
+    data = np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(2)])[None]
+    data[0, 0, :7] = mods[0] - 1
+    for v in (0, 1):
+        ctx.set_ntt_variant(v)
+        fwd = ctx.ntt_host(data.copy(), 0, inverse=False)
+        for j in range(2):
+            tab, _ = O.ntt_tables(N, mods[j], ctx.roots[j])
+            assert np.array_equal(fwd[0, j], O.ntt_fwd(data[0, j], mods[j], tab)), (logN, v, j)
