@@ -73,6 +73,7 @@ _SIGS = {
     "fides_eval_rotate": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int32, u32p]),
     "fides_eval_automorphism": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_fast_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, i32p, u32p]),
+    "fides_eval_batch_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]),
     "fides_eval_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "fides_ctx_get_shape": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fides_pt_load": (C.c_int, [C.c_void_p, u64p, C.c_uint32, C.c_double, u32p]),
@@ -90,7 +91,7 @@ _SIGS = {
     "fides_lt_create_strided": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
                                           u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
-    "fides_ctx_ntt_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "fides_ctx_ntt_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32]),
     "fides_pt_encode": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                   C.c_uint32, u32p]),
@@ -126,6 +127,11 @@ _SIGS = {
 }
 
 OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM, OP_KEY_SWITCH, OP_BOOTSTRAP = range(1, 10)
+
+
+class HostOp(C.Structure):
+    _fields_ = [("op", C.c_int32), ("a", C.c_void_p), ("b", C.c_void_p), ("meta", CtMeta), ("index", C.c_int32),
+                ("out", C.c_void_p), ("out_meta", CtMeta)]
 
 
 class Op(C.Structure):
@@ -379,11 +385,13 @@ class CryptoContext:
         return h.value
 
     def ntt_tuning(self) -> dict:
-        """The forward-NTT variant the autotuner chose at creation and the two variants' times (ms / 64 limbs)."""
-        v = C.c_int32()
-        ms = (C.c_float * 2)()
-        _check(lib().fides_ctx_ntt_tuning(self._h, C.byref(v), ms))
-        return {"fwd_variant": v.value, "ms_per_64_limbs": [round(ms[0], 4), round(ms[1], 4)]}
+        """The forward-NTT variants the autotuner chose at creation (small / large launches) and the timings."""
+        v = (C.c_int32 * 2)()
+        ms = (C.c_float * 4)()
+        _check(lib().fides_ctx_ntt_tuning(self._h, v, ms))
+        return {"fwd_variant_small": v[0], "fwd_variant_large": v[1],
+                "ms_small_v0_v1": [round(ms[0], 4), round(ms[1], 4)],
+                "ms_large_v0_v1": [round(ms[2], 4), round(ms[3], 4)]}
 
     def set_ntt_variant(self, fwd_variant: int):
         _check(lib().fides_ctx_ntt_tuning_set(self._h, fwd_variant))
@@ -467,6 +475,22 @@ class CryptoContext:
             arr[i] = Op(code, a, b, index, 0)
         _check(lib().fides_eval_batch(self._h, arr, len(ops)))
         return [arr[i].out for i in range(len(ops))]
+
+    def eval_batch_host(self, ops, chunk: int = 0) -> list[CtMeta]:
+        """ops: iterable of (op_code, a, b, index, out, scale) with a / b / out host u64[2][t][N] arrays (b None
+        for unary ops; out sized for the result).  Results are written into `out`; returns their metadata."""
+        ops = list(ops)
+        arr = (HostOp * max(1, len(ops)))()
+        keep = []
+        for i, (code, a, b, index, out, scale) in enumerate(ops):
+            for x in (a, b, out):
+                if x is not None:
+                    assert x.dtype == np.uint64 and x.flags["C_CONTIGUOUS"] and x.shape[-1] == self.N
+                    keep.append(x)
+            arr[i] = HostOp(code, a.ctypes.data, b.ctypes.data if b is not None else None,
+                            CtMeta(a.shape[1], 1, 0, 0, scale), index, out.ctypes.data, CtMeta())
+        _check(lib().fides_eval_batch_host(self._h, arr, len(ops), chunk))
+        return [arr[i].out_meta for i in range(len(ops))]
 
     def eval_fast_rotation(self, a: int, indices) -> list[int]:
         idx = np.ascontiguousarray(np.array(indices, dtype=np.int32))

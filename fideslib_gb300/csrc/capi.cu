@@ -71,11 +71,12 @@ const char* fides_version(void) { return "fideslib_gb300 0.1 (sm_103a)"; }
 
 int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
-  if (fwd_variant) *fwd_variant = ctx->c->tabs.fwd_variant;
-  if (ms) {
-    ms[0] = ctx->c->ntt_tune_ms[0];
-    ms[1] = ctx->c->ntt_tune_ms[1];
+  if (fwd_variant) {
+    fwd_variant[0] = ctx->c->tabs.fwd_variant_small;
+    fwd_variant[1] = ctx->c->tabs.fwd_variant;
   }
+  if (ms)
+    for (int i = 0; i < 4; i++) ms[i] = ctx->c->ntt_tune_ms[i];
   return FIDES_OK;
 }
 
@@ -84,7 +85,7 @@ int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant) {
   if (fwd_variant != 0 && fwd_variant != 1) return fail(FIDES_EINVAL, "forward variant must be 0 or 1");
   if (ctx->c->logN < 13 && fwd_variant == 0) return fail(FIDES_EINVAL, "the radix-16 forward needs N >= 2^13");
   cudaStreamSynchronize(ctx->c->stream);
-  ctx->c->tabs.fwd_variant = fwd_variant;
+  ctx->c->tabs.fwd_variant = ctx->c->tabs.fwd_variant_small = fwd_variant;
   return FIDES_OK;
 }
 
@@ -199,6 +200,7 @@ int fides_ntt_batch_device(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint
   fgb::Context* c = ctx->c;
   if (limbs == 0 || npolys == 0) return FIDES_OK;
   if (limbs > 64 || first_prime + limbs > (uint32_t)c->ntow) return fail(FIDES_EINVAL, "tower range out of bounds");
+  if ((uintptr_t)data % 16) return fail(FIDES_EINVAL, "device data must be 16-byte aligned");
   cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
   CK(c->ntt((const fgb::u64*)data, (fgb::u64*)data, (int)npolys, (int)limbs, (int)first_prime, (long long)limbs * c->N, inverse != 0, s),
      "ntt launch");
@@ -456,6 +458,87 @@ static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
   }
   for (uint32_t i = 0; i < n; i++) ops[i].out = register_ct(ctx, pd[i].out);
   return FIDES_OK;
+}
+
+// Pipelined batch from and to host memory: chunk k's inputs are copied in on one stream while chunk k-1 computes
+// on the context stream and chunk k-2's results are copied out on a third, so the copy engines run beside the
+// kernels.  Inputs and outputs must be pinned host memory for the copies to be asynchronous.  Device memory comes
+// from the stream-ordered pool, whose reuse across the three streams follows their event dependencies.
+int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32_t chunk) {
+  if (!valid_ctx(ctx) || (!ops && n)) return fail(FIDES_EINVAL, "null argument");
+  if (n == 0) return FIDES_OK;
+  fgb::Context* c = ctx->c;
+  if (chunk == 0) chunk = n;
+  for (uint32_t i = 0; i < n; i++) {
+    const fides_host_op& o = ops[i];
+    const bool binary = o.op == FIDES_OP_ADD || o.op == FIDES_OP_SUB || o.op == FIDES_OP_MULT;
+    if (!o.a || !o.out || (binary && !o.b)) return fail(FIDES_EINVAL, "null host buffer in request " + std::to_string(i));
+    if (o.op == FIDES_OP_BOOTSTRAP) return fail(FIDES_EINVAL, "bootstrap requests go through the server");
+    if (o.meta.towers < 1 || o.meta.towers > (uint32_t)c->nq) return fail(FIDES_EINVAL, "towers out of range");
+  }
+  if (!c->copy_in) CK(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking), "copy stream");
+  if (!c->copy_out) CK(cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking), "copy stream");
+  const size_t limb = (size_t)c->N * sizeof(uint64_t);
+  std::vector<cudaEvent_t> events;
+  auto event = [&]() {
+    cudaEvent_t e;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    events.push_back(e);
+    return e;
+  };
+  int rc = FIDES_OK;
+  std::vector<fides_op> fo(n);
+  for (uint32_t k0 = 0; k0 < n && rc == FIDES_OK; k0 += chunk) {
+    const uint32_t k1 = std::min(n, k0 + chunk);
+    // copy in (input handles are registered now; their memory is ready once ev_in has passed)
+    std::vector<uint32_t> inputs;
+    for (uint32_t i = k0; i < k1 && rc == FIDES_OK; i++) {
+      const fides_host_op& o = ops[i];
+      const bool binary = o.op == FIDES_OP_ADD || o.op == FIDES_OP_SUB || o.op == FIDES_OP_MULT;
+      uint32_t hab[2] = {0, 0};
+      for (int w = 0; w < (binary ? 2 : 1) && rc == FIDES_OK; w++) {
+        fgb::DevCt ct;
+        ct.t = (int)o.meta.towers;
+        ct.scale = o.meta.scale;
+        ct.noise_deg = (int)o.meta.noise_deg;
+        ct.slots = (int)o.meta.slots;
+        ct.data = c->alloc_limbs((size_t)2 * ct.t, c->copy_in);
+        if (!ct.data) {
+          rc = fail(FIDES_ENOMEM, "input allocation failed");
+          break;
+        }
+        const cudaError_t e = cudaMemcpyAsync(ct.data, w ? o.b : o.a, 2 * ct.t * limb, cudaMemcpyHostToDevice,
+                                              c->copy_in);
+        hab[w] = register_ct(ctx, ct);
+        inputs.push_back(hab[w]);
+        if (e != cudaSuccess) rc = cuda_fail(e, "input copy");
+      }
+      fo[i] = fides_op{o.op, hab[0], hab[1], o.index, 0};
+    }
+    cudaEvent_t ev_in = event();
+    cudaEventRecord(ev_in, c->copy_in);
+    cudaStreamWaitEvent(c->stream, ev_in, 0);
+    if (rc == FIDES_OK) rc = run_batch(ctx, fo.data() + k0, k1 - k0);
+    for (uint32_t h : inputs) fides_ct_free(ctx, h);  // stream-ordered after the batch
+    if (rc != FIDES_OK) break;
+    // copy out after the batch, results freed on the copy stream once copied
+    cudaEvent_t ev_done = event();
+    cudaEventRecord(ev_done, c->stream);
+    cudaStreamWaitEvent(c->copy_out, ev_done, 0);
+    for (uint32_t i = k0; i < k1; i++) {
+      auto it = c->cts.find(fo[i].out);
+      fgb::DevCt& r = it->second;
+      ops[i].out_meta = fides_ct_meta{(uint32_t)r.t, (uint32_t)r.noise_deg, (uint32_t)r.slots, 0, r.scale};
+      const cudaError_t e = cudaMemcpyAsync(ops[i].out, r.data, 2 * r.t * limb, cudaMemcpyDeviceToHost, c->copy_out);
+      if (e != cudaSuccess && rc == FIDES_OK) rc = cuda_fail(e, "result copy");
+      c->free_limbs(r.data, c->copy_out);
+      c->cts.erase(it);
+    }
+  }
+  const cudaError_t e1 = cudaStreamSynchronize(c->copy_out), e2 = cudaStreamSynchronize(c->stream);
+  for (cudaEvent_t e : events) cudaEventDestroy(e);
+  if (rc == FIDES_OK && (e1 != cudaSuccess || e2 != cudaSuccess)) rc = cuda_fail(e1 ? e1 : e2, "host batch");
+  return rc;
 }
 
 static int one(fides_ctx* ctx, int32_t code, uint32_t a, uint32_t b, int32_t index, uint32_t* out) {

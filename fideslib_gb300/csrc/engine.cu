@@ -121,6 +121,8 @@ Context::~Context() {
   for (auto& kv : rot_keys) cudaFree(kv.second);
   if (relin_key) cudaFree(relin_key);
   for (void* p : owned_) cudaFree(p);
+  if (copy_in) cudaStreamDestroy(copy_in);
+  if (copy_out) cudaStreamDestroy(copy_out);
   if (stream) cudaStreamDestroy(stream);
 }
 

@@ -60,9 +60,10 @@ class Context {
   std::vector<u64> mod, psi;
   cudaStream_t stream = nullptr;      // stream all work is ordered on
   cudaStream_t own_stream = nullptr;  // the context's own stream
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;  // copy streams of the pipelined host batch (lazily made)
 
   DeviceTables tabs{};
-  float ntt_tune_ms[2] = {-1.f, -1.f};  // forward NTT variants timed by tune_ntt (ms per 64 limbs)
+  float ntt_tune_ms[4] = {-1.f, -1.f, -1.f, -1.f};  // forward NTT variants timed by tune_ntt (small, large)
   CrtTables crt{};
   PrimeConst* d_pc = nullptr;
 

@@ -149,8 +149,11 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
 #undef FGB_MODUP_CASE
 }
 
-// Key inner product: grid (N/256, nq+np, njobs), row j of the extended basis Q_t ∪ P.  Digits and key values
-// are split into 30-bit halves and accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max).
+// Key inner product: grid (N/512, nq+np, njobs), row j of the extended basis Q_t ∪ P, two coefficients per
+// thread (16-byte loads).  Every digit's value and both key halves are loaded before any arithmetic, so a thread
+// has 3 beta loads in flight; MAXB bounds beta at compile time.  Digits and key values are split into 30-bit
+// halves and accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max).
+template <int MAXB>
 __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                       const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
@@ -159,33 +162,44 @@ __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ Ks
   const int ext = t + c.np;
   if (j >= ext) return;
   const int tower = j < t ? j : c.nq + (j - t);
-  const int n = blockIdx.x * kT + threadIdx.x;
+  const int n = (blockIdx.x * kT + threadIdx.x) * 2;
   const size_t N = r.N;
   const int beta = (t + c.alpha - 1) / c.alpha;
-  Acc4 A0{0, 0, 0, 0}, A1{0, 0, 0, 0};
-#pragma unroll 1
-  for (int d = 0; d < beta; d++) {
+  ulonglong2 D[MAXB], KA[MAXB], KB[MAXB];
+#pragma unroll
+  for (int d = 0; d < MAXB; d++) {
+    if (d >= beta) break;
     const int start = d * c.alpha;
     const int s = min(c.alpha, t - start);
-    u64 D;
+    const u64* src;
     if (j >= start && j < start + s) {
-      D = J.a[(size_t)j * N + n];
+      src = J.a + (size_t)j * N;
     } else {
       const int jj = j < start ? j : j - s;
-      D = J.conv[((size_t)d * ext + jj) * N + n];
+      src = J.conv + ((size_t)d * ext + jj) * N;
     }
-    const u64 ka = J.key[((size_t)(0 * c.dnum + d) * c.ntow + tower) * N + n];
-    const u64 kb = J.key[((size_t)(1 * c.dnum + d) * c.ntow + tower) * N + n];
-    const uint32_t dl = (uint32_t)(D & kMask30), dh = (uint32_t)(D >> 30);
-    acc4_mac(A0, dl, dh, (uint32_t)(kb & kMask30), (uint32_t)(kb >> 30));
-    acc4_mac(A1, dl, dh, (uint32_t)(ka & kMask30), (uint32_t)(ka >> 30));
+    D[d] = *reinterpret_cast<const ulonglong2*>(src + n);
+    KA[d] = *reinterpret_cast<const ulonglong2*>(J.key + ((size_t)(0 * c.dnum + d) * c.ntow + tower) * N + n);
+    KB[d] = *reinterpret_cast<const ulonglong2*>(J.key + ((size_t)(1 * c.dnum + d) * c.ntow + tower) * N + n);
   }
-  u64 h0 = 0, l0 = 0, h1 = 0, l1 = 0;
-  acc4_fold(A0, h0, l0);
-  acc4_fold(A1, h1, l1);
   const PrimeConst& P = pc[tower];
-  J.inner[(size_t)j * N + n] = reduce128_fast(h0, l0, P);
-  J.inner[((size_t)ext + j) * N + n] = reduce128_fast(h1, l1, P);
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    Acc4 A0{0, 0, 0, 0}, A1{0, 0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < MAXB; d++) {
+      if (d >= beta) break;
+      const u64 Dv = e ? D[d].y : D[d].x, ka = e ? KA[d].y : KA[d].x, kb = e ? KB[d].y : KB[d].x;
+      const uint32_t dl = (uint32_t)(Dv & kMask30), dh = (uint32_t)(Dv >> 30);
+      acc4_mac(A0, dl, dh, (uint32_t)(kb & kMask30), (uint32_t)(kb >> 30));
+      acc4_mac(A1, dl, dh, (uint32_t)(ka & kMask30), (uint32_t)(ka >> 30));
+    }
+    u64 h0 = 0, l0 = 0, h1 = 0, l1 = 0;
+    acc4_fold(A0, h0, l0);
+    acc4_fold(A1, h1, l1);
+    J.inner[(size_t)j * N + n + e] = reduce128_fast(h0, l0, P);
+    J.inner[((size_t)ext + j) * N + n + e] = reduce128_fast(h1, l1, P);
+  }
 }
 
 // ModDown basis conversion P -> Q_t: grid (N/256, 2, njobs); reads the (coefficient-form) P rows of inner.
@@ -223,22 +237,27 @@ __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_const
   const KsJob& J = b.jobs[z];
   const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
   const int poly = row >= t ? 1 : 0, j = row - poly * t;
-  const int n = blockIdx.x * kT + threadIdx.x;
+  const int n = (blockIdx.x * kT + threadIdx.x) * 2;  // two coefficients per thread, 16-byte loads
   const size_t N = r.N;
   const u64 q = pc[j].p;
   const ulonglong2 w = c.md_pinv[j];
-  const u64 x = J.inner[((size_t)poly * (t + c.np) + j) * N + n];
-  const u64 y = J.md[((size_t)poly * t + j) * N + n];
-  u64 v = shoup(sub_mod(x, y, q), w.x, w.y, q);
+  const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(J.inner + ((size_t)poly * (t + c.np) + j) * N + n);
+  const ulonglong2 y = *reinterpret_cast<const ulonglong2*>(J.md + ((size_t)poly * t + j) * N + n);
   const u64* add = poly == 0 ? J.add0 : J.add1;
-  if (add) v = add_mod(v, add[(size_t)j * N + n], q);
-  uint32_t pos = n;
-  if (J.galois_inv != 1) {
-    const uint32_t idx = brev_n(n, r.logN);
-    const uint32_t jj = (uint32_t)((((2ull * idx + 1) * J.galois_inv) & (2ull * N - 1)) >> 1);
-    pos = brev_n(jj, r.logN);
+  const ulonglong2 a = add ? *reinterpret_cast<const ulonglong2*>(add + (size_t)j * N + n) : make_ulonglong2(0, 0);
+  u64* out = J.out + ((size_t)poly * t + j) * N;
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    u64 v = shoup(sub_mod(e ? x.y : x.x, e ? y.y : y.x, q), w.x, w.y, q);
+    if (add) v = add_mod(v, e ? a.y : a.x, q);
+    uint32_t pos = n + e;
+    if (J.galois_inv != 1) {
+      const uint32_t idx = brev_n(n + e, r.logN);
+      const uint32_t jj = (uint32_t)((((2ull * idx + 1) * J.galois_inv) & (2ull * N - 1)) >> 1);
+      pos = brev_n(jj, r.logN);
+    }
+    out[pos] = v;
   }
-  J.out[((size_t)poly * t + j) * N + pos] = v;
 }
 
 __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ TensorBatch b, Ring r,
@@ -458,8 +477,13 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
   KsBatch bb;
   const int np = c.np;
   const int rows = with_rows(b, bb, [np](const KsJob& j) { return j.t + np; });
-  dim3 grid(r.N / kT, rows, 1);
-  ks_inner_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
+  dim3 grid(r.N / (2 * kT), rows, 1);
+  if (c.dnum <= 2)
+    ks_inner_kernel<2><<<grid, kT, 0, s>>>(bb, r, c, pc);
+  else if (c.dnum <= 4)
+    ks_inner_kernel<4><<<grid, kT, 0, s>>>(bb, r, c, pc);
+  else
+    ks_inner_kernel<8><<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -492,7 +516,7 @@ cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTa
   if (b.njobs <= 0) return cudaSuccess;
   KsBatch bb;
   const int rows = with_rows(b, bb, [](const KsJob& j) { return 2 * j.t; });
-  dim3 grid(r.N / kT, rows, 1);
+  dim3 grid(r.N / (2 * kT), rows, 1);
   moddown_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();

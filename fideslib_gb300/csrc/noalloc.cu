@@ -69,6 +69,8 @@ extern "C" int fides_eval_rotate_noalloc(fides_ctx* ctx, const uint64_t* dev_in,
                                          uint64_t* dev_out, void* stream) {
   using fgb::u64;
   if (!ctx || !ctx->c || !dev_in || !dev_out) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+  if ((uintptr_t)dev_in % 16 || (uintptr_t)dev_out % 16)  // the kernels read and write 16-byte vectors
+    return fgb::set_last_error(FIDES_EINVAL, "device buffers must be 16-byte aligned");
   fgb::Context* c = ctx->c;
   const int t = (int)towers;
   if (t < 1 || t > c->nq) return fgb::set_last_error(FIDES_EINVAL, "towers out of range");

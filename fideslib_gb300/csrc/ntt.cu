@@ -467,61 +467,64 @@ cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cud
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   if (b.njobs <= 0 || b.limb_begin[b.njobs] <= 0) return cudaSuccess;
   if (b.njobs > kMaxNttJobs || b.limb_begin[b.njobs] > 65535) return cudaErrorInvalidValue;
+  const bool small = ((long long)b.limb_begin[b.njobs] << t.logN) <= kSmallNttWork;
+  const int v = small ? t.fwd_variant_small : t.fwd_variant;
   switch (t.logN) {
     case 10: return launch_t<10>(b, t, inverse, s);
     case 11: return launch_t<11>(b, t, inverse, s);
     case 12: return launch_t<12>(b, t, inverse, s);
     // forward: the variant tune_ntt picked (on GB300 the radix-16 one, 5% faster at N = 2^16); inverse: the
     // radix-32/16 kernel (a radix-16 inverse of the same shape, pull or push exchange, was 3% slower)
-    case 13: return inverse || t.fwd_variant ? launch_t<13>(b, t, inverse, s) : launch16_fwd<13>(b, t, s);
-    case 14: return inverse || t.fwd_variant ? launch_t<14>(b, t, inverse, s) : launch16_fwd<14>(b, t, s);
-    case 15: return inverse || t.fwd_variant ? launch_t<15>(b, t, inverse, s) : launch16_fwd<15>(b, t, s);
-    case 16: return inverse || t.fwd_variant ? launch_t<16>(b, t, inverse, s) : launch16_fwd<16>(b, t, s);
+    case 13: return inverse || v ? launch_t<13>(b, t, inverse, s) : launch16_fwd<13>(b, t, s);
+    case 14: return inverse || v ? launch_t<14>(b, t, inverse, s) : launch16_fwd<14>(b, t, s);
+    case 15: return inverse || v ? launch_t<15>(b, t, inverse, s) : launch16_fwd<15>(b, t, s);
+    case 16: return inverse || v ? launch_t<16>(b, t, inverse, s) : launch16_fwd<16>(b, t, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
 cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
-  if (ms) ms[0] = ms[1] = -1.f;
+  if (ms)
+    for (int i = 0; i < 4; i++) ms[i] = -1.f;
   if (t.logN < 13) return cudaSuccess;  // one forward kernel below 2^13
-  constexpr int kLimbs = 64;
   const size_t n = (size_t)1 << t.logN;
+  const int small = (int)((64ll << 16) >> t.logN), large = (int)((640ll << 16) >> t.logN);
   u64* buf = nullptr;
-  cudaError_t e = cudaMallocAsync(&buf, kLimbs * n * sizeof(u64), s);
+  cudaError_t e = cudaMallocAsync(&buf, (size_t)large * n * sizeof(u64), s);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(buf, 0, kLimbs * n * sizeof(u64), s);  // zeros are valid residues of every prime
-  NttBatch b{};
-  uint8_t pm[1] = {0};
-  ntt_add_job(b, buf, buf, (long long)n, (long long)n, 1, kLimbs, pm);
+  e = cudaMemsetAsync(buf, 0, (size_t)large * n * sizeof(u64), s);  // zeros are valid residues of every prime
   cudaEvent_t ev[2];
   cudaEventCreate(&ev[0]);
   cudaEventCreate(&ev[1]);
-  float best = 0;
-  int pick = 0;
-  for (int v = 0; v < 2 && e == cudaSuccess; v++) {
-    DeviceTables tv = t;
-    tv.fwd_variant = v;
-    e = launch_ntt(b, tv, false, s);  // warm-up
-    if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
-    for (int r = 0; r < 3 && e == cudaSuccess; r++) e = launch_ntt(b, tv, false, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-    float el = 0;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&el, ev[0], ev[1]);
-    el /= 3;
-    if (ms) ms[v] = el;
-    if (e == cudaSuccess && (v == 0 || el < best)) {
-      best = el;
-      pick = v;
+  for (int size = 0; size < 2 && e == cudaSuccess; size++) {
+    NttBatch b{};
+    uint8_t pm[1] = {0};
+    ntt_add_job(b, buf, buf, (long long)n, (long long)n, 1, size ? large : small, pm);
+    float best = 0;
+    int pick = 0;
+    for (int v = 0; v < 2 && e == cudaSuccess; v++) {
+      DeviceTables tv = t;
+      tv.fwd_variant = tv.fwd_variant_small = v;
+      e = launch_ntt(b, tv, false, s);  // warm-up
+      if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+      for (int r = 0; r < 3 && e == cudaSuccess; r++) e = launch_ntt(b, tv, false, s);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+      float el = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&el, ev[0], ev[1]);
+      el /= 3;
+      if (ms) ms[2 * size + v] = el;
+      if (v == 0 || el < best) {
+        best = el;
+        pick = v;
+      }
     }
+    if (e == cudaSuccess) (size ? t.fwd_variant : t.fwd_variant_small) = pick;
   }
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
   cudaFreeAsync(buf, s);
-  if (e == cudaSuccess) {
-    t.fwd_variant = pick;
-    e = cudaStreamSynchronize(s);
-  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e;
 }
 

@@ -64,12 +64,14 @@ typedef struct {
 const char* fides_last_error(void);
 const char* fides_version(void);
 
-/* The NTT autotuner's choice for this ring (no counterpart in the reference, whose NTT kernel is fixed at build
- * time): at context creation both forward kernels are timed on 64 scratch limbs and the faster one is used.
- * fwd_variant 0 = radix-16 passes (three CTAs per SM), 1 = radix-32/16 passes; ms[0..1] = their times in ms
- * (-1 where a single kernel applies, N < 2^13). */
+/* The NTT autotuner's choices for this ring (no counterpart in the reference, whose NTT kernel is fixed at build
+ * time): at context creation both forward kernels are timed on a small and a large scratch batch (64 and 640
+ * limbs' worth of residues at N = 2^16) and the faster one of each size is used for launches of at most / more
+ * than 256 limbs' worth.  fwd_variant[0] (small), [1] (large): 0 = radix-16 passes (three CTAs per SM),
+ * 1 = radix-32/16 passes; ms[0..3] = small v0, small v1, large v0, large v1 in ms (-1 where a single kernel
+ * applies, N < 2^13). */
 int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms);
-/* Overrides the autotuner's choice (both variants give identical residues). */
+/* Overrides the autotuner's choices (both variants give identical residues). */
 int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant);
 /* Parameter helper (the role of OpenFHE's FirstPrime/PreviousPrime in GenCryptoContext): the `count` largest
  * primes below 2^bits that are == 1 mod two_n, skipping `exclude`.  Returns the number found. */
@@ -102,7 +104,7 @@ uint64_t fides_kernel_launches(void);
 /* Batched negacyclic NTT (inverse = 0: coefficient -> evaluation, bit-reversed) or INTT on `npolys`
  * polynomials of `limbs` towers each, tower j using prime first_prime + j.  Device memory, in place,
  * ordered on `stream` (a cudaStream_t; NULL = the context stream).  Replaces the batched NTT_/INTT_
- * launches of LimbPartition::NTT / INTT (src/CKKS/LimbPartition.cu:332-421). */
+ * launches of LimbPartition::NTT / INTT (src/CKKS/LimbPartition.cu:332-421).  `data` must be 16-byte aligned. */
 int fides_ntt_batch_device(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint32_t limbs, uint32_t first_prime,
                            int inverse, void* stream);
 /* Same from host memory: copies in, transforms, copies back, synchronises. */
@@ -266,6 +268,23 @@ typedef struct {
 } fides_op;
 int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n);
 
+/* The same from and to host memory, pipelined (no counterpart in the reference, whose API loads, evaluates and
+ * stores one ciphertext per call, api/CryptoContext.cpp:270-289): requests run in chunks of `chunk` (0 = all in
+ * one); chunk k's inputs are copied to the device while chunk k-1 computes and chunk k-2's results are copied
+ * back, on separate streams.  a (and b for ADD / SUB / MULT) are host u64[2][towers][N] with `meta`; out receives
+ * u64[2][out towers][N] and out_meta its metadata.  Returns after every result is in host memory.  Use pinned
+ * host buffers: pageable ones make the copies synchronous. */
+typedef struct {
+  int32_t op;               /* FIDES_OP_* except BOOTSTRAP */
+  const uint64_t* a;
+  const uint64_t* b;
+  fides_ct_meta meta;       /* of a (and b) */
+  int32_t index;            /* rotation index / Galois element / switch-key id */
+  uint64_t* out;
+  fides_ct_meta out_meta;   /* written */
+} fides_host_op;
+int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32_t chunk);
+
 /* Allocation-free rotation (no counterpart in the reference).  For callers that cannot allocate device memory
  * on their request path — a process whose GPU memory is pre-reserved by its own allocator, or a
  * latency-critical caller that cannot pay for cudaMalloc's implicit synchronisation.  Same result as
@@ -278,7 +297,7 @@ int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n);
  * them on one stream.  The first call on a device looks up the array's address with that device current; make
  * it before any stream capture.  `stream` is a cudaStream_t (NULL = the context stream). */
 int fides_eval_rotate_noalloc(fides_ctx* ctx, const uint64_t* dev_in, uint32_t towers, uint32_t galois,
-                              uint64_t* dev_out, void* stream);
+                              uint64_t* dev_out, void* stream);  /* dev_in, dev_out 16-byte aligned */
 
 /* Continuous-batching request server over one context (no counterpart in the reference, whose API runs one op
  * per call).  One worker thread owns the context: while a server runs, use the context only through it.

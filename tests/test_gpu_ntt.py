@@ -85,7 +85,8 @@ def test_both_forward_variants_and_autotuner(engine_lib, logN):
     N = 1 << logN
     ctx, mods = make_ctx(logN, 2, bits=60)
     tune = ctx.ntt_tuning()
-    assert tune["fwd_variant"] in (0, 1) and min(tune["ms_per_64_limbs"]) > 0
+    assert tune["fwd_variant_small"] in (0, 1) and tune["fwd_variant_large"] in (0, 1)
+    assert min(tune["ms_small_v0_v1"] + tune["ms_large_v0_v1"]) > 0
     rng = np.random.default_rng(logN + 100)
     data = np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(2)])[None]
     data[0, 0, :7] = mods[0] - 1

@@ -161,6 +161,35 @@ def test_batch_mixed_ops_same_alone_and_in_mix(env):
         assert np.array_equal(alone, got), op
 
 
+@pytest.mark.parametrize("chunk", [0, 1, 3])
+def test_host_batch_pipelined_equals_oracle(env, chunk):
+    """fides_eval_batch_host (inputs and outputs in host memory, chunks pipelined across copy and compute
+    streams): every output equals the oracle's, for any chunking."""
+    import fideslib_gb300 as F
+    nq = env.nq
+    levels = [nq, max(2, nq // 2), 2, nq, max(2, nq - 1)]
+    g1, k1 = env.rot_key(1)
+    ops, expect = [], []
+    for i, t in enumerate(levels):
+        ct = env.at(t)
+        if i % 3 == 0:
+            out = np.zeros_like(ct)
+            ops.append((F.OP_ROTATE, ct, None, 1, out, env.scale))
+            expect.append(env.orc.rotate(ct, g1, k1))
+        elif i % 3 == 1:
+            out = np.zeros_like(ct)
+            ops.append((F.OP_MULT, ct, ct, 0, out, env.scale))
+            expect.append(env.orc.mult(ct, ct, env.rlk))
+        else:
+            out = np.zeros((2, t - 1, env.N), dtype=np.uint64)
+            ops.append((F.OP_RESCALE, ct, None, 0, out, env.scale))
+            expect.append(env.orc.rescale(ct))
+    metas = env.gpu.eval_batch_host(ops, chunk)
+    for (code, a, b, idx, out, _), e, m in zip(ops, expect, metas):
+        assert np.array_equal(out, e), code
+        assert m.towers == e.shape[1]
+
+
 def test_batched_rotations_full_ring_cfg3(engine_lib):
     """Config-3 shape at full size: N=2^16, 30 Q towers (60 + 29x50 bits), 10 special 60-bit primes, dnum=3.
     Four ciphertexts at levels 0, 13, 21, 28 rotated in one batch (two of them twice, sharing a ModUp):
