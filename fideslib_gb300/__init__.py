@@ -93,6 +93,8 @@ _SIGS = {
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fides_ctx_ntt_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32]),
+    "fides_ctx_set_mem_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "fides_ctx_mem_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_pt_encode": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                   C.c_uint32, u32p]),
     "fides_pt_decode": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -392,6 +394,14 @@ class CryptoContext:
         return {"fwd_variant_small": v[0], "fwd_variant_large": v[1],
                 "ms_small_v0_v1": [round(ms[0], 4), round(ms[1], 4)],
                 "ms_large_v0_v1": [round(ms[2], 4), round(ms[3], 4)]}
+
+    def set_mem_limit(self, nbytes: int):
+        _check(lib().fides_ctx_set_mem_limit(self._h, nbytes))
+
+    def mem_in_use(self) -> int:
+        v = C.c_uint64()
+        _check(lib().fides_ctx_mem_in_use(self._h, C.byref(v)))
+        return v.value
 
     def set_ntt_variant(self, fwd_variant: int):
         _check(lib().fides_ctx_ntt_tuning_set(self._h, fwd_variant))

@@ -80,6 +80,18 @@ int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms) {
   return FIDES_OK;
 }
 
+int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  ctx->c->mem_limit = (size_t)bytes;
+  return FIDES_OK;
+}
+
+int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes) {
+  if (!valid_ctx(ctx) || !bytes) return fail(FIDES_EINVAL, "null argument");
+  *bytes = ctx->c->mem_in_use;
+  return FIDES_OK;
+}
+
 int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
   if (fwd_variant != 0 && fwd_variant != 1) return fail(FIDES_EINVAL, "forward variant must be 0 or 1");

@@ -338,13 +338,28 @@ bool Context::build(const u64* roots, std::string* err) {
 }
 
 u64* Context::alloc_limbs(size_t nlimbs, cudaStream_t s) {
+  const size_t bytes = nlimbs * (size_t)N * sizeof(u64);
+  std::lock_guard<std::mutex> lk(mem_mu_);
+  if (mem_limit && mem_in_use + bytes > mem_limit) return nullptr;  // the caller reports FIDES_ENOMEM
   void* p = nullptr;
-  if (cudaMallocAsync(&p, nlimbs * (size_t)N * sizeof(u64), s) != cudaSuccess) return nullptr;
+  if (cudaMallocAsync(&p, bytes, s) != cudaSuccess) {
+    cudaGetLastError();  // a failed allocation must not surface as a later launch error
+    return nullptr;
+  }
+  mem_in_use += bytes;
+  mem_sizes_[p] = bytes;
   return (u64*)p;
 }
 
 void Context::free_limbs(u64* p, cudaStream_t s) {
-  if (p) cudaFreeAsync(p, s);
+  if (!p) return;
+  cudaFreeAsync(p, s);
+  std::lock_guard<std::mutex> lk(mem_mu_);
+  auto it = mem_sizes_.find(p);
+  if (it != mem_sizes_.end()) {
+    mem_in_use -= it->second;
+    mem_sizes_.erase(it);
+  }
 }
 
 uint32_t Context::galois_inverse(uint32_t g) const {

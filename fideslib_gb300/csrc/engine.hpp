@@ -129,13 +129,17 @@ class Context {
   std::unordered_map<uint32_t, DevLT> lts;
   u64* relin_key = nullptr;
 
+  // Stream-ordered pool allocations of ciphertexts and workspaces, counted against mem_limit (0 = none).
   u64* alloc_limbs(size_t nlimbs, cudaStream_t s);
   void free_limbs(u64* p, cudaStream_t s);
+  size_t mem_limit = 0, mem_in_use = 0;
 
   uint32_t galois_inverse(uint32_t g) const;
   static uint32_t galois_for_index(int N, int32_t index);
 
  private:
+  std::mutex mem_mu_;
+  std::unordered_map<const void*, size_t> mem_sizes_;
   Context() = default;
   bool build(const u64* roots, std::string* err);
   std::vector<void*> owned_;  // device allocations freed at destruction

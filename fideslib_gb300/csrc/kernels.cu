@@ -478,12 +478,17 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
   const int np = c.np;
   const int rows = with_rows(b, bb, [np](const KsJob& j) { return j.t + np; });
   dim3 grid(r.N / (2 * kT), rows, 1);
-  if (c.dnum <= 2)
-    ks_inner_kernel<2><<<grid, kT, 0, s>>>(bb, r, c, pc);
-  else if (c.dnum <= 4)
-    ks_inner_kernel<4><<<grid, kT, 0, s>>>(bb, r, c, pc);
-  else
-    ks_inner_kernel<8><<<grid, kT, 0, s>>>(bb, r, c, pc);
+  switch (c.dnum) {  // beta <= dnum: size the register arrays exactly (fewer registers, more resident warps)
+#define FGB_KSI_CASE(B_)                                   \
+  case B_:                                                 \
+    ks_inner_kernel<B_><<<grid, kT, 0, s>>>(bb, r, c, pc); \
+    break;
+    FGB_KSI_CASE(1) FGB_KSI_CASE(2) FGB_KSI_CASE(3) FGB_KSI_CASE(4) FGB_KSI_CASE(5) FGB_KSI_CASE(6)
+    FGB_KSI_CASE(7) FGB_KSI_CASE(8)
+#undef FGB_KSI_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
   count_launch();
   return cudaGetLastError();
 }

@@ -71,6 +71,12 @@ const char* fides_version(void);
  * 1 = radix-32/16 passes; ms[0..3] = small v0, small v1, large v0, large v1 in ms (-1 where a single kernel
  * applies, N < 2^13). */
 int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms);
+/* Device-memory budget of the context (the reference's pool has a release threshold only, Context.cu:74-80):
+ * ciphertexts and per-op workspaces come from the stream-ordered pool and are counted; an op whose allocation
+ * would exceed `bytes` fails with FIDES_ENOMEM and leaves the context usable (0 = no limit; keys, plaintexts and
+ * transforms are not counted).  fides_ctx_mem_in_use reports the bytes currently counted. */
+int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes);
+int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes);
 /* Overrides the autotuner's choices (both variants give identical residues). */
 int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant);
 /* Parameter helper (the role of OpenFHE's FirstPrime/PreviousPrime in GenCryptoContext): the `count` largest

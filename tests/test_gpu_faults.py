@@ -1,0 +1,75 @@
+"""Failure handling without a GPU fault: device-memory exhaustion is injected through the context's memory
+budget (fides_ctx_set_mem_limit), never by exhausting the GPU.  Every failure must come back as a status code,
+leave nothing allocated, and leave the context (and a request server over it) usable."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+LOGN = 12
+N = 1 << LOGN
+
+
+@pytest.fixture(scope="module")
+def env(engine_lib):
+    import fideslib_gb300 as F
+    mods = O.make_moduli(LOGN, [60] + [45] * 5, [60] * 2)
+    gpu = F.CryptoContext(LOGN, mods, 2, 3)
+    orc = O.Ctx(N, 6, 2, 3, mods, threads=8)
+    s = orc.secret(11)
+    g = orc.galois(3)
+    key = orc.rot_key(12, s, g)
+    gpu.load_rotation_key(g, key)
+    rlk = orc.relin_key(13, s)
+    gpu.load_eval_mult_key(rlk)
+    rng = np.random.default_rng(3)
+    ct = orc.encrypt(14, s, orc.encode(rng.uniform(-1, 1, N // 2), 2.0 ** 40, 6))
+    return dict(F=F, gpu=gpu, orc=orc, g=g, key=key, rlk=rlk, ct=ct)
+
+
+def test_out_of_memory_is_a_status_and_recoverable(env):
+    F, gpu, orc = env["F"], env["gpu"], env["orc"]
+    h = gpu.load_ciphertext(env["ct"], 2.0 ** 40)
+    base = gpu.mem_in_use()
+    gpu.set_mem_limit(base + 8 * N * 4)  # room for 4 limbs: an output ciphertext fits, the key-switch workspace not
+    for call in (lambda: gpu.eval_rotate(h, 3), lambda: gpu.eval_mult(h, h),
+                 lambda: gpu.eval_batch([(F.OP_ROTATE, h, 0, 3), (F.OP_SQUARE, h, 0, 0)])):
+        with pytest.raises(F.FidesError) as ei:
+            call()
+        assert ei.value.code == F.FIDES_ENOMEM
+        assert gpu.mem_in_use() == base  # nothing leaked by the failed op
+    gpu.set_mem_limit(0)
+    got = gpu.store_ciphertext(gpu.eval_rotate(h, 3))
+    assert np.array_equal(got, orc.rotate(env["ct"], env["g"], env["key"]))
+
+
+def test_server_reports_per_request_status(env):
+    """Under a budget that admits rescales but not key switches, a mixed stream completes: the rescales succeed
+    with the right residues, the rotations come back with FIDES_ENOMEM, and the server keeps serving."""
+    F, gpu, orc = env["F"], env["gpu"], env["orc"]
+    h = gpu.load_ciphertext(env["ct"], 2.0 ** 40)
+    base = gpu.mem_in_use()
+    # a rescale at 6 towers takes 10 output + 12 workspace limbs, a rotation 12 + 50: with up to three rescale
+    # results held, 56 limbs admit every rescale and no rotation
+    gpu.set_mem_limit(base + 8 * N * 56)
+    srv = F.Server(gpu, max_batch=4, max_inflight=1, mem_budget=1 << 30)
+    tickets = [srv.submit(F.OP_RESCALE if i % 2 == 0 else F.OP_ROTATE, h, 0, 0 if i % 2 == 0 else 3)
+               for i in range(6)]
+    results = []
+    for i, t in enumerate(tickets):
+        try:
+            results.append(("ok", srv.wait(t)[0]))
+        except F.FidesError as e:
+            results.append(("err", e.code))
+    srv.close()
+    gpu.set_mem_limit(0)
+    expect = orc.rescale(env["ct"])
+    for i, (kind, v) in enumerate(results):
+        if i % 2 == 0:
+            assert kind == "ok"
+            assert np.array_equal(gpu.store_ciphertext(v), expect)
+            gpu.free(v)
+        else:
+            assert (kind, v) == ("err", F.FIDES_ENOMEM)
