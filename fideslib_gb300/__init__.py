@@ -73,6 +73,9 @@ _SIGS = {
     "fides_eval_rotate": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int32, u32p]),
     "fides_eval_automorphism": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_eval_fast_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, i32p, u32p]),
+    "fides_fast_rotation_precompute": (C.c_int, [C.c_void_p, C.c_uint32, u32p]),
+    "fides_eval_fast_rotation_precomputed": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, u32p]),
+    "fides_precompute_free": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fides_eval_batch_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]),
     "fides_eval_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "fides_ctx_get_shape": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -501,6 +504,17 @@ class CryptoContext:
                             CtMeta(a.shape[1], 1, 0, 0, scale), index, out.ctypes.data, CtMeta())
         _check(lib().fides_eval_batch_host(self._h, arr, len(ops), chunk))
         return [arr[i].out_meta for i in range(len(ops))]
+
+    def fast_rotation_precompute(self, a: int) -> int:
+        h = C.c_uint32()
+        _check(lib().fides_fast_rotation_precompute(self._h, a, C.byref(h)))
+        return h.value
+
+    def eval_fast_rotation_precomputed(self, a: int, pre: int, index: int) -> int:
+        return self._un(lib().fides_eval_fast_rotation_precomputed, a, pre, index)
+
+    def precompute_free(self, pre: int):
+        _check(lib().fides_precompute_free(self._h, pre))
 
     def eval_fast_rotation(self, a: int, indices) -> list[int]:
         idx = np.ascontiguousarray(np.array(indices, dtype=np.int32))

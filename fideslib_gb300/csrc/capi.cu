@@ -578,6 +578,78 @@ int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_
   return one(ctx, FIDES_OP_AUTOMORPHISM, a, 0, (int32_t)galois, out);
 }
 
+int fides_fast_rotation_precompute(fides_ctx* ctx, uint32_t a, uint32_t* pre) {
+  if (!valid_ctx(ctx) || !pre) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(a));
+  if (int rc = check_ks_shape(ctx)) return rc;
+  const int t = A->t, beta = (t + c->alpha - 1) / c->alpha;
+  fgb::DevModUp m;
+  m.t = t;
+  m.c1 = c->alloc_limbs((size_t)t, c->stream);
+  m.digits = c->alloc_limbs((size_t)beta * (t + c->np), c->stream);
+  fgb::u64* scratch = c->alloc_limbs((size_t)t, c->stream);
+  auto release = [&]() {
+    c->free_limbs(m.c1, c->stream);
+    c->free_limbs(m.digits, c->stream);
+    c->free_limbs(scratch, c->stream);
+  };
+  if (!m.c1 || !m.digits || !scratch) {
+    release();
+    return fail(FIDES_ENOMEM, "precomputation allocation failed");
+  }
+  const size_t NN = (size_t)c->N;
+  cudaError_t e = cudaMemcpyAsync(m.c1, A->data + (size_t)t * NN, (size_t)t * NN * sizeof(fgb::u64),
+                                  cudaMemcpyDeviceToDevice, c->stream);
+  const fgb::u64* in = m.c1;
+  if (e == cudaSuccess) e = c->modup(&in, &t, &scratch, &m.digits, 1, c->stream);
+  c->free_limbs(scratch, c->stream);
+  if (e != cudaSuccess) {
+    c->free_limbs(m.c1, c->stream);
+    c->free_limbs(m.digits, c->stream);
+    return cuda_fail(e, "fast rotation precompute");
+  }
+  const uint32_t h = c->next_handle++;
+  c->modups[h] = m;
+  *pre = h;
+  return FIDES_OK;
+}
+
+int fides_eval_fast_rotation_precomputed(fides_ctx* ctx, uint32_t a, uint32_t pre, int32_t index, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  auto it = c->modups.find(pre);
+  if (!A || it == c->modups.end()) return fail(FIDES_EINVAL, "unknown ciphertext or precomputation handle");
+  const fgb::DevModUp& M = it->second;
+  if (M.t != A->t) return fail(FIDES_EINVAL, "precomputation was made at a different tower count");
+  const uint32_t g = fgb::Context::galois_for_index(c->N, index);
+  auto kt = c->rot_keys.find(g);
+  if (kt == c->rot_keys.end()) return fail(FIDES_ENOKEY, "no rotation key for Galois element " + std::to_string(g));
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, *A, &r);
+  if (rc) return rc;
+  fgb::Context::KsReq q{M.c1, A->t, kt->second, A->data, nullptr, r.data, c->galois_inverse(g), M.digits};
+  const cudaError_t e = c->keyswitch_batch(&q, 1, c->stream);
+  if (e != cudaSuccess) {
+    c->free_limbs(r.data, c->stream);
+    return cuda_fail(e, "fast rotation");
+  }
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_precompute_free(fides_ctx* ctx, uint32_t pre) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  auto it = ctx->c->modups.find(pre);
+  if (it == ctx->c->modups.end()) return fail(FIDES_EINVAL, "unknown precomputation handle");
+  ctx->c->free_limbs(it->second.c1, ctx->c->stream);
+  ctx->c->free_limbs(it->second.digits, ctx->c->stream);
+  ctx->c->modups.erase(it);
+  return FIDES_OK;
+}
+
 int fides_eval_key_switch(fides_ctx* ctx, uint32_t a, uint32_t key_id, uint32_t* out) {
   return one(ctx, FIDES_OP_KEY_SWITCH, a, 0, (int32_t)key_id, out);
 }

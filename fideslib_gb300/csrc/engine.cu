@@ -114,6 +114,10 @@ Context::~Context() {
     if (kv.second.data) cudaFree(kv.second.data);
   for (auto& kv : pts)
     if (kv.second.data) cudaFree(kv.second.data);
+  for (auto& kv : modups) {
+    if (kv.second.c1) cudaFree(kv.second.c1);
+    if (kv.second.digits) cudaFree(kv.second.digits);
+  }
   for (auto& kv : lts) {
     if (kv.second.diags) cudaFree(kv.second.diags);
     if (kv.second.present_dev) cudaFree(kv.second.present_dev);
@@ -414,19 +418,67 @@ cudaError_t Context::ntt(const u64* src, u64* dst, int npolys, int limbs, int fi
   return q.err;
 }
 
+cudaError_t Context::modup(const u64* const* a, const int* ts, u64* const* coeff, u64* const* conv, int ng,
+                           cudaStream_t s) {
+  const size_t NN = (size_t)N;
+  cudaError_t err = cudaSuccess;
+  uint8_t pm[64];
+  // 1) INTT of every input into its coefficient buffer
+  {
+    NttQueue q(tabs, true, s);
+    for (int g = 0; g < ng; g++) {
+      for (int j = 0; j < ts[g]; j++) pm[j] = (uint8_t)j;
+      q.add(a[g], coeff[g], 0, 0, ts[g], 1, pm);
+    }
+    q.flush();
+    err = q.err;
+  }
+  // 2) ModUp basis conversion, 3) NTT of the converted rows
+  for (int g0 = 0; g0 < ng && err == cudaSuccess; g0 += kMaxJobs) {
+    KsBatch kb{};
+    for (int g = g0; g < ng && kb.njobs < kMaxJobs; g++) {
+      KsJob& j = kb.jobs[kb.njobs++];
+      j = KsJob{};
+      j.a = a[g];
+      j.coeff = coeff[g];
+      j.conv = conv[g];
+      j.t = ts[g];
+    }
+    err = launch_modup_conv(kb, ring_, crt, d_pc, s);
+  }
+  if (err == cudaSuccess) {
+    NttQueue q(tabs, false, s);
+    for (int g = 0; g < ng; g++) {
+      const int t = ts[g], beta = (t + alpha - 1) / alpha;
+      for (int d = 0; d < beta; d++) {
+        const int start = d * alpha, sz = std::min(alpha, t - start), rows = t - sz + np;
+        for (int jj = 0; jj < rows; jj++)
+          pm[jj] = (uint8_t)(jj < start ? jj : (jj < t - sz ? jj + sz : nq + (jj - (t - sz))));
+        u64* c = conv[g] + (size_t)d * (t + np) * NN;
+        q.add(c, c, 0, 0, rows, 1, pm);
+      }
+    }
+    q.flush();
+    err = q.err;
+  }
+  return err;
+}
+
 cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const size_t NN = (size_t)N;
-  // ModUp groups: requests with the same input share the digits.
+  // ModUp groups: requests with the same input (and no precomputed digits) share the digits.
   std::vector<int> group_of(n);
   std::vector<int> gfirst;
   for (int i = 0; i < n; i++) {
     int g = -1;
-    for (size_t k = 0; k < gfirst.size(); k++)
-      if (reqs[gfirst[k]].a == reqs[i].a && reqs[gfirst[k]].t == reqs[i].t) {
+    for (size_t k = 0; k < gfirst.size(); k++) {
+      const KsReq& f = reqs[gfirst[k]];
+      if (f.a == reqs[i].a && f.t == reqs[i].t && f.digits == reqs[i].digits) {
         g = (int)k;
         break;
       }
+    }
     if (g < 0) {
       g = (int)gfirst.size();
       gfirst.push_back(i);
@@ -439,7 +491,7 @@ cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
   for (int g = 0; g < ng; g++) {
     const int t = reqs[gfirst[g]].t, beta = (t + alpha - 1) / alpha;
     g_off[g] = total;
-    total += (size_t)t + (size_t)beta * (t + np);
+    if (!reqs[gfirst[g]].digits) total += (size_t)t + (size_t)beta * (t + np);
   }
   for (int i = 0; i < n; i++) {
     const int t = reqs[i].t;
@@ -449,51 +501,25 @@ cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
   u64* ws = alloc_limbs(total, s);
   if (!ws) return cudaErrorMemoryAllocation;
   auto coeff_of = [&](int g) { return ws + g_off[g] * NN; };
-  auto conv_of = [&](int g) { return ws + (g_off[g] + reqs[gfirst[g]].t) * NN; };
+  auto conv_of = [&](int g) {
+    const KsReq& f = reqs[gfirst[g]];
+    return f.digits ? const_cast<u64*>(f.digits) : ws + (g_off[g] + f.t) * NN;
+  };
   auto inner_of = [&](int i) { return ws + r_off[i] * NN; };
   auto md_of = [&](int i) { return ws + (r_off[i] + 2 * (size_t)(reqs[i].t + np)) * NN; };
-  cudaError_t err = cudaSuccess;
   uint8_t pm[64];
-
-  // 1) INTT of every distinct input into its coefficient buffer
-  {
-    NttQueue q(tabs, true, s);
-    for (int g = 0; g < ng; g++) {
-      const KsReq& r = reqs[gfirst[g]];
-      for (int j = 0; j < r.t; j++) pm[j] = (uint8_t)j;
-      q.add(r.a, coeff_of(g), 0, 0, r.t, 1, pm);
-    }
-    q.flush();
-    err = q.err;
+  std::vector<const u64*> ma;
+  std::vector<int> mt;
+  std::vector<u64*> mcoeff, mconv;
+  for (int g = 0; g < ng; g++) {
+    const KsReq& f = reqs[gfirst[g]];
+    if (f.digits) continue;  // precomputed (fides_fast_rotation_precompute)
+    ma.push_back(f.a);
+    mt.push_back(f.t);
+    mcoeff.push_back(coeff_of(g));
+    mconv.push_back(conv_of(g));
   }
-  // 2) ModUp basis conversion, 3) NTT of the converted rows
-  for (int g0 = 0; g0 < ng && err == cudaSuccess; g0 += kMaxJobs) {
-    KsBatch kb{};
-    for (int g = g0; g < ng && kb.njobs < kMaxJobs; g++) {
-      KsJob& j = kb.jobs[kb.njobs++];
-      j = KsJob{};
-      j.a = reqs[gfirst[g]].a;
-      j.coeff = coeff_of(g);
-      j.conv = conv_of(g);
-      j.t = reqs[gfirst[g]].t;
-    }
-    err = launch_modup_conv(kb, ring_, crt, d_pc, s);
-  }
-  if (err == cudaSuccess) {
-    NttQueue q(tabs, false, s);
-    for (int g = 0; g < ng; g++) {
-      const int t = reqs[gfirst[g]].t, beta = (t + alpha - 1) / alpha;
-      for (int d = 0; d < beta; d++) {
-        const int start = d * alpha, sz = std::min(alpha, t - start), rows = t - sz + np;
-        for (int jj = 0; jj < rows; jj++)
-          pm[jj] = (uint8_t)(jj < start ? jj : (jj < t - sz ? jj + sz : nq + (jj - (t - sz))));
-        u64* c = conv_of(g) + (size_t)d * (t + np) * NN;
-        q.add(c, c, 0, 0, rows, 1, pm);
-      }
-    }
-    q.flush();
-    err = q.err;
-  }
+  cudaError_t err = modup(ma.data(), mt.data(), mcoeff.data(), mconv.data(), (int)ma.size(), s);
   // 4) inner products, 5) INTT of the P rows, 6) ModDown conversion, 7) NTT, 8) epilogue
   for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
     KsBatch kb{};

@@ -27,6 +27,14 @@ struct DevCt {
   int slots = 0;
 };
 
+// Precomputed ModUp of a ciphertext's c1 (EvalFastRotationPrecompute): a copy of c1 (its own-digit towers are
+// read from it) and the extended digits.
+struct DevModUp {
+  u64* c1 = nullptr;      // [t][N] evaluation form
+  u64* digits = nullptr;  // [beta][t+np][N], modup()'s layout
+  int t = 0;
+};
+
 struct DevPt {
   u64* data = nullptr;  // [t][N] evaluation form
   int t = 0;
@@ -82,9 +90,13 @@ class Context {
     const u64* add1;
     u64* out;
     uint32_t galois_inv;
+    const u64* digits = nullptr;  // precomputed ModUp of `a` (modup()'s conv layout); skips the ModUp
   };
   // All requests in one pipeline: requests with the same (a, t) share one ModUp (hoisting).
   cudaError_t keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s);
+  // ModUp of ng inputs a[g] (t[g] towers, evaluation form): coeff[g] (t limbs) is scratch, conv[g] receives the
+  // beta (t + np) limbs of extended digits (digit d at conv + d (t+np) N; its own towers are not written).
+  cudaError_t modup(const u64* const* a, const int* ts, u64* const* coeff, u64* const* conv, int ng, cudaStream_t s);
 
   struct MultReq {
     const u64* x;
@@ -126,6 +138,7 @@ class Context {
   uint32_t next_handle = 1;
   std::map<uint32_t, u64*> rot_keys;  // Galois element -> key
   std::unordered_map<uint32_t, DevPt> pts;
+  std::unordered_map<uint32_t, DevModUp> modups;
   std::unordered_map<uint32_t, DevLT> lts;
   u64* relin_key = nullptr;
 

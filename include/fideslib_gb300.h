@@ -64,21 +64,6 @@ typedef struct {
 const char* fides_last_error(void);
 const char* fides_version(void);
 
-/* The NTT autotuner's choices for this ring (no counterpart in the reference, whose NTT kernel is fixed at build
- * time): at context creation both forward kernels are timed on a small and a large scratch batch (64 and 640
- * limbs' worth of residues at N = 2^16) and the faster one of each size is used for launches of at most / more
- * than 256 limbs' worth.  fwd_variant[0] (small), [1] (large): 0 = radix-16 passes (three CTAs per SM),
- * 1 = radix-32/16 passes; ms[0..3] = small v0, small v1, large v0, large v1 in ms (-1 where a single kernel
- * applies, N < 2^13). */
-int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms);
-/* Device-memory budget of the context (the reference's pool has a release threshold only, Context.cu:74-80):
- * ciphertexts and per-op workspaces come from the stream-ordered pool and are counted; an op whose allocation
- * would exceed `bytes` fails with FIDES_ENOMEM and leaves the context usable (0 = no limit; keys, plaintexts and
- * transforms are not counted).  fides_ctx_mem_in_use reports the bytes currently counted. */
-int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes);
-int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes);
-/* Overrides the autotuner's choices (both variants give identical residues). */
-int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant);
 /* Parameter helper (the role of OpenFHE's FirstPrime/PreviousPrime in GenCryptoContext): the `count` largest
  * primes below 2^bits that are == 1 mod two_n, skipping `exclude`.  Returns the number found. */
 int fides_find_primes(uint32_t bits, uint32_t count, uint64_t two_n, const uint64_t* exclude, uint32_t nexclude,
@@ -99,6 +84,21 @@ int fides_synchronize(fides_ctx* ctx);
  * LimbPartition / Stream (src/CudaUtils.cuh:98-160). */
 void* fides_ctx_stream(fides_ctx* ctx);
 int fides_ctx_set_stream(fides_ctx* ctx, void* stream);
+/* The NTT autotuner's choices for this ring (no counterpart in the reference, whose NTT kernel is fixed at build
+ * time): at context creation both forward kernels are timed on a small and a large scratch batch (64 and 640
+ * limbs' worth of residues at N = 2^16) and the faster one of each size is used for launches of at most / more
+ * than 256 limbs' worth.  fwd_variant[0] (small), [1] (large): 0 = radix-16 passes (three CTAs per SM),
+ * 1 = radix-32/16 passes; ms[0..3] = small v0, small v1, large v0, large v1 in ms (-1 where a single kernel
+ * applies, N < 2^13). */
+int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms);
+/* Device-memory budget of the context (the reference's pool has a release threshold only, Context.cu:74-80):
+ * ciphertexts and per-op workspaces come from the stream-ordered pool and are counted; an op whose allocation
+ * would exceed `bytes` fails with FIDES_ENOMEM and leaves the context usable (0 = no limit; keys, plaintexts and
+ * transforms are not counted).  fides_ctx_mem_in_use reports the bytes currently counted. */
+int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes);
+int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes);
+/* Overrides the autotuner's choices (both variants give identical residues). */
+int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant);
 /* Ring and basis shape of a context. */
 typedef struct {
   uint32_t n, log_n, nq, np, dnum, alpha;
@@ -150,6 +150,14 @@ int fides_eval_automorphism(fides_ctx* ctx, uint32_t a, uint32_t galois, uint32_
 /* Key switch with a key loaded by fides_load_switch_key (Ciphertext::keySwitch, src/CKKS/Ciphertext.cpp:1354). */
 int fides_eval_key_switch(fides_ctx* ctx, uint32_t a, uint32_t key_id, uint32_t* out);
 int fides_eval_fast_rotation(fides_ctx* ctx, uint32_t a, uint32_t n, const int32_t* indices, uint32_t* outs);
+/* EvalFastRotationPrecompute (api/CryptoContext.hpp:169): the ModUp of a's c1, kept on the device under a handle
+ * (a copy of c1 is kept with it, so `a` may change or be freed afterwards). */
+int fides_fast_rotation_precompute(fides_ctx* ctx, uint32_t a, uint32_t* pre);
+/* EvalFastRotation(ct, index, m, precomp) (api/CryptoContext.hpp:170): the rotation of `a` by `index` from the
+ * precomputed digits; `a` must be the ciphertext the digits were computed from (same residues).  Same result as
+ * fides_eval_rotate. */
+int fides_eval_fast_rotation_precomputed(fides_ctx* ctx, uint32_t a, uint32_t pre, int32_t index, uint32_t* out);
+int fides_precompute_free(fides_ctx* ctx, uint32_t pre);
 
 /* Plaintexts (RawPlainText / LoadPlaintext, RawCiphertext.cuh:37-48, api/CryptoContext.cpp:250-269):
  * u64[towers][N] evaluation form at scaling factor `scale`. */

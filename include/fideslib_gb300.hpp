@@ -3,7 +3,8 @@
 // Mirrors the method names and argument meaning of the reference's fideslib::CryptoContextImpl<DCRTPoly>
 // (api/CryptoContext.hpp:43-203) for the evaluation hot path, on raw residues instead of OpenFHE objects:
 // LoadContext (the constructor), LoadCiphertext / LoadPlaintext, EvalAdd / EvalSub / EvalMult / EvalSquare,
-// EvalRotate, EvalFastRotation, Rescale, EvalChebyshevSeries, EvalBootstrap, Synchronize.  Like the reference
+// EvalRotate, EvalFastRotationPrecompute / EvalFastRotation, the *InPlace forms, Rescale, EvalChebyshevSeries,
+// EvalBootstrap, Synchronize.  Like the reference
 // API it reports failures by throwing (fideslib_gb300::Error carries the C status code and message); the C ABI
 // underneath never throws or exits.  Ciphertext is a shared, reference-counted device handle
 // (the reference's Ciphertext<DCRTPoly> is a shared_ptr, api/Ciphertext.hpp:13-58).
@@ -99,6 +100,26 @@ class Plaintext {
   std::shared_ptr<Handle> h_;
 };
 
+// EvalFastRotationPrecompute's result (the reference returns a shared_ptr<void>, api/CryptoContext.hpp:169).
+class Precomputation {
+ public:
+  Precomputation() = default;
+  uint32_t handle() const { return h_ ? h_->id : 0; }
+
+ private:
+  friend class CryptoContext;
+  struct Handle {
+    Handle(fides_ctx* c, uint32_t i) : ctx(c), id(i) {}
+    Handle(const Handle&) = delete;
+    Handle& operator=(const Handle&) = delete;
+    ~Handle() { fides_precompute_free(ctx, id); }
+    fides_ctx* ctx;
+    uint32_t id;
+  };
+  Precomputation(fides_ctx* ctx, uint32_t id) : h_(std::make_shared<Handle>(ctx, id)) {}
+  std::shared_ptr<Handle> h_;
+};
+
 class CryptoContext {
  public:
   // LoadContext: moduli, roots and all derived tables to the device.
@@ -166,6 +187,23 @@ class CryptoContext {
     for (uint32_t h : outs) r.push_back(Ciphertext(ctx_, h));
     return r;
   }
+  Precomputation EvalFastRotationPrecompute(const Ciphertext& a) {
+    uint32_t h;
+    check(fides_fast_rotation_precompute(ctx_, a.handle(), &h));
+    return Precomputation(ctx_, h);
+  }
+  // EvalFastRotation(ct, index, m, precomp): m (the cyclotomic order) is implied by the context.
+  Ciphertext EvalFastRotation(const Ciphertext& a, int32_t index, uint32_t /*m*/, const Precomputation& pre) {
+    return wrap(fides_eval_fast_rotation_precomputed(ctx_, a.handle(), pre.handle(), index, &tmp_));
+  }
+  // In-place forms (EvalAddInPlace, EvalMultInPlace, EvalSquareInPlace, RescaleInPlace, EvalRotateInPlace): the
+  // handle is replaced by the result's.
+  void EvalAddInPlace(Ciphertext& a, const Ciphertext& b) { a = EvalAdd(a, b); }
+  void EvalSubInPlace(Ciphertext& a, const Ciphertext& b) { a = EvalSub(a, b); }
+  void EvalMultInPlace(Ciphertext& a, const Ciphertext& b) { a = EvalMult(a, b); }
+  void EvalSquareInPlace(Ciphertext& a) { a = EvalSquare(a); }
+  void RescaleInPlace(Ciphertext& a) { a = Rescale(a); }
+  void EvalRotateInPlace(Ciphertext& a, int32_t index) { a = EvalRotate(a, index); }
   Ciphertext EvalChebyshevSeries(const Ciphertext& a, const std::vector<double>& coeffs, double lo, double hi,
                                  double const_scale) {
     return wrap(fides_eval_chebyshev(ctx_, a.handle(), coeffs.data(), (uint32_t)coeffs.size(), lo, hi, const_scale,

@@ -55,6 +55,13 @@ int main() {
   same(hoisted[0], cc.EvalRotate(a, 1), "hoisted rotation by 1");
   same(hoisted[1], cc.EvalRotate(a, 2), "hoisted rotation by 2");
   same(cc.EvalMult(a, b), cc.EvalMult(b, a), "mult commutes");
+  {  // EvalFastRotationPrecompute + EvalFastRotation(ct, index, m, precomp) == EvalRotate
+    auto pre = cc.EvalFastRotationPrecompute(a);
+    same(cc.EvalFastRotation(a, 2, cc.GetCyclotomicOrder(), pre), cc.EvalRotate(a, 2), "precomputed rotation");
+    Ciphertext c = a;
+    cc.EvalRotateInPlace(c, 1);
+    same(c, hoisted[0], "in-place rotation");
+  }
   if (cc.StoreCiphertext(cc.EvalSub(cc.EvalAdd(a, b), b)) != ha) {
     std::printf("mismatch: (a + b) - b\n");
     fails++;

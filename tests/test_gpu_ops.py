@@ -81,6 +81,24 @@ def test_fast_rotation_bit_exact(env):
         assert np.array_equal(env.gpu.store_ciphertext(o), e)
 
 
+def test_precomputed_fast_rotation(env):
+    """EvalFastRotationPrecompute, then rotations by several indices from the kept digits (after the source
+    handle is freed): bit-identical to plain rotations and to the oracle."""
+    for t in sorted({env.nq, 2}):
+        ct = env.at(t)
+        h = env.gpu.load_ciphertext(ct, env.scale)
+        pre = env.gpu.fast_rotation_precompute(h)
+        outs = {}
+        for index in (1, -5, 3):
+            g, key = env.rot_key(index)
+            outs[index] = env.gpu.store_ciphertext(env.gpu.eval_fast_rotation_precomputed(h, pre, index))
+            assert np.array_equal(outs[index], env.orc.rotate(ct, g, key)), (t, index)
+        h2 = env.gpu.load_ciphertext(ct, env.scale)  # the same residues under another handle
+        env.gpu.free(h)
+        assert np.array_equal(env.gpu.store_ciphertext(env.gpu.eval_fast_rotation_precomputed(h2, pre, 1)), outs[1])
+        env.gpu.precompute_free(pre)
+
+
 def test_mult_square_rescale_bit_exact(env):
     for t in sorted({env.nq, max(2, env.nq // 2 + 1), 2}):
         ct = env.at(t)
@@ -99,6 +117,21 @@ def test_mult_square_rescale_bit_exact(env):
         assert err < 1e-4, err
         meta = env.gpu.meta(r)
         assert meta.towers == t - 1 and meta.noise_deg == 1
+
+
+def test_mult_square_rotate_at_every_level(env):
+    """Mult, Square and Rotate at every tower count (the reference's all-levels cases, test/OpenFheInterfaceTests.cu
+    Mult/Square/Rotate all levels): bit-identical to the oracle."""
+    levels = range(1, env.nq + 1) if env.nq <= 8 else sorted({1, 2, 3, env.nq // 3, env.nq // 2, env.nq - 1, env.nq})
+    g, key = env.rot_key(2)
+    for t in levels:
+        ct = env.at(t)
+        h = env.gpu.load_ciphertext(ct, env.scale)
+        expect_mult = env.orc.mult(ct, ct, env.rlk)
+        assert np.array_equal(env.gpu.store_ciphertext(env.gpu.eval_mult(h, h)), expect_mult), t
+        assert np.array_equal(env.gpu.store_ciphertext(env.gpu.eval_square(h)), expect_mult), t
+        assert np.array_equal(env.gpu.store_ciphertext(env.gpu.eval_rotate(h, 2)), env.orc.rotate(ct, g, key)), t
+        env.gpu.free(h)
 
 
 def test_add_sub_bit_exact(env):
