@@ -95,7 +95,7 @@ _SIGS = {
                                           u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fides_ctx_ntt_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
-    "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32]),
+    "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "fides_ctx_set_mem_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fides_ctx_mem_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_pt_encode": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32, C.c_double,
@@ -391,12 +391,13 @@ class CryptoContext:
 
     def ntt_tuning(self) -> dict:
         """The forward-NTT variants the autotuner chose at creation (small / large launches) and the timings."""
-        v = (C.c_int32 * 2)()
-        ms = (C.c_float * 4)()
+        v = (C.c_int32 * 4)()
+        ms = (C.c_float * 10)()
         _check(lib().fides_ctx_ntt_tuning(self._h, v, ms))
-        return {"fwd_variant_small": v[0], "fwd_variant_large": v[1],
-                "ms_small_v0_v1": [round(ms[0], 4), round(ms[1], 4)],
-                "ms_large_v0_v1": [round(ms[2], 4), round(ms[3], 4)]}
+        r = lambda a, b: [round(ms[i], 4) for i in range(a, b)]  # noqa: E731
+        return {"fwd_variant_small": v[0], "fwd_variant_large": v[1], "inv_variant_small": v[2],
+                "inv_variant_large": v[3], "fwd_ms_small": r(0, 3), "fwd_ms_large": r(3, 6),
+                "inv_ms_small": r(6, 8), "inv_ms_large": r(8, 10)}
 
     def set_mem_limit(self, nbytes: int):
         _check(lib().fides_ctx_set_mem_limit(self._h, nbytes))
@@ -406,8 +407,8 @@ class CryptoContext:
         _check(lib().fides_ctx_mem_in_use(self._h, C.byref(v)))
         return v.value
 
-    def set_ntt_variant(self, fwd_variant: int):
-        _check(lib().fides_ctx_ntt_tuning_set(self._h, fwd_variant))
+    def set_ntt_variant(self, fwd_variant: int, inv_variant: int = 0):
+        _check(lib().fides_ctx_ntt_tuning_set(self._h, fwd_variant, inv_variant))
 
     def encode(self, z, scale: float, towers: int) -> int:
         """Plaintext handle: the slot vector z (complex, length a power of two <= N/2) encoded on the GPU."""

@@ -99,6 +99,12 @@ __device__ __forceinline__ u64 reduce128_fast(u64 hi, u64 lo, const PrimeConst& 
   return csub(s, c.p);
 }
 
+// The same without the final corrections: a value congruent to z in [0, 8p), for consumers that accept lazy
+// inputs (the forward NTT takes [0, 8p)).
+__device__ __forceinline__ u64 reduce128_lazy8(u64 hi, u64 lo, const PrimeConst& c) {
+  return shoup_lazy4(hi, c.r64, c.r64_sh, c.negp) + reduce64_lazy4(lo, c.one_sh, c.negp);
+}
+
 __device__ __forceinline__ u64 mul_mod(u64 a, u64 b, const PrimeConst& c) {
   return reduce128_fast(mulhi(a, b), a * b, c);
 }

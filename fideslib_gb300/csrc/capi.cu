@@ -69,14 +69,17 @@ extern "C" {
 const char* fides_last_error(void) { return g_err.c_str(); }
 const char* fides_version(void) { return "fideslib_gb300 0.1 (sm_103a)"; }
 
-int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms) {
+int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
-  if (fwd_variant) {
-    fwd_variant[0] = ctx->c->tabs.fwd_variant_small;
-    fwd_variant[1] = ctx->c->tabs.fwd_variant;
+  const fgb::DeviceTables& t = ctx->c->tabs;
+  if (variant) {
+    variant[0] = t.fwd_variant_small;
+    variant[1] = t.fwd_variant;
+    variant[2] = t.inv_variant_small;
+    variant[3] = t.inv_variant;
   }
   if (ms)
-    for (int i = 0; i < 4; i++) ms[i] = ctx->c->ntt_tune_ms[i];
+    for (int i = 0; i < 2 * (fgb::kNttFwdVariants + fgb::kNttInvVariants); i++) ms[i] = ctx->c->ntt_tune_ms[i];
   return FIDES_OK;
 }
 
@@ -92,12 +95,17 @@ int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes) {
   return FIDES_OK;
 }
 
-int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant) {
+int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant, int32_t inv_variant) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
-  if (fwd_variant != 0 && fwd_variant != 1) return fail(FIDES_EINVAL, "forward variant must be 0 or 1");
-  if (ctx->c->logN < 13 && fwd_variant == 0) return fail(FIDES_EINVAL, "the radix-16 forward needs N >= 2^13");
+  if (fwd_variant < 0 || fwd_variant >= fgb::kNttFwdVariants || inv_variant < 0 ||
+      inv_variant >= fgb::kNttInvVariants)
+    return fail(FIDES_EINVAL, "forward variant must be 0, 1 or 2 and inverse variant 0 or 1");
+  if (ctx->c->logN < 13 && (fwd_variant != 1 || inv_variant != 0))
+    return fail(FIDES_EINVAL, "below N = 2^13 only forward variant 1 and inverse variant 0 exist");
   cudaStreamSynchronize(ctx->c->stream);
-  ctx->c->tabs.fwd_variant = ctx->c->tabs.fwd_variant_small = fwd_variant;
+  fgb::DeviceTables& t = ctx->c->tabs;
+  t.fwd_variant = t.fwd_variant_small = fwd_variant;
+  t.inv_variant = t.inv_variant_small = inv_variant;
   return FIDES_OK;
 }
 

@@ -71,7 +71,7 @@ class Context {
   cudaStream_t copy_in = nullptr, copy_out = nullptr;  // copy streams of the pipelined host batch (lazily made)
 
   DeviceTables tabs{};
-  float ntt_tune_ms[4] = {-1.f, -1.f, -1.f, -1.f};  // forward NTT variants timed by tune_ntt (small, large)
+  float ntt_tune_ms[2 * (kNttFwdVariants + kNttInvVariants)] = {};  // tune_ntt timings
   CrtTables crt{};
   PrimeConst* d_pc = nullptr;
 

@@ -65,7 +65,8 @@ __device__ __forceinline__ int conv_tower(int jj, int start, int s, int t, int n
 // Basis conversion core: for one coefficient, outputs sum_{i<S} y_i * c_{i,jj} mod m_jj for jj < nout, with the
 // S inputs y_i (already multiplied by the Qhat^-1 / Phat^-1 factor) held in registers as 30-bit halves and the
 // constants c_{i,jj} staged in shared memory as 30-bit halves.  S is a compile-time constant so no multiply-add
-// is issued for absent towers.
+// is issued for absent towers.  Every output feeds a forward NTT, which accepts residues in [0, 8p), so the
+// outputs are left unreduced in that range (the NTT's own output is fully reduced).
 template <int S, class TowerOf>
 __device__ __forceinline__ void conv_rows(const uint32_t (&yl)[S], const uint32_t (&yh)[S], const uint2* cs, int nout,
                                           u64* out, size_t stride, const PrimeConst* __restrict__ pc, TowerOf tower_of) {
@@ -82,7 +83,7 @@ __device__ __forceinline__ void conv_rows(const uint32_t (&yl)[S], const uint32_
       }
       acc4_fold(A, hi, lo);
     }
-    out[(size_t)jj * stride] = reduce128_fast(hi, lo, pc[tower_of(jj)]);
+    out[(size_t)jj * stride] = reduce128_lazy8(hi, lo, pc[tower_of(jj)]);
   }
 }
 

@@ -298,35 +298,37 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
 
 // ---- forward, N = 2^13 .. 2^16: radix-16 passes, 16 residues per thread ----
 //
-// Same cluster layout (C = N/8192 CTAs of 8192 residues, 64 KiB of shared memory each), but every pass works
-// on 16-residue groups, so a thread holds 16 residues (not 32) at a time: 256 threads per CTA each take two
-// groups per pass, and with 64 registers a thread three CTAs share an SM (24 warps; 8-CTA clusters then also
-// pack a 19-SM GPC almost fully).  Passes (forward; the inverse runs them in reverse order):
+// Same cluster layout as above with a per-CTA share of E = 2^LOGE residues (LOGE = 13: C = N/8192 CTAs with 64 KiB
+// of shared memory each; LOGE = 12: twice the CTAs per limb with 32 KiB each, for small batches whose launch
+// latency matters more than throughput).  Every pass works on 16-residue groups, so a thread holds 16 residues
+// at a time: 256 threads per CTA each take E/4096 groups per pass, and with 80 registers a thread three CTAs
+// share an SM (24 warps; 8-CTA clusters then also pack a 19-SM GPC almost fully).  Passes:
 //   X : bits [LOGN-1 .. 12] (LOGX = LOGN - 12 bits; the top LOGC of them cross CTAs via distributed shared
-//       memory, bit 12 is inside the CTA) on columns l' in [0, 4096) of CTA c's share;
+//       memory, the rest (bit 12 when LOGE = 13) inside the CTA) on columns l' in [0, 4096) of CTA c's share;
 //   A : bits [11 .. 8]   (16 residues at stride 256),
 //   B : bits [7 .. 4]    (16 residues at stride 16),
 //   C : bits [3 .. 0]    (16 contiguous residues), then the store to HBM.
 // The profile of this kernel shows the ALU pipe (64-bit compares, selects and adds of the lazy reductions) as the
 // busiest unit; occupancy (16, 24 or 32 warps per SM) barely moves its time.
 constexpr int kThreads16 = 256;
-constexpr int kGroups16 = 512 / kThreads16;  // 16-residue groups per thread and pass
 
-template <int LOGN>
+template <int LOGN, int LOGE>
 struct Shape16 {
   static constexpr int N = 1 << LOGN;
-  static constexpr int E = 8192;
-  static constexpr int LOGC = LOGN - 13;
+  static constexpr int E = 1 << LOGE;
+  static constexpr int LOGC = LOGN - LOGE;
   static constexpr int C = 1 << LOGC;
   static constexpr int LOGX = LOGN - 12;
-  static constexpr int GX = (16 >> LOGX) * kGroups16;  // phase-X groups per thread
-  static constexpr int COLS = 4096 / C;                // phase-X columns per CTA
+  static constexpr int LOCAL = LOGE - 12;                  // phase-X bits inside the CTA (0 or 1)
+  static constexpr int COLS = 4096 / C;                    // phase-X columns per CTA
+  static constexpr int GX = COLS / kThreads16;             // phase-X groups per thread
+  static constexpr int GROUPS = E / 16;                    // 16-residue groups per pass
 };
 
-template <int LOGN>
+template <int LOGN, int LOGE>
 __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_constant__ NttBatch b,
                                                                  const __grid_constant__ DeviceTables T) {
-  using S = Shape16<LOGN>;
+  using S = Shape16<LOGN, LOGE>;
   extern __shared__ __align__(16) u64 sm[];
   const int tid = threadIdx.x;
   const LimbRef L = locate(b, S::N);
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
     asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
     h = (int)cg::this_cluster().block_rank();
   }
-  {  // phase X
+  {  // phase X: residue k*4096 + col lives in CTA k >> LOCAL at (k & local mask) * 4096 + col
     constexpr int R = 1 << S::LOGX;
 #pragma unroll 1
     for (int q = 0; q < S::GX; q++) {
@@ -352,8 +354,8 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
         cg::cluster_group cl = cg::this_cluster();
 #pragma unroll
         for (int k = 0; k < R; k++) {
-          u64* dst = cl.map_shared_rank(sm, k >> 1);
-          dst[swz((k & 1) * 4096 + col)] = x[k];
+          u64* dst = cl.map_shared_rank(sm, k >> S::LOCAL);
+          dst[swz((k & ((1 << S::LOCAL) - 1)) * 4096 + col)] = x[k];
         }
       } else {
 #pragma unroll
@@ -366,33 +368,33 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
       __syncthreads();
   }
 #pragma unroll 1
-  for (int g = tid; g < 512; g += kThreads16) {  // pass A
-    const int b12 = g >> 8, low = g & 255;
+  for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass A
+    const int hi = g >> 8, low = g & 255;
     u64 x[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) x[k] = sm[swz(b12 * 4096 + k * 256 + low)];
-    fwd_radix<4, 8, LOGN>(x, h * 2 + b12, tw, negp, p4);
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(hi * 4096 + k * 256 + low)];
+    fwd_radix<4, 8, LOGN>(x, h * (S::E / 4096) + hi, tw, negp, p4);
 #pragma unroll
-    for (int k = 0; k < 16; k++) sm[swz(b12 * 4096 + k * 256 + low)] = x[k];
+    for (int k = 0; k < 16; k++) sm[swz(hi * 4096 + k * 256 + low)] = x[k];
   }
   __syncthreads();
 #pragma unroll 1
-  for (int g = tid; g < 512; g += kThreads16) {  // pass B
+  for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass B
     const int low = g & 15, high = g >> 4;
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    fwd_radix<4, 4, LOGN>(x, h * 32 + high, tw, negp, p4);
+    fwd_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
   __syncthreads();
 #pragma unroll 1
-  for (int g = tid; g < 512; g += kThreads16) {  // pass C
+  for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass C
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
-    fwd_radix<4, 0, LOGN>(x, h * 512 + g, tw, negp, p4);
+    fwd_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p4);
     ulonglong2* out = reinterpret_cast<ulonglong2*>(L.dst + h * S::E + g * 16);
 #pragma unroll
     for (int k = 0; k < 16; k += 2) {
@@ -404,16 +406,97 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
   }
 }
 
-template <int LOGN>
-cudaError_t launch16_fwd(const NttBatch& b, const DeviceTables& t, cudaStream_t s) {
-  using S = Shape16<LOGN>;
-  auto kern = ntt16_fwd_kernel<LOGN>;
-  static bool attr_done = false;
+// Inverse of the same shape (Gentleman–Sande, passes C^-1, B^-1, A^-1, then the cross-CTA phase X^-1 reading
+// the peers' shared memory; N^-1 applied on the way out).  Used with LOGE = 12 for small batches.
+template <int LOGN, int LOGE>
+__global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_constant__ NttBatch b,
+                                                                 const __grid_constant__ DeviceTables T) {
+  using S = Shape16<LOGN, LOGE>;
+  extern __shared__ __align__(16) u64 sm[];
+  const int tid = threadIdx.x;
+  const LimbRef L = locate(b, S::N);
+  if (!L.valid) return;
+  const PrimeConst& pc = T.pc[L.prime];
+  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp, ninv = pc.ninv, ninv_sh = pc.ninv_sh;
+  const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
+  int h = 0;
+  if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
+#pragma unroll 1
+  for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass C^-1
+    u64 x[16];
+    const ulonglong2* in = reinterpret_cast<const ulonglong2*>(L.src + h * S::E + g * 16);
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+      const ulonglong2 v = __ldg(in + k / 2);
+      x[k] = v.x;
+      x[k + 1] = v.y;
+    }
+    inv_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p4);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(g * 16 + k)] = x[k];
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass B^-1
+    const int low = g & 15, high = g >> 4;
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
+    inv_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass A^-1
+    const int hi = g >> 8, low = g & 255;
+    u64 x[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) x[k] = sm[swz(hi * 4096 + k * 256 + low)];
+    inv_radix<4, 8, LOGN>(x, h * (S::E / 4096) + hi, tw, negp, p4);
+#pragma unroll
+    for (int k = 0; k < 16; k++) sm[swz(hi * 4096 + k * 256 + low)] = x[k];
+  }
+  {  // phase X^-1
+    constexpr int R = 1 << S::LOGX;
+    if constexpr (S::C > 1)
+      cg::this_cluster().sync();
+    else
+      __syncthreads();
+#pragma unroll 1
+    for (int q = 0; q < S::GX; q++) {
+      const int col = h * S::COLS + q * kThreads16 + tid;
+      u64 x[R];
+      if constexpr (S::C > 1) {
+        cg::cluster_group cl = cg::this_cluster();
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+          const u64* src = cl.map_shared_rank(sm, k >> S::LOCAL);
+          x[k] = src[swz((k & ((1 << S::LOCAL) - 1)) * 4096 + col)];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; k++) x[k] = sm[swz(k * 4096 + col)];
+      }
+      inv_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4);
+#pragma unroll
+      for (int k = 0; k < R; k++) L.dst[k * 4096 + col] = csub(csub(shoup_lazy4(x[k], ninv, ninv_sh, negp), p2), p);
+    }
+    if constexpr (S::C > 1) cg::this_cluster().sync();  // peers may still be reading this CTA's shared memory
+  }
+}
+
+template <int LOGN, int LOGE>
+cudaError_t launch16(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
+  using S = Shape16<LOGN, LOGE>;
+  auto kern = inverse ? ntt16_inv_kernel<LOGN, LOGE> : ntt16_fwd_kernel<LOGN, LOGE>;
+  static bool attr_done[2] = {false, false};
   const size_t smem = sizeof(u64) * S::E;
-  if (!attr_done) {
+  if (!attr_done[inverse]) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && S::C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    attr_done = true;
+    attr_done[inverse] = true;
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(S::C, b.limb_begin[b.njobs], 1);
@@ -468,27 +551,40 @@ cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, c
   if (b.njobs <= 0 || b.limb_begin[b.njobs] <= 0) return cudaSuccess;
   if (b.njobs > kMaxNttJobs || b.limb_begin[b.njobs] > 65535) return cudaErrorInvalidValue;
   const bool small = ((long long)b.limb_begin[b.njobs] << t.logN) <= kSmallNttWork;
-  const int v = small ? t.fwd_variant_small : t.fwd_variant;
+  const int v = inverse ? (small ? t.inv_variant_small : t.inv_variant) : (small ? t.fwd_variant_small : t.fwd_variant);
   switch (t.logN) {
     case 10: return launch_t<10>(b, t, inverse, s);
     case 11: return launch_t<11>(b, t, inverse, s);
     case 12: return launch_t<12>(b, t, inverse, s);
-    // forward: the variant tune_ntt picked (on GB300 the radix-16 one, 5% faster at N = 2^16); inverse: the
-    // radix-32/16 kernel (a radix-16 inverse of the same shape, pull or push exchange, was 3% slower)
-    case 13: return inverse || v ? launch_t<13>(b, t, inverse, s) : launch16_fwd<13>(b, t, s);
-    case 14: return inverse || v ? launch_t<14>(b, t, inverse, s) : launch16_fwd<14>(b, t, s);
-    case 15: return inverse || v ? launch_t<15>(b, t, inverse, s) : launch16_fwd<15>(b, t, s);
-    case 16: return inverse || v ? launch_t<16>(b, t, inverse, s) : launch16_fwd<16>(b, t, s);
+    // the variants tune_ntt picked for this direction and batch size (forward: 0 = radix-16 / 8192 per CTA,
+    // 1 = radix-32/16, 2 = radix-16 / 4096 per CTA; inverse: 0 = radix-32/16, 1 = radix-16 / 4096 per CTA)
+    case 13:
+      if (inverse) return v ? launch16<13, 12>(b, t, true, s) : launch_t<13>(b, t, true, s);
+      return v == 1 ? launch_t<13>(b, t, false, s) : v == 0 ? launch16<13, 13>(b, t, false, s)
+                                                           : launch16<13, 12>(b, t, false, s);
+    case 14:
+      if (inverse) return v ? launch16<14, 12>(b, t, true, s) : launch_t<14>(b, t, true, s);
+      return v == 1 ? launch_t<14>(b, t, false, s) : v == 0 ? launch16<14, 13>(b, t, false, s)
+                                                           : launch16<14, 12>(b, t, false, s);
+    case 15:
+      if (inverse) return v ? launch16<15, 12>(b, t, true, s) : launch_t<15>(b, t, true, s);
+      return v == 1 ? launch_t<15>(b, t, false, s) : v == 0 ? launch16<15, 13>(b, t, false, s)
+                                                           : launch16<15, 12>(b, t, false, s);
+    case 16:
+      if (inverse) return v ? launch16<16, 12>(b, t, true, s) : launch_t<16>(b, t, true, s);
+      return v == 1 ? launch_t<16>(b, t, false, s) : v == 0 ? launch16<16, 13>(b, t, false, s)
+                                                           : launch16<16, 12>(b, t, false, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
 cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
+  constexpr int kSlots = 2 * (kNttFwdVariants + kNttInvVariants);
   if (ms)
-    for (int i = 0; i < 4; i++) ms[i] = -1.f;
-  if (t.logN < 13) return cudaSuccess;  // one forward kernel below 2^13
+    for (int i = 0; i < kSlots; i++) ms[i] = -1.f;
+  if (t.logN < 13) return cudaSuccess;  // one kernel per direction below 2^13
   const size_t n = (size_t)1 << t.logN;
-  const int small = (int)((64ll << 16) >> t.logN), large = (int)((640ll << 16) >> t.logN);
+  const int small = (int)((32ll << 16) >> t.logN), large = (int)((640ll << 16) >> t.logN);
   u64* buf = nullptr;
   cudaError_t e = cudaMallocAsync(&buf, (size_t)large * n * sizeof(u64), s);
   if (e != cudaSuccess) return e;
@@ -496,30 +592,37 @@ cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
   cudaEvent_t ev[2];
   cudaEventCreate(&ev[0]);
   cudaEventCreate(&ev[1]);
-  for (int size = 0; size < 2 && e == cudaSuccess; size++) {
-    NttBatch b{};
-    uint8_t pm[1] = {0};
-    ntt_add_job(b, buf, buf, (long long)n, (long long)n, 1, size ? large : small, pm);
-    float best = 0;
-    int pick = 0;
-    for (int v = 0; v < 2 && e == cudaSuccess; v++) {
-      DeviceTables tv = t;
-      tv.fwd_variant = tv.fwd_variant_small = v;
-      e = launch_ntt(b, tv, false, s);  // warm-up
-      if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
-      for (int r = 0; r < 3 && e == cudaSuccess; r++) e = launch_ntt(b, tv, false, s);
-      if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
-      if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-      float el = 0;
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&el, ev[0], ev[1]);
-      el /= 3;
-      if (ms) ms[2 * size + v] = el;
-      if (v == 0 || el < best) {
-        best = el;
-        pick = v;
+  int slot = 0;  // ms layout: forward small, forward large, inverse small, inverse large
+  for (int inverse = 0; inverse < 2 && e == cudaSuccess; inverse++) {
+    const int nv = inverse ? kNttInvVariants : kNttFwdVariants;
+    for (int size = 0; size < 2 && e == cudaSuccess; size++) {
+      NttBatch b{};
+      uint8_t pm[1] = {0};
+      ntt_add_job(b, buf, buf, (long long)n, (long long)n, 1, size ? large : small, pm);
+      float best = 0;
+      int pick = 0;
+      for (int v = 0; v < nv && e == cudaSuccess; v++, slot++) {
+        DeviceTables tv = t;
+        tv.fwd_variant = tv.fwd_variant_small = tv.inv_variant = tv.inv_variant_small = v;
+        e = launch_ntt(b, tv, inverse, s);  // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+        for (int r = 0; r < 3 && e == cudaSuccess; r++) e = launch_ntt(b, tv, inverse, s);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+        float el = 0;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&el, ev[0], ev[1]);
+        el /= 3;
+        if (ms) ms[slot] = el;
+        if (v == 0 || el < best) {
+          best = el;
+          pick = v;
+        }
+      }
+      if (e == cudaSuccess) {
+        int& dst = inverse ? (size ? t.inv_variant : t.inv_variant_small) : (size ? t.fwd_variant : t.fwd_variant_small);
+        dst = pick;
       }
     }
-    if (e == cudaSuccess) (size ? t.fwd_variant : t.fwd_variant_small) = pick;
   }
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);

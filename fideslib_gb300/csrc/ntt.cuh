@@ -35,21 +35,27 @@ struct DeviceTables {
   const ulonglong2* tw_fwd;  // [ntowers][N] {psi^brev(i), shoup}
   const ulonglong2* tw_inv;  // [ntowers][N] {psi^-brev(i), shoup}
   int logN;
-  // forward kernel for N >= 2^13 (0 = radix-16, three CTAs/SM; 1 = radix-32/16), chosen by tune_ntt separately for
-  // launches of at most kSmallNttWork residues (latency-bound) and larger ones (throughput-bound)
+  // forward kernel for N >= 2^13 (0 = radix-16 with 8192 residues per CTA; 1 = radix-32/16; 2 = radix-16 with 4096
+  // residues per CTA, twice the CTAs per limb), chosen by tune_ntt separately for launches of at most
+  // kSmallNttWork residues (latency-bound) and larger ones (throughput-bound)
   int fwd_variant = 0;
   int fwd_variant_small = 0;
+  int inv_variant = 0;  // inverse: 0 = radix-32/16, 1 = radix-16 with 4096 residues per CTA
+  int inv_variant_small = 0;
 };
-constexpr long long kSmallNttWork = 256ll << 16;  // residues per launch (256 limbs at N = 2^16)
+constexpr int kNttFwdVariants = 3;
+constexpr int kNttInvVariants = 2;
+constexpr long long kSmallNttWork = 128ll << 16;  // residues per launch (128 limbs at N = 2^16)
 
 // Forward (inverse=false: coefficient -> evaluation, bit-reversed) or inverse transform of every job.
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s);
 
 // Autotuner: times the forward kernel variants on scratch batches of this ring (device memory from the
-// stream-ordered pool, synchronising `s`) — a small one (64 limbs' worth of residues at N = 2^16) and a large one
-// (640 limbs' worth) — and stores the faster variant of each in t.fwd_variant_small / t.fwd_variant.  The times
-// (ms: small v0, small v1, large v0, large v1) are written to ms[0..3] when ms is non-null (-1 where a single
-// kernel applies).
+// stream-ordered pool, synchronising `s`) — a small one (32 limbs' worth of residues at N = 2^16) and a large one
+// (640 limbs' worth) — for both directions, and stores the fastest variant of each in t.fwd_variant_small /
+// t.fwd_variant / t.inv_variant_small / t.inv_variant.  The times in ms (forward small v0..v2, forward large
+// v0..v2, inverse small v0..v1, inverse large v0..v1) are written to ms[0..9] when ms is non-null (-1 where a
+// single kernel applies).
 cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms);
 
 // Job owning flattened row `row` of a prefix-sum table begin[0..njobs] (uniform per block / cluster).

@@ -84,21 +84,23 @@ int fides_synchronize(fides_ctx* ctx);
  * LimbPartition / Stream (src/CudaUtils.cuh:98-160). */
 void* fides_ctx_stream(fides_ctx* ctx);
 int fides_ctx_set_stream(fides_ctx* ctx, void* stream);
-/* The NTT autotuner's choices for this ring (no counterpart in the reference, whose NTT kernel is fixed at build
- * time): at context creation both forward kernels are timed on a small and a large scratch batch (64 and 640
- * limbs' worth of residues at N = 2^16) and the faster one of each size is used for launches of at most / more
- * than 256 limbs' worth.  fwd_variant[0] (small), [1] (large): 0 = radix-16 passes (three CTAs per SM),
- * 1 = radix-32/16 passes; ms[0..3] = small v0, small v1, large v0, large v1 in ms (-1 where a single kernel
- * applies, N < 2^13). */
-int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* fwd_variant, float* ms);
+/* The NTT autotuner's choices for this ring (no counterpart in the reference, whose NTT kernels are fixed at build
+ * time): at context creation every forward and inverse kernel variant is timed on a small and a large scratch
+ * batch (32 and 640 limbs' worth of residues at N = 2^16) and the fastest one of each is used for launches of at
+ * most / more than 128 limbs' worth (the key-switch stages of single ops / of batches).  variant[0..3] = forward
+ * small, forward large, inverse small, inverse large; forward variants: 0 = radix-16 passes with 8192 residues
+ * per CTA, 1 = radix-32/16 passes, 2 = radix-16 passes with 4096 residues per CTA (twice the CTAs per limb);
+ * inverse: 0 = radix-32/16, 1 = radix-16 with 4096 per CTA.  ms[0..9] = forward small v0..v2, forward large
+ * v0..v2, inverse small v0..v1, inverse large v0..v1 (-1 where a single kernel applies, N < 2^13). */
+int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms);
 /* Device-memory budget of the context (the reference's pool has a release threshold only, Context.cu:74-80):
  * ciphertexts and per-op workspaces come from the stream-ordered pool and are counted; an op whose allocation
  * would exceed `bytes` fails with FIDES_ENOMEM and leaves the context usable (0 = no limit; keys, plaintexts and
  * transforms are not counted).  fides_ctx_mem_in_use reports the bytes currently counted. */
 int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes);
 int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes);
-/* Overrides the autotuner's choices (both variants give identical residues). */
-int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant);
+/* Overrides the autotuner's choices for every batch size (all variants give identical residues). */
+int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant, int32_t inv_variant);
 /* Ring and basis shape of a context. */
 typedef struct {
   uint32_t n, log_n, nq, np, dnum, alpha;

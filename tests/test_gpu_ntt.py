@@ -79,20 +79,40 @@ def test_batched_ntt_full_size_config(engine_lib):
 
 
 @pytest.mark.parametrize("logN", [13, 14, 15, 16])
-def test_both_forward_variants_and_autotuner(engine_lib, logN):
-    """The autotuner picked one of the two forward kernels with both timed; each variant, forced, gives the
-    oracle's residues (edge values included)."""
+def test_all_ntt_variants_and_autotuner(engine_lib, logN):
+    """The autotuner picked one kernel per direction and batch size with all of them timed; each variant,
+    forced, gives the oracle's residues (edge values included) and inverts exactly."""
     N = 1 << logN
     ctx, mods = make_ctx(logN, 2, bits=60)
     tune = ctx.ntt_tuning()
-    assert tune["fwd_variant_small"] in (0, 1) and tune["fwd_variant_large"] in (0, 1)
-    assert min(tune["ms_small_v0_v1"] + tune["ms_large_v0_v1"]) > 0
+    assert tune["fwd_variant_small"] in (0, 1, 2) and tune["fwd_variant_large"] in (0, 1, 2)
+    assert tune["inv_variant_small"] in (0, 1) and tune["inv_variant_large"] in (0, 1)
+    assert min(tune["fwd_ms_small"] + tune["fwd_ms_large"] + tune["inv_ms_small"] + tune["inv_ms_large"]) > 0
     rng = np.random.default_rng(logN + 100)
     data = np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(2)])[None]
     data[0, 0, :7] = mods[0] - 1
-    for v in (0, 1):
-        ctx.set_ntt_variant(v)
+    for v in (0, 1, 2):
+        ctx.set_ntt_variant(v, v % 2)
         fwd = ctx.ntt_host(data.copy(), 0, inverse=False)
         for j in range(2):
             tab, _ = O.ntt_tables(N, mods[j], ctx.roots[j])
             assert np.array_equal(fwd[0, j], O.ntt_fwd(data[0, j], mods[j], tab)), (logN, v, j)
+        assert np.array_equal(ctx.ntt_host(fwd.copy(), 0, inverse=True), data), (logN, v)
+
+
+@pytest.mark.parametrize("logN", [12, 16])
+def test_forward_ntt_accepts_lazy_inputs(engine_lib, logN):
+    """The basis conversions hand the forward NTT residues in [0, 8p) (unreduced): the transform of x + k p,
+    k < 8, equals the transform of x, for every kernel variant."""
+    N = 1 << logN
+    ctx, mods = make_ctx(logN, 2, bits=60)
+    rng = np.random.default_rng(logN + 7)
+    x = np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(2)])[None]
+    lazy = x.copy()
+    for j in range(2):
+        k = rng.integers(0, 8, N, dtype=np.uint64)
+        lazy[0, j] = x[0, j] + k * np.uint64(mods[j])
+    assert lazy.max() >= max(mods[:2])
+    for v in ((0, 1, 2) if logN >= 13 else (1,)):
+        ctx.set_ntt_variant(v, 0)
+        assert np.array_equal(ctx.ntt_host(lazy.copy(), 0, inverse=False), ctx.ntt_host(x.copy(), 0, inverse=False))
