@@ -38,6 +38,17 @@ METRIC = "HRotate/HMult ops/s at N=2^16 (served vs per-op), p50/p99 latency, NTT
 E2E_CHUNK = 8  # requests per pipelined chunk of the host-memory path
 
 
+def max_over_ranks(dist, value: float, device) -> float:
+    """Replicas run independent copies of the workload: the job's step time is its slowest rank's (None = one
+    process).  Every rank gets the maximum."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def hrotate_bytes(t: int) -> int:
     beta = (t + ALPHA - 1) // ALPHA
     return (2 * t + 2 * beta * (t + NP) + 2 * t) * S_BYTES
@@ -221,11 +232,8 @@ def run_ours(args, rank, world, dist):
         e1.record(stream)
         torch.cuda.synchronize()
         launches = F.kernel_launches() - l0
-        ms = e0.elapsed_time(e1) / steps
+        ms = max_over_ranks(dist, e0.elapsed_time(e1) / steps, dev)
         if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
             dist.barrier()
         return ms, launches
 
@@ -277,11 +285,7 @@ def run_ours(args, rank, world, dist):
     for _ in range(e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / e2e_steps, dev)
 
     # HMult + relinearisation + Rescale on the same 64 ragged-level ciphertexts (each squared against a second
     # ciphertext of its level), batched and per op
