@@ -244,7 +244,8 @@ def run_ours(args, rank, world, dist):
         l0 = F.kernel_launches()
         step_batched()
         torch.cuda.synchronize()
-        return {"profile_step": True, "warmup": args.warmup, "launches_per_step": F.kernel_launches() - l0}
+        return {"profile_step": True, "warmup": args.warmup, "launches_before_step": l0,
+                "launches_per_step": F.kernel_launches() - l0}
 
     per_op_ms, _ = timed(step_per_op, args.steps)
     with Clocks(dev.index) as clk:

@@ -87,6 +87,8 @@ _SIGS = {
     "fides_eval_mult_int": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int64, u32p]),
     "fides_eval_mult_scalar": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, C.c_double, u32p]),
     "fides_eval_add_scalar": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, u32p]),
+    "fides_eval_many_to_one": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, u32p, u32p,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double), u32p]),
     "fides_level_reduce": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_mod_raise": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_lt_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, u64p, C.POINTER(C.c_uint8),
@@ -132,6 +134,7 @@ _SIGS = {
 }
 
 OP_ADD, OP_SUB, OP_MULT, OP_SQUARE, OP_RESCALE, OP_ROTATE, OP_AUTOMORPHISM, OP_KEY_SWITCH, OP_BOOTSTRAP = range(1, 10)
+OP_MULT_PLAIN, OP_ADD_PLAIN, OP_SUB_PLAIN, OP_MULT_SCALAR, OP_ADD_SCALAR, OP_MULT_INT = range(10, 16)
 
 
 class HostOp(C.Structure):
@@ -356,6 +359,27 @@ class CryptoContext:
 
     def eval_add_scalar(self, a: int, v: float) -> int:
         return self._un(lib().fides_eval_add_scalar, a, v)
+
+    def eval_many_to_one(self, op: int, a, b=None, values=None, scales=None, stride: int = 1,
+                         in_place: bool = False):
+        """Many-to-one batch (fides_eval_many_to_one): a[i*stride + j] combined with operand i (b[i], or
+        values[i] / scales[i] for the scalar ops).  Returns the result handles, or None when in place."""
+        a_arr = np.ascontiguousarray(np.array(a, dtype=np.uint32))
+        nb = len(a_arr) // stride
+        assert nb * stride == len(a_arr)
+        u32 = C.POINTER(C.c_uint32)
+        f64 = C.POINTER(C.c_double)
+        b_arr = None if b is None else np.ascontiguousarray(np.array(b, dtype=np.uint32))
+        v_arr = None if values is None else np.ascontiguousarray(np.array(values, dtype=np.float64))
+        s_arr = None if scales is None else np.ascontiguousarray(np.array(scales, dtype=np.float64))
+        outs = None if in_place else np.zeros(len(a_arr), dtype=np.uint32)
+
+        def ptr(x, t):
+            return None if x is None else x.ctypes.data_as(t)
+
+        _check(lib().fides_eval_many_to_one(self._h, op, nb, stride, ptr(a_arr, u32), ptr(b_arr, u32),
+                                            ptr(v_arr, f64), ptr(s_arr, f64), ptr(outs, u32)))
+        return None if in_place else [int(x) for x in outs]
 
     def level_reduce(self, a: int, towers: int) -> int:
         return self._un(lib().fides_level_reduce, a, towers)

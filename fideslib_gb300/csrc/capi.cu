@@ -1,4 +1,5 @@
 // extern "C" boundary of the engine (declarations and contract: include/fideslib_gb300.h).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -32,6 +33,11 @@ int cuda_fail(cudaError_t e, const char* where) {
 fgb::DevCt* find_ct(fides_ctx* ctx, uint32_t h) {
   auto it = ctx->c->cts.find(h);
   return it == ctx->c->cts.end() ? nullptr : &it->second;
+}
+
+fgb::DevPt* find_pt(fides_ctx* ctx, uint32_t h) {
+  auto it = ctx->c->pts.find(h);
+  return it == ctx->c->pts.end() ? nullptr : &it->second;
 }
 
 uint32_t register_ct(fides_ctx* ctx, const fgb::DevCt& ct) {
@@ -361,11 +367,25 @@ int fides_ct_free(fides_ctx* ctx, uint32_t handle) {
   return FIDES_OK;
 }
 
+// Plaintext jobs, kMaxJobs per launch.
+static cudaError_t launch_plain_jobs(fgb::Context* c, const fgb::PtJob* jobs, size_t n) {
+  const fgb::Ring ring{c->N, c->logN};
+  for (size_t k0 = 0; k0 < n; k0 += fgb::kMaxJobs) {
+    fgb::PtBatch pb{};
+    pb.njobs = (int)std::min(n - k0, (size_t)fgb::kMaxJobs);
+    for (int k = 0; k < pb.njobs; k++) pb.jobs[k] = jobs[k0 + k];
+    const cudaError_t e = fgb::launch_ptop(pb, ring, c->d_pc, c->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // Validates one request and prepares its output ciphertext; the compute is issued by run_batch.
 struct Pending {
   fgb::DevCt out;
   const fgb::DevCt* a = nullptr;
   const fgb::DevCt* b = nullptr;
+  const fgb::DevPt* pt = nullptr;  // *_PLAIN requests
   uint32_t galois_inv = 1;  // automorphism applied after the key switch (1 = none)
   const fgb::u64* key = nullptr;
 };
@@ -379,6 +399,12 @@ static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
     B = find_ct(ctx, op.b);
     if (!B) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(op.b));
     if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
+  }
+  const bool plain = op.op == FIDES_OP_MULT_PLAIN || op.op == FIDES_OP_ADD_PLAIN || op.op == FIDES_OP_SUB_PLAIN;
+  if (plain) {
+    pd->pt = find_pt(ctx, op.b);
+    if (!pd->pt) return fail(FIDES_EINVAL, "unknown plaintext handle " + std::to_string(op.b));
+    if (pd->pt->t < A->t) return fail(FIDES_EINVAL, "plaintext has fewer towers than the ciphertext");
   }
   pd->a = A;
   pd->b = B;
@@ -399,6 +425,13 @@ static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
       pd->b = Y;
       break;
     }
+    case FIDES_OP_MULT_PLAIN:
+      meta.scale = A->scale * pd->pt->scale;
+      meta.noise_deg = A->noise_deg + 1;
+      break;
+    case FIDES_OP_ADD_PLAIN:
+    case FIDES_OP_SUB_PLAIN:
+      break;
     case FIDES_OP_RESCALE:
       if (A->t < 2) return fail(FIDES_EINVAL, "cannot rescale a ciphertext with one tower");
       t_out = A->t - 1;
@@ -448,6 +481,7 @@ static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
   std::vector<fgb::Context::MultReq> mults;
   std::vector<fgb::Context::RescaleReq> rescales;
   std::vector<fgb::Context::KsReq> rots;
+  std::vector<fgb::PtJob> ptops;
   const size_t NN = (size_t)c->N;
   for (uint32_t i = 0; i < n; i++) {
     const Pending& p = pd[i];
@@ -464,11 +498,17 @@ static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
       case FIDES_OP_RESCALE:
         rescales.push_back({p.a->data, t, p.out.data});
         break;
+      case FIDES_OP_MULT_PLAIN:
+      case FIDES_OP_ADD_PLAIN:
+      case FIDES_OP_SUB_PLAIN:
+        ptops.push_back({p.a->data, p.pt->data, p.out.data, t, ops[i].op - FIDES_OP_MULT_PLAIN});
+        break;
       default:
         rots.push_back({p.a->data + (size_t)t * NN, t, p.key, p.a->data, nullptr, p.out.data, p.galois_inv});
     }
   }
   cudaError_t e = c->add_batch(adds.data(), (int)adds.size(), c->stream);
+  if (e == cudaSuccess) e = launch_plain_jobs(c, ptops.data(), ptops.size());
   if (e == cudaSuccess) e = c->rescale_batch(rescales.data(), (int)rescales.size(), c->stream);
   if (e == cudaSuccess) e = c->mult_batch(mults.data(), (int)mults.size(), c->relin_key, c->stream);
   if (e == cudaSuccess) e = c->keyswitch_batch(rots.data(), (int)rots.size(), c->stream);
@@ -494,6 +534,8 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
     const bool binary = o.op == FIDES_OP_ADD || o.op == FIDES_OP_SUB || o.op == FIDES_OP_MULT;
     if (!o.a || !o.out || (binary && !o.b)) return fail(FIDES_EINVAL, "null host buffer in request " + std::to_string(i));
     if (o.op == FIDES_OP_BOOTSTRAP) return fail(FIDES_EINVAL, "bootstrap requests go through the server");
+    if (o.op >= FIDES_OP_MULT_PLAIN && o.op <= FIDES_OP_SUB_PLAIN)
+      return fail(FIDES_EINVAL, "plaintext requests take resident plaintext handles: use fides_eval_batch");
     if (o.meta.towers < 1 || o.meta.towers > (uint32_t)c->nq) return fail(FIDES_EINVAL, "towers out of range");
   }
   if (!c->copy_in) CK(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking), "copy stream");
@@ -704,31 +746,58 @@ uint64_t double_residue(double v, uint64_t q) {
 
 uint64_t shoup_const(uint64_t w, uint64_t q) { return (uint64_t)(((unsigned __int128)w << 64) / q); }
 
-fgb::DevPt* find_pt(fides_ctx* ctx, uint32_t h) {
-  auto it = ctx->c->pts.find(h);
-  return it == ctx->c->pts.end() ? nullptr : &it->second;
+// One scalar constant set: residues of round(mul_v) (or of the integer k when `integer`) and round(add_v).
+void make_set(fgb::Context* c, double mul_v, double add_v, bool integer, int64_t k, fgb::ScalarSet* set) {
+  for (int j = 0; j < c->nq; j++) {
+    const uint64_t q = c->mod[j];
+    uint64_t m = double_residue(mul_v, q);
+    if (integer && (k > (1ll << 52) || k < -(1ll << 52))) {
+      const uint64_t r = (uint64_t)(k < 0 ? -(k + 1) : k) % q;
+      m = k < 0 ? (q - 1 - r) % q : r;
+    }
+    set->mul[j] = m;
+    set->mul_sh[j] = shoup_const(m, q);
+    set->add[j] = add_v == 0.0 ? 0 : double_residue(add_v, q);
+  }
 }
 
-int scalar_op(fides_ctx* ctx, uint32_t a, const uint64_t* mul, const uint64_t* addv, fgb::DevCt meta, uint32_t* out) {
+// Scalar jobs in launches of up to kMaxJobs jobs and kMaxScalarSets constant sets; consecutive jobs with the same
+// set index (into `sets`) share one copy of it.
+cudaError_t launch_scalar_jobs(fgb::Context* c, const fgb::ScalarJob* jobs, const fgb::ScalarSet* sets, size_t n) {
+  const fgb::Ring ring{c->N, c->logN};
+  fgb::ScalarBatch sb{};
+  int nsets = 0, last = -1;  // sets copied into sb; source index of the last one
+  auto flush = [&]() {
+    const cudaError_t e = sb.njobs ? fgb::launch_scalar(sb, ring, c->d_pc, c->stream) : cudaSuccess;
+    sb.njobs = 0;
+    nsets = 0;
+    last = -1;
+    return e;
+  };
+  for (size_t k = 0; k < n; k++) {
+    if (sb.njobs == fgb::kMaxJobs || (jobs[k].set != last && nsets == fgb::kMaxScalarSets)) {
+      const cudaError_t e = flush();
+      if (e != cudaSuccess) return e;
+    }
+    if (jobs[k].set != last) {
+      sb.sets[nsets++] = sets[jobs[k].set];
+      last = jobs[k].set;
+    }
+    sb.jobs[sb.njobs] = jobs[k];
+    sb.jobs[sb.njobs++].set = nsets - 1;
+  }
+  return flush();
+}
+
+int scalar_op(fides_ctx* ctx, uint32_t a, const fgb::ScalarSet& set, fgb::DevCt meta, uint32_t* out) {
   fgb::Context* c = ctx->c;
   fgb::DevCt* A = find_ct(ctx, a);
   if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
   fgb::DevCt r;
   int rc = new_ct(ctx, A->t, meta, &r);
   if (rc) return rc;
-  fgb::ScalarBatch sb{};
-  fgb::ScalarJob& j = sb.jobs[0];
-  j.ct = A->data;
-  j.out = r.data;
-  j.t = A->t;
-  for (int k = 0; k < A->t; k++) {
-    j.mul[k] = mul[k];
-    j.mul_sh[k] = shoup_const(mul[k], c->mod[k]);
-    j.add[k] = addv[k];
-  }
-  sb.njobs = 1;
-  const fgb::Ring ring{c->N, c->logN};
-  CK(fgb::launch_scalar(sb, ring, c->d_pc, c->stream), "scalar op");
+  const fgb::ScalarJob job{A->data, r.data, A->t, 0};
+  CK(launch_scalar_jobs(c, &job, &set, 1), "scalar op");
   *out = register_ct(ctx, r);
   return FIDES_OK;
 }
@@ -772,71 +841,134 @@ int fides_pt_free(fides_ctx* ctx, uint32_t handle) {
   return FIDES_OK;
 }
 
-static int plain_op(fides_ctx* ctx, uint32_t a, uint32_t pt, int mode, uint32_t* out) {
-  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
-  fgb::Context* c = ctx->c;
-  fgb::DevCt* A = find_ct(ctx, a);
-  fgb::DevPt* P = find_pt(ctx, pt);
-  if (!A || !P) return fail(FIDES_EINVAL, "unknown ciphertext or plaintext handle");
-  if (P->t < A->t) return fail(FIDES_EINVAL, "plaintext has fewer towers than the ciphertext");
-  fgb::DevCt meta = *A;
-  if (mode == 0) {
-    meta.scale = A->scale * P->scale;
-    meta.noise_deg = A->noise_deg + 1;
-  }
-  fgb::DevCt r;
-  int rc = new_ct(ctx, A->t, meta, &r);
-  if (rc) return rc;
-  fgb::PtBatch pb{};
-  pb.jobs[0] = fgb::PtJob{A->data, P->data, r.data, A->t, mode};
-  pb.njobs = 1;
-  const fgb::Ring ring{c->N, c->logN};
-  CK(fgb::launch_ptop(pb, ring, c->d_pc, c->stream), "plaintext op");
-  *out = register_ct(ctx, r);
-  return FIDES_OK;
+int fides_eval_mult_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) {
+  return one(ctx, FIDES_OP_MULT_PLAIN, a, pt, 0, out);
 }
-
-int fides_eval_mult_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) { return plain_op(ctx, a, pt, 0, out); }
-int fides_eval_add_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) { return plain_op(ctx, a, pt, 1, out); }
-int fides_eval_sub_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) { return plain_op(ctx, a, pt, 2, out); }
+int fides_eval_add_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) {
+  return one(ctx, FIDES_OP_ADD_PLAIN, a, pt, 0, out);
+}
+int fides_eval_sub_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) {
+  return one(ctx, FIDES_OP_SUB_PLAIN, a, pt, 0, out);
+}
 
 int fides_eval_mult_int(fides_ctx* ctx, uint32_t a, int64_t k, uint32_t* out) {
   if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
   fgb::DevCt* A = find_ct(ctx, a);
   if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  uint64_t mul[64], addv[64] = {0};
-  for (int j = 0; j < A->t; j++) mul[j] = double_residue((double)k, ctx->c->mod[j]);
-  if (k > (1ll << 52) || k < -(1ll << 52))
-    for (int j = 0; j < A->t; j++) {
-      const uint64_t q = ctx->c->mod[j];
-      const uint64_t m = (uint64_t)(k < 0 ? -(k + 1) : k) % q;
-      mul[j] = k < 0 ? (q - 1 - m) % q : m;
-    }
-  return scalar_op(ctx, a, mul, addv, *A, out);
+  fgb::ScalarSet set;
+  make_set(ctx->c, (double)k, 0.0, true, k, &set);
+  return scalar_op(ctx, a, set, *A, out);
 }
 
 int fides_eval_mult_scalar(fides_ctx* ctx, uint32_t a, double v, double scale, uint32_t* out) {
   if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
-  fgb::DevCt* A = find_ct(ctx, a);
-  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  uint64_t mul[64], addv[64] = {0};
-  for (int j = 0; j < A->t; j++) mul[j] = double_residue(v * scale, ctx->c->mod[j]);
-  fgb::DevCt meta = *A;
-  meta.scale = A->scale * scale;
-  meta.noise_deg = A->noise_deg + 1;
-  return scalar_op(ctx, a, mul, addv, meta, out);
+  return fides_eval_many_to_one(ctx, FIDES_OP_MULT_SCALAR, 1, 1, &a, nullptr, &v, &scale, out);
 }
 
 int fides_eval_add_scalar(fides_ctx* ctx, uint32_t a, double v, uint32_t* out) {
   if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
-  fgb::DevCt* A = find_ct(ctx, a);
-  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  uint64_t mul[64], addv[64];
-  for (int j = 0; j < A->t; j++) {
-    mul[j] = 1;
-    addv[j] = double_residue(v * A->scale, ctx->c->mod[j]);
+  return fides_eval_many_to_one(ctx, FIDES_OP_ADD_SCALAR, 1, 1, &a, nullptr, &v, nullptr, out);
+}
+
+int fides_eval_many_to_one(fides_ctx* ctx, int32_t op, uint32_t nb, uint32_t stride, const uint32_t* a,
+                           const uint32_t* b, const double* values, const double* scales, uint32_t* outs) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  const size_t n = (size_t)nb * stride;
+  if (n == 0) return FIDES_OK;
+  const bool cts = op == FIDES_OP_ADD || op == FIDES_OP_SUB;
+  const bool pts = op == FIDES_OP_MULT_PLAIN || op == FIDES_OP_ADD_PLAIN || op == FIDES_OP_SUB_PLAIN;
+  const bool scalar = op == FIDES_OP_MULT_SCALAR || op == FIDES_OP_ADD_SCALAR || op == FIDES_OP_MULT_INT;
+  if (!cts && !pts && !scalar) return fail(FIDES_EINVAL, "op code " + std::to_string(op) + " has no many-to-one form");
+  if (!a || ((cts || pts) && !b) || (scalar && !values) || (op == FIDES_OP_MULT_SCALAR && !scales))
+    return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  const bool in_place = outs == nullptr;
+  std::vector<fgb::DevCt*> A(n);
+  for (size_t k = 0; k < n; k++)
+    if (!(A[k] = find_ct(ctx, a[k]))) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(a[k]));
+  if (in_place) {
+    std::vector<uint32_t> sorted(a, a + n);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return fail(FIDES_EINVAL, "a ciphertext appears twice in an in-place many-to-one op");
+    if (cts)
+      for (uint32_t i = 0; i < nb; i++)
+        if (std::binary_search(sorted.begin(), sorted.end(), b[i]))
+          return fail(FIDES_EINVAL, "an in-place many-to-one op cannot read one of the ciphertexts it writes");
   }
-  return scalar_op(ctx, a, mul, addv, *A, out);
+  // Validate the operands and work out the result metadata.
+  std::vector<fgb::DevCt> R(n);
+  std::vector<const fgb::DevCt*> B(cts ? nb : 0);
+  std::vector<const fgb::DevPt*> P(pts ? nb : 0);
+  for (uint32_t i = 0; i < nb; i++) {
+    if (cts && !(B[i] = find_ct(ctx, b[i]))) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(b[i]));
+    if (pts && !(P[i] = find_pt(ctx, b[i]))) return fail(FIDES_EINVAL, "unknown plaintext handle " + std::to_string(b[i]));
+    if (op == FIDES_OP_MULT_INT && (values[i] != std::nearbyint(values[i]) || std::fabs(values[i]) >= 9007199254740992.0))
+      return fail(FIDES_EINVAL, "MULT_INT values must be integers below 2^53 in magnitude");
+    for (uint32_t j = 0; j < stride; j++) {
+      const size_t k = (size_t)i * stride + j;
+      fgb::DevCt m = *A[k];
+      if (cts) {
+        if (B[i]->t != m.t) return fail(FIDES_EINVAL, "operands have different tower counts");
+        m.noise_deg = std::max(m.noise_deg, B[i]->noise_deg);
+      }
+      if (pts && P[i]->t < m.t) return fail(FIDES_EINVAL, "plaintext has fewer towers than the ciphertext");
+      if (op == FIDES_OP_MULT_PLAIN || op == FIDES_OP_MULT_SCALAR) {
+        m.scale *= op == FIDES_OP_MULT_PLAIN ? P[i]->scale : scales[i];
+        m.noise_deg += 1;
+      }
+      R[k] = m;
+    }
+  }
+  if (!in_place)
+    for (size_t k = 0; k < n; k++) {
+      R[k].data = c->alloc_limbs((size_t)2 * R[k].t, c->stream);
+      if (!R[k].data) {
+        for (size_t q = 0; q < k; q++) c->free_limbs(R[q].data, c->stream);
+        return fail(FIDES_ENOMEM, "ciphertext allocation failed");
+      }
+    }
+  cudaError_t e = cudaSuccess;
+  if (cts) {
+    std::vector<fgb::Context::AddReq> adds(n);
+    for (size_t k = 0; k < n; k++)
+      adds[k] = {A[k]->data, B[k / stride]->data, A[k]->t, R[k].data, op == FIDES_OP_SUB};
+    e = c->add_batch(adds.data(), (int)n, c->stream);
+  } else if (pts) {
+    std::vector<fgb::PtJob> jobs(n);
+    for (size_t k = 0; k < n; k++)
+      jobs[k] = fgb::PtJob{A[k]->data, P[k / stride]->data, R[k].data, A[k]->t, op - FIDES_OP_MULT_PLAIN};
+    e = launch_plain_jobs(c, jobs.data(), n);
+  } else {
+    // One constant set per group, or per (group, ciphertext scale) for ADD_SCALAR, whose constant is
+    // round(v * scale of the ciphertext).
+    std::vector<fgb::ScalarSet> sets;
+    std::vector<fgb::ScalarJob> jobs(n);
+    double last_scale = 0.0;
+    for (size_t k = 0; k < n; k++) {
+      const uint32_t i = (uint32_t)(k / stride);
+      const bool first = k % stride == 0;
+      if (first || (op == FIDES_OP_ADD_SCALAR && A[k]->scale != last_scale)) {
+        sets.emplace_back();
+        if (op == FIDES_OP_MULT_SCALAR) make_set(c, values[i] * scales[i], 0.0, false, 0, &sets.back());
+        else if (op == FIDES_OP_MULT_INT) make_set(c, values[i], 0.0, true, (int64_t)values[i], &sets.back());
+        else make_set(c, 1.0, values[i] * A[k]->scale, false, 0, &sets.back());
+        last_scale = A[k]->scale;
+      }
+      jobs[k] = fgb::ScalarJob{A[k]->data, R[k].data, A[k]->t, (int)sets.size() - 1};
+    }
+    e = launch_scalar_jobs(c, jobs.data(), sets.data(), n);
+  }
+  if (e != cudaSuccess) {
+    if (!in_place)
+      for (size_t k = 0; k < n; k++) c->free_limbs(R[k].data, c->stream);
+    return cuda_fail(e, "many-to-one op");
+  }
+  for (size_t k = 0; k < n; k++) {
+    if (in_place) *A[k] = R[k];
+    else outs[k] = register_ct(ctx, R[k]);
+  }
+  return FIDES_OK;
 }
 
 int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out) {

@@ -275,16 +275,23 @@ __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ Tens
   J.d[2 * P + o] = mul_mod(x1, y1, c);
 }
 
+// Element-wise kernels move two coefficients per thread (16-byte accesses); grid.x = N / (2 kT).
+__device__ __forceinline__ ulonglong2 ld2(const u64* p) { return *reinterpret_cast<const ulonglong2*>(p); }
+__device__ __forceinline__ void st2(u64* p, ulonglong2 v) { *reinterpret_cast<ulonglong2*>(p) = v; }
+
 __global__ void __launch_bounds__(kT) addsub_kernel(const __grid_constant__ AddBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const AddJob& J = b.jobs[z];
   const int j = (int)blockIdx.y - b.row_begin[z];
   const u64 p = pc[j].p;
+  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
 #pragma unroll
   for (int poly = 0; poly < 2; poly++) {
-    const size_t o = ((size_t)poly * J.t + j) * r.N + blockIdx.x * kT + threadIdx.x;
-    J.out[o] = J.sub ? sub_mod(J.x[o], J.y[o], p) : add_mod(J.x[o], J.y[o], p);
+    const size_t o = ((size_t)poly * J.t + j) * r.N + n;
+    const ulonglong2 x = ld2(J.x + o), y = ld2(J.y + o);
+    st2(J.out + o, J.sub ? make_ulonglong2(sub_mod(x.x, y.x, p), sub_mod(x.y, y.y, p))
+                         : make_ulonglong2(add_mod(x.x, y.x, p), add_mod(x.y, y.y, p)));
   }
 }
 
@@ -326,16 +333,18 @@ __global__ void __launch_bounds__(kT) ptop_kernel(const __grid_constant__ PtBatc
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const PtJob& J = b.jobs[z];
   const int j = (int)blockIdx.y - b.row_begin[z];
-  const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
+  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
   const size_t o0 = (size_t)j * r.N + n, o1 = ((size_t)J.t + j) * r.N + n;
   const PrimeConst& c = pc[j];
-  const u64 w = J.pt[(size_t)j * r.N + n];
+  const ulonglong2 w = ld2(J.pt + (size_t)j * r.N + n);
+  const ulonglong2 x0 = ld2(J.ct + o0), x1 = ld2(J.ct + o1);
   if (J.mode == 0) {
-    J.out[o0] = mul_mod(J.ct[o0], w, c);
-    J.out[o1] = mul_mod(J.ct[o1], w, c);
+    st2(J.out + o0, make_ulonglong2(mul_mod(x0.x, w.x, c), mul_mod(x0.y, w.y, c)));
+    st2(J.out + o1, make_ulonglong2(mul_mod(x1.x, w.x, c), mul_mod(x1.y, w.y, c)));
   } else {
-    J.out[o0] = J.mode == 1 ? add_mod(J.ct[o0], w, c.p) : sub_mod(J.ct[o0], w, c.p);
-    J.out[o1] = J.ct[o1];
+    st2(J.out + o0, J.mode == 1 ? make_ulonglong2(add_mod(x0.x, w.x, c.p), add_mod(x0.y, w.y, c.p))
+                                : make_ulonglong2(sub_mod(x0.x, w.x, c.p), sub_mod(x0.y, w.y, c.p)));
+    st2(J.out + o1, x1);
   }
 }
 
@@ -343,12 +352,14 @@ __global__ void __launch_bounds__(kT) scalar_kernel(const __grid_constant__ Scal
                                                     const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const ScalarJob& J = b.jobs[z];
+  const ScalarSet& S = b.sets[J.set];
   const int j = (int)blockIdx.y - b.row_begin[z];
-  const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
-  const u64 q = pc[j].p, w = J.mul[j], wsh = J.mul_sh[j];
+  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
+  const u64 q = pc[j].p, w = S.mul[j], wsh = S.mul_sh[j], a = S.add[j];
   const size_t o0 = (size_t)j * r.N + n, o1 = ((size_t)J.t + j) * r.N + n;
-  J.out[o0] = add_mod(shoup(J.ct[o0], w, wsh, q), J.add[j], q);
-  J.out[o1] = shoup(J.ct[o1], w, wsh, q);
+  const ulonglong2 x0 = ld2(J.ct + o0), x1 = ld2(J.ct + o1);
+  st2(J.out + o0, make_ulonglong2(add_mod(shoup(x0.x, w, wsh, q), a, q), add_mod(shoup(x0.y, w, wsh, q), a, q)));
+  st2(J.out + o1, make_ulonglong2(shoup(x1.x, w, wsh, q), shoup(x1.y, w, wsh, q)));
 }
 
 // grid rows per job: 2*t (poly-major).  X^k at point psi^(2 brev(i) + 1) is psi^e, e = (2 brev(i) + 1) k mod 2N;
@@ -542,7 +553,7 @@ cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeC
   if (b.njobs <= 0) return cudaSuccess;
   AddBatch bb;
   const int rows = with_rows(b, bb, [](const AddJob& j) { return j.t; });
-  dim3 grid(r.N / kT, rows, 1);
+  dim3 grid(r.N / (2 * kT), rows, 1);
   addsub_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
@@ -576,7 +587,7 @@ cudaError_t launch_ptop(const PtBatch& b, const Ring& r, const PrimeConst* pc, c
   if (b.njobs <= 0) return cudaSuccess;
   PtBatch bb;
   const int rows = with_rows(b, bb, [](const PtJob& j) { return j.t; });
-  ptop_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  ptop_kernel<<<dim3(r.N / (2 * kT), rows, 1), kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -585,7 +596,7 @@ cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst*
   if (b.njobs <= 0) return cudaSuccess;
   ScalarBatch bb;
   const int rows = with_rows(b, bb, [](const ScalarJob& j) { return j.t; });
-  scalar_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  scalar_kernel<<<dim3(r.N / (2 * kT), rows, 1), kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }

@@ -105,20 +105,25 @@ struct PtBatch {
   PtJob jobs[kMaxJobs];
 };
 
-// out[p][j] = ct[p][j] * mul[j] (+ add[j] on poly 0), per-tower constants inline.
-constexpr int kMaxScalarJobs = 16;
-struct ScalarJob {
-  const u64* ct;
-  u64* out;
-  int t;
+// out[p][j] = ct[p][j] * mul[j] (+ add[j] on poly 0) with the per-tower constants of the job's set; several
+// jobs may share one set (the many-to-one form: one scalar applied to a group of ciphertexts).
+constexpr int kMaxScalarSets = 8;
+struct ScalarSet {
   u64 mul[64];
   u64 mul_sh[64];
   u64 add[64];
 };
+struct ScalarJob {
+  const u64* ct;
+  u64* out;
+  int t;
+  int set;
+};
 struct ScalarBatch {
   int njobs;
-  int row_begin[kMaxScalarJobs + 1];
-  ScalarJob jobs[kMaxScalarJobs];
+  int row_begin[kMaxJobs + 1];
+  ScalarJob jobs[kMaxJobs];
+  ScalarSet sets[kMaxScalarSets];
 };
 
 // Baby-step/giant-step inner sums: job (x, g) writes out[p][j] = sum_{b<bs, present} rot[b][p][j] (.) pt[g*bs+b][j]

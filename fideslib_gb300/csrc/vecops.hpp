@@ -93,21 +93,32 @@ inline int each(Scope& sc, const V& a, V& out, F f) {
   sc.keep(out);
   return FIDES_OK;
 }
+// Scalar ops: one many-to-one call (one launch) for the whole vector; element i uses v[i] (and scale[i]).
+inline int scalar_batch(Scope& sc, int32_t op, const V& a, const std::vector<double>& v,
+                        const std::vector<double>* scale, V& out) {
+  out.assign(a.size(), 0);
+  if (a.empty()) return FIDES_OK;
+  FGB_TRY(fides_eval_many_to_one(sc.ctx, op, (uint32_t)a.size(), 1, a.data(), nullptr, v.data(),
+                                 scale ? scale->data() : nullptr, out.data()));
+  sc.keep(out);
+  return FIDES_OK;
+}
 inline int mult_scalar(Scope& sc, const V& a, const std::vector<double>& v, double scale, V& out) {
-  return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_mult_scalar(sc.ctx, a[i], v[i], scale, o); });
+  const std::vector<double> s(a.size(), scale);
+  return scalar_batch(sc, FIDES_OP_MULT_SCALAR, a, v, &s, out);
 }
 inline int mult_scalar(Scope& sc, const V& a, double v, double scale, V& out) {
-  return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_mult_scalar(sc.ctx, a[i], v, scale, o); });
+  return mult_scalar(sc, a, std::vector<double>(a.size(), v), scale, out);
 }
 // Per-element constant scales: element i gets round(v * scale[i]) and scale *= scale[i].
 inline int mult_scalar_at(Scope& sc, const V& a, double v, const std::vector<double>& scale, V& out) {
-  return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_mult_scalar(sc.ctx, a[i], v, scale[i], o); });
+  return scalar_batch(sc, FIDES_OP_MULT_SCALAR, a, std::vector<double>(a.size(), v), &scale, out);
 }
 inline int add_scalar(Scope& sc, const V& a, double v, V& out) {
-  return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_add_scalar(sc.ctx, a[i], v, o); });
+  return scalar_batch(sc, FIDES_OP_ADD_SCALAR, a, std::vector<double>(a.size(), v), nullptr, out);
 }
 inline int mult_int(Scope& sc, const V& a, int64_t k, V& out) {
-  return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_mult_int(sc.ctx, a[i], k, o); });
+  return scalar_batch(sc, FIDES_OP_MULT_INT, a, std::vector<double>(a.size(), (double)k), nullptr, out);
 }
 inline int monomial(Scope& sc, const V& a, uint32_t k, V& out) {
   return each(sc, a, out, [&](size_t i, uint32_t* o) { return fides_eval_mult_monomial(sc.ctx, a[i], k, o); });

@@ -176,6 +176,20 @@ int fides_eval_mult_int(fides_ctx* ctx, uint32_t a, int64_t k, uint32_t* out);
 int fides_eval_mult_scalar(fides_ctx* ctx, uint32_t a, double v, double scale, uint32_t* out);
 /* Adds v in every slot: round(v * ct scale) added to c0 (EvalAdd(ct, double), src/AddSub.cu scalar_add_). */
 int fides_eval_add_scalar(fides_ctx* ctx, uint32_t a, double v, uint32_t* out);
+/* Batched many-to-one form of the element-wise ops (addBatchManyToOne, multPtBatchManyToOne,
+ * addScalarBatchManyToOne, multScalarBatchManyToOne: src/CKKS/LimbPartitionBatch.cu:20-266,
+ * src/CKKS/RNSPolyBatch.cpp:15-80): for i < nb and j < stride, ciphertext a[i*stride + j] is combined with
+ * operand i, all nb*stride ciphertexts (each at its own level) in one launch per 64.  `op` and operand i:
+ *   FIDES_OP_ADD / FIDES_OP_SUB               b[i], a ciphertext with the same towers as its group
+ *   FIDES_OP_MULT_PLAIN / ADD_PLAIN / SUB_PLAIN   b[i], a plaintext with at least as many towers
+ *   FIDES_OP_MULT_SCALAR  round(values[i] * scales[i]); the result's scale is multiplied by scales[i]
+ *   FIDES_OP_ADD_SCALAR   values[i] in every slot (round(values[i] * ct scale) added to c0)
+ *   FIDES_OP_MULT_INT     the integer values[i] (|values[i]| < 2^53); scale unchanged
+ * outs (nb*stride handles) receives new ciphertexts; outs == NULL updates the a ciphertexts in place, as the
+ * reference does (their handles stay valid, metadata updated; no handle may repeat in `a`). */
+enum { FIDES_OP_MULT_SCALAR = 13, FIDES_OP_ADD_SCALAR = 14, FIDES_OP_MULT_INT = 15 };
+int fides_eval_many_to_one(fides_ctx* ctx, int32_t op, uint32_t nb, uint32_t stride, const uint32_t* a,
+                           const uint32_t* b, const double* values, const double* scales, uint32_t* outs);
 /* Keeps the first `towers` towers (LevelReduce / SetLevel, api/CryptoContext.hpp:184). */
 int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out);
 /* ModRaise (src/CKKS/Bootstrap.cu:393-...): tower 0 of `a`, lifted (centred) to `towers` towers. */
@@ -274,11 +288,12 @@ int fides_eval_bootstrap_batch(fides_ctx* ctx, uint32_t m, const uint32_t* cts, 
  * RNSPolyBatch.cpp) to the whole key-switching pipeline. */
 enum { FIDES_OP_ADD = 1, FIDES_OP_SUB = 2, FIDES_OP_MULT = 3, FIDES_OP_SQUARE = 4, FIDES_OP_RESCALE = 5,
        FIDES_OP_ROTATE = 6, FIDES_OP_AUTOMORPHISM = 7, FIDES_OP_KEY_SWITCH = 8,
-       FIDES_OP_BOOTSTRAP = 9 /* request server only (fides_server_set_bootstrap_plan) */ };
+       FIDES_OP_BOOTSTRAP = 9 /* request server only (fides_server_set_bootstrap_plan) */,
+       FIDES_OP_MULT_PLAIN = 10, FIDES_OP_ADD_PLAIN = 11, FIDES_OP_SUB_PLAIN = 12 /* b = plaintext handle */ };
 typedef struct {
   int32_t op;      /* FIDES_OP_* */
   uint32_t a;      /* first operand handle */
-  uint32_t b;      /* second operand (ADD / SUB / MULT) */
+  uint32_t b;      /* second operand (ADD / SUB / MULT: ciphertext; *_PLAIN: plaintext) */
   int32_t index;   /* rotation index (ROTATE), Galois element (AUTOMORPHISM) or switch-key id (KEY_SWITCH) */
   uint32_t out;    /* result handle, written by the call */
 } fides_op;
