@@ -513,15 +513,8 @@ def served_bench(args, dev):
             "single_op_latency_ms_p50_n16": single}
 
 
-def boot_bench(args, dev):
-    """Config 5: CKKS bootstrapping at N = 2^16 with 32768 full slots, level budget {3, 3} (CoeffsToSlots and
-    SlotsToCoeffs each three factors of the special FFT, up to 63 diagonals per factor, encoded on the GPU),
-    sparse-secret encapsulation (two switch keys), EvalMod = Chebyshev degree 47 on [-12.5K, 12.5K] + 3 double
-    angles (K = q_0 / 2^55).  Moduli as in the N = 2^16 bootstrap precision test: q_0 of 60 bits, 24 towers of
-    55 bits (scale 2^55), 5 special primes of 60 bits, dnum 5.  Eight bootstraps in flight together
-    (fides_eval_bootstrap_batch: every step one batched launch for all eight), the same eight one at a time, and
-    the eight submitted as requests to the continuous-batching server.  Keys are seeded random residues of the
-    real shape (a key switch costs the same on any residues)."""
+def boot_setup(dev):
+    """Context, keys, plan and eight level-0 ciphertexts of the config-5 bootstrap (see boot_bench)."""
     import numpy as np
     import numpy.polynomial.chebyshev as Cheb
     import torch
@@ -553,11 +546,12 @@ def boot_bench(args, dev):
     need = set()
     for inverse in (True, False):
         for M, stride, r in BP.factors(n, 3, inverse, scale=n / N if inverse else 1.0):
-            bs, gs, base, slots = BP.bsgs_layout(M, n, stride, r)
+            bs, gs, base, slots = BP.bsgs_layout(M, n, stride, r, bs=BP.ext_baby_steps(r))
             need |= BP.rotation_indices(n, N, stride, bs, gs, base, slots)
             present = [s is not None for s in slots]
             diag = np.array([x if x is not None else np.zeros(n) for x in slots])
-            lts[inverse].append(ctx.lt_create_slots(bs, gs, diag, present, delta, nq, stride=stride, base=base))
+            lts[inverse].append(ctx.lt_create_slots(bs, gs, diag, present, delta, nq, stride=stride, base=base,
+                                                    ext=True))
     for idx in sorted(need):
         k = rand_key()
         ctx.load_rotation_key_device(ctx.galois(idx), k.data_ptr())
@@ -573,6 +567,41 @@ def boot_bench(args, dev):
         x = torch.randint(0, 1 << 62, (2, 1, N), dtype=torch.int64, device=dev, generator=gen) % modt[0]
         hs.append(ctx.load_ciphertext_device(x.data_ptr(), 1, scale=delta))
     torch.cuda.synchronize()
+    return ctx, plan, hs, stream, len(need) + 1
+
+
+def profile_bootstrap():
+    import torch
+
+    import fideslib_gb300 as F
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ctx, plan, hs, stream, _ = boot_setup(dev)
+    for o in ctx.eval_bootstrap_batch(hs, plan):
+        ctx.free(o)
+    torch.cuda.synchronize()
+    l0 = F.kernel_launches()
+    for o in ctx.eval_bootstrap_batch(hs, plan):
+        ctx.free(o)
+    torch.cuda.synchronize()
+    return {"profile_bootstrap": True, "launches_before_batch": l0, "launches_per_batch": F.kernel_launches() - l0}
+
+
+def boot_bench(args, dev):
+    """Config 5: CKKS bootstrapping at N = 2^16 with 32768 full slots, level budget {3, 3} (CoeffsToSlots and
+    SlotsToCoeffs each three factors of the special FFT, up to 63 diagonals per factor, encoded on the GPU at the
+    special primes too and evaluated double-hoisted with 16 or 8 baby steps),
+    sparse-secret encapsulation (two switch keys), EvalMod = Chebyshev degree 47 on [-12.5K, 12.5K] + 3 double
+    angles (K = q_0 / 2^55).  Moduli as in the N = 2^16 bootstrap precision test: q_0 of 60 bits, 24 towers of
+    55 bits (scale 2^55), 5 special primes of 60 bits, dnum 5.  Eight bootstraps in flight together
+    (fides_eval_bootstrap_batch: every step one batched launch for all eight), the same eight one at a time, and
+    the eight submitted as requests to the continuous-batching server.  Keys are seeded random residues of the
+    real shape (a key switch costs the same on any residues)."""
+    import torch
+
+    import fideslib_gb300 as F
+    ctx, plan, hs, stream, nkeys = boot_setup(dev)
+    m = len(hs)
 
     def timed(fn, reps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -616,8 +645,9 @@ def boot_bench(args, dev):
     torch.cuda.synchronize()
     return {"workload": "cfg5: bootstrap N=2^16, 32768 full slots, level budget {3,3}, sparse-secret "
                         "encapsulation, Chebyshev 47 + 3 double angles, 8 in flight; q_0 60 bits + 24 x 55-bit "
-                        "towers, 5 x 60-bit special primes, dnum 5; diagonals encoded on the GPU",
-            "rotation_keys": len(need) + 1, "towers_after": towers_left,
+                        "towers, 5 x 60-bit special primes, dnum 5; diagonals encoded on the GPU at Q and P, "
+                        "double-hoisted factors (bs 16 / 8)",
+            "rotation_keys": nkeys, "towers_after": towers_left,
             "batched_8": {"ms": round(batch_ms, 2), "bootstraps_per_s": round(m / (batch_ms / 1e3), 2),
                           "gpu_launches": int(launches)},
             "one_at_a_time_8": {"ms": round(single_ms, 2), "bootstraps_per_s": round(m / (single_ms / 1e3), 2),
@@ -730,6 +760,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-bootstrap", action="store_true")
+    ap.add_argument("--profile-bootstrap", action="store_true",
+                    help="set up the config-5 bootstrap, run one batch of eight as warm-up and one more, print the "
+                         "launch counts and exit (the command profiled for the bootstrap launch list)")
     ap.add_argument("--profile-step", action="store_true",
                     help="set up the headline workload, run --warmup batched steps and one more, print the launch "
                          "count and exit (the command profiled for the per-kernel launch list)")
@@ -737,6 +770,9 @@ def main():
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.profile_bootstrap:
+        print(json.dumps(profile_bootstrap()), flush=True)
+        return
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)

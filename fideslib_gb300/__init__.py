@@ -95,6 +95,8 @@ _SIGS = {
                                   C.c_double, u32p]),
     "fides_lt_create_strided": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
                                           u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
+    "fides_lt_create_strided_ext": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32,
+                                              C.c_uint32, u64p, C.POINTER(C.c_uint8), C.c_double, u32p]),
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fides_ctx_ntt_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
@@ -107,6 +109,9 @@ _SIGS = {
     "fides_lt_create_slots": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
                                         C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_uint8),
                                         C.c_uint32, C.c_double, u32p]),
+    "fides_lt_create_slots_ext": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_uint8),
+                                            C.c_uint32, C.c_double, u32p]),
     "fides_load_switch_key": (C.c_int, [C.c_void_p, C.c_uint32, u64p]),
     "fides_load_switch_key_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "fides_eval_key_switch": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
@@ -388,14 +393,17 @@ class CryptoContext:
         return self._un(lib().fides_mod_raise, a, towers)
 
     def lt_create(self, bs: int, gs: int, diags: np.ndarray, present, scale: float = 1.0, stride: int = 1,
-                  base: int = 0) -> int:
+                  base: int = 0, ext: bool = False) -> int:
         """diags: u64[gs*bs][towers][N], diagonal k = g*bs+b (slot offset base + k*stride) pre-rotated by
-        -(base + g*bs*stride); present: bool[gs*bs]."""
+        -(base + g*bs*stride); present: bool[gs*bs].  ext: every diagonal carries towers + np rows (the special
+        primes last) and the transform is evaluated double-hoisted."""
         diags = np.ascontiguousarray(diags, dtype=np.uint64)
         pres = np.ascontiguousarray(np.array(present, dtype=np.uint8))
         h = C.c_uint32()
-        _check(lib().fides_lt_create_strided(self._h, bs, gs, stride, base, diags.shape[1], _p(diags),
-                                             pres.ctypes.data_as(C.POINTER(C.c_uint8)), scale, C.byref(h)))
+        fn = lib().fides_lt_create_strided_ext if ext else lib().fides_lt_create_strided
+        towers = diags.shape[1] - (self.np if ext else 0)
+        _check(fn(self._h, bs, gs, stride, base, towers, _p(diags), pres.ctypes.data_as(C.POINTER(C.c_uint8)),
+                  scale, C.byref(h)))
         return h.value
 
     def eval_linear_transform_batch(self, cts, lt: int) -> list[int]:
@@ -456,16 +464,17 @@ class CryptoContext:
         return out
 
     def lt_create_slots(self, bs: int, gs: int, diags, present, scale: float, towers: int, stride: int = 1,
-                        base: int = 0) -> int:
-        """diags: complex [bs*gs][slots] (rows of absent diagonals ignored), encoded on the GPU."""
+                        base: int = 0, ext: bool = False) -> int:
+        """diags: complex [bs*gs][slots] (rows of absent diagonals ignored), encoded on the GPU (also at the
+        special primes when ext: a double-hoisted transform)."""
         d = np.asarray(diags, dtype=np.complex128)
         re, im = np.ascontiguousarray(d.real), np.ascontiguousarray(d.imag)
         pres = np.ascontiguousarray(np.array(present, dtype=np.uint8))
         h = C.c_uint32()
         dp = C.POINTER(C.c_double)
-        _check(lib().fides_lt_create_slots(self._h, bs, gs, stride, base, towers, re.ctypes.data_as(dp),
-                                           im.ctypes.data_as(dp), pres.ctypes.data_as(C.POINTER(C.c_uint8)),
-                                           d.shape[1], scale, C.byref(h)))
+        fn = lib().fides_lt_create_slots_ext if ext else lib().fides_lt_create_slots
+        _check(fn(self._h, bs, gs, stride, base, towers, re.ctypes.data_as(dp), im.ctypes.data_as(dp),
+                  pres.ctypes.data_as(C.POINTER(C.c_uint8)), d.shape[1], scale, C.byref(h)))
         return h.value
 
     def eval_mult_monomial(self, a: int, k: int) -> int:

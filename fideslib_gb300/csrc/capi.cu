@@ -1007,8 +1007,8 @@ int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, c
   return fides_lt_create_strided(ctx, bs, gs, 1, 0, towers, diags, present, scale, handle);
 }
 
-int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
-                            const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle) {
+static int lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers, bool ext,
+                     const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle) {
   if (!valid_ctx(ctx) || !diags || !present || !handle) return fail(FIDES_EINVAL, "null argument");
   fgb::Context* c = ctx->c;
   if (bs < 1 || gs < 1 || gs > (uint32_t)fgb::kMaxJobs || towers < 1 || towers > (uint32_t)c->nq)
@@ -1020,22 +1020,43 @@ int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t st
   lt.stride = (int)stride;
   lt.base = (int)base;
   lt.t = (int)towers;
+  lt.ext = ext;
+  lt.rows = (int)towers + (ext ? c->np : 0);
   lt.scale = scale;
   lt.present.assign(present, present + (size_t)bs * gs);
-  const size_t bytes = (size_t)bs * gs * towers * c->N * sizeof(uint64_t);
+  const size_t bytes = (size_t)bs * gs * lt.rows * c->N * sizeof(uint64_t);
   void* d = nullptr;
   void* pd = nullptr;
   CK(cudaMalloc(&d, bytes), "linear transform allocation");
-  CK(cudaMalloc(&pd, (size_t)bs * gs), "linear transform allocation");
+  if (cudaMalloc(&pd, (size_t)bs * gs) != cudaSuccess) {
+    cudaFree(d);
+    return fail(FIDES_ENOMEM, "linear transform allocation failed");
+  }
   lt.diags = (fgb::u64*)d;
   lt.present_dev = (uint8_t*)pd;
-  CK(cudaMemcpyAsync(d, diags, bytes, cudaMemcpyDefault, c->stream), "linear transform copy");
-  CK(cudaMemcpyAsync(pd, present, (size_t)bs * gs, cudaMemcpyHostToDevice, c->stream), "linear transform copy");
-  CK(cudaStreamSynchronize(c->stream), "linear transform copy");
+  cudaError_t e = cudaMemcpyAsync(d, diags, bytes, cudaMemcpyDefault, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(pd, present, (size_t)bs * gs, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    cudaFree(pd);
+    return cuda_fail(e, "linear transform copy");
+  }
   const uint32_t h = c->next_handle++;
   c->lts[h] = std::move(lt);
   *handle = h;
   return FIDES_OK;
+}
+
+int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
+                            const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle) {
+  return lt_create(ctx, bs, gs, stride, base, towers, false, diags, present, scale, handle);
+}
+
+int fides_lt_create_strided_ext(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base,
+                                uint32_t towers, const uint64_t* diags, const uint8_t* present, double scale,
+                                uint32_t* handle) {
+  return lt_create(ctx, bs, gs, stride, base, towers, true, diags, present, scale, handle);
 }
 
 int fides_lt_free(fides_ctx* ctx, uint32_t handle) {

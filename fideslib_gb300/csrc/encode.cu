@@ -62,9 +62,10 @@ __global__ void fft_stage_kernel(double2* __restrict__ a, int nv, int n, int len
 
 __device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) { return bits ? __brev(x) >> (32 - bits) : 0; }
 
-// Encode placement: out[v][j][c] = round(scale m_c) mod q_j with m from the FFT output y (w_k = y[brev(k)]).
+// Encode placement: out[v][j][c] = round(scale m_c) mod m_j with m from the FFT output y (w_k = y[brev(k)]);
+// row j < tq is Q tower j, row tq + k the special prime nq + k (t rows in all).
 __global__ void encode_place_kernel(const double2* __restrict__ y, int nv, int n, int logn, int N, double scale, int t,
-                                    const fgb::PrimeConst* __restrict__ pc, u64* __restrict__ out,
+                                    int tq, int nq, const fgb::PrimeConst* __restrict__ pc, u64* __restrict__ out,
                                     int* __restrict__ overflow) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)nv * N) return;
@@ -83,7 +84,7 @@ __global__ void encode_place_kernel(const double2* __restrict__ y, int nv, int n
   const long long iv = (long long)r;
   const u64 mag = (u64)(iv < 0 ? -iv : iv);
   for (int j = 0; j < t; j++) {
-    const u64 q = pc[j].p, m = mag % q;
+    const u64 q = pc[j < tq ? j : nq + (j - tq)].p, m = mag % q;
     out[((size_t)v * t + j) * N + c] = (iv < 0 && m) ? q - m : m;
   }
 }
@@ -173,10 +174,11 @@ int ilog2(uint32_t x) {
   return l;
 }
 
-// Encodes nv vectors (host re/im, [nv][slots]) into out ([nv][towers][N] device, evaluation form).
+// Encodes nv vectors (host re/im, [nv][slots]) into out ([nv][rows][N] device, evaluation form): rows = towers Q
+// towers, followed by the np special primes when `ext`.
 int encode_many(fgb::Context* c, const double* re, const double* im, int nv, uint32_t slots, double scale, int towers,
-                u64* out) {
-  const int n = (int)slots, N = c->N;
+                bool ext, u64* out) {
+  const int n = (int)slots, N = c->N, rows = towers + (ext ? c->np : 0);
   FftTables T;
   if (int rc = tables_for(n, &T)) return rc;
   std::vector<double2> host((size_t)nv * n);
@@ -196,12 +198,15 @@ int encode_many(fgb::Context* c, const double* re, const double* im, int nv, uin
   }
   if (e == cudaSuccess) {
     const long long total = (long long)nv * N;
-    encode_place_kernel<<<(unsigned)((total + kT - 1) / kT), kT, 0, c->stream>>>(a, nv, n, ilog2(n), N, scale, towers,
-                                                                                 c->d_pc, out, ovf);
+    encode_place_kernel<<<(unsigned)((total + kT - 1) / kT), kT, 0, c->stream>>>(a, nv, n, ilog2(n), N, scale, rows,
+                                                                                 towers, c->nq, c->d_pc, out, ovf);
     fgb::count_launch();
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = c->ntt(out, out, nv, towers, 0, (long long)towers * N, false, c->stream);
+  if (e == cudaSuccess) e = c->ntt(out, out, nv, towers, 0, (long long)rows * N, false, c->stream);
+  if (e == cudaSuccess && ext)
+    e = c->ntt(out + (size_t)towers * N, out + (size_t)towers * N, nv, c->np, c->nq, (long long)rows * N, false,
+               c->stream);
   int hovf = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&hovf, ovf, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(a, c->stream);
@@ -227,7 +232,7 @@ int fides_pt_encode(fides_ctx* ctx, const double* re, const double* im, uint32_t
   p.scale = scale;
   p.data = c->alloc_limbs(towers, c->stream);
   if (!p.data) return fgb::set_last_error(FIDES_ENOMEM, "plaintext allocation failed");
-  if (int rc = encode_many(c, re, im, 1, slots, scale, (int)towers, p.data)) {
+  if (int rc = encode_many(c, re, im, 1, slots, scale, (int)towers, false, p.data)) {
     c->free_limbs(p.data, c->stream);
     return rc;
   }
@@ -289,14 +294,14 @@ int fides_pt_decode(fides_ctx* ctx, uint32_t pt, uint32_t slots, double* re, dou
   return FIDES_OK;
 }
 
-int fides_lt_create_slots(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
-                          const double* re, const double* im, const uint8_t* present, uint32_t slots, double scale,
-                          uint32_t* handle) {
+static int lt_create_slots(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
+                           bool ext, const double* re, const double* im, const uint8_t* present, uint32_t slots,
+                           double scale, uint32_t* handle) {
   if (!ctx || !ctx->c || !re || !im || !present || !handle) return fgb::set_last_error(FIDES_EINVAL, "null argument");
   fgb::Context* c = ctx->c;
   if (int rc = check_slots(c, slots)) return rc;
   if (towers < 1 || towers > (uint32_t)c->nq) return fgb::set_last_error(FIDES_EINVAL, "towers out of range");
-  const size_t nd = (size_t)bs * gs, per = (size_t)towers * c->N;
+  const size_t nd = (size_t)bs * gs, per = (size_t)(towers + (ext ? c->np : 0)) * c->N;
   std::vector<double> r, i;
   std::vector<size_t> idx;
   for (size_t d = 0; d < nd; d++)
@@ -309,7 +314,7 @@ int fides_lt_create_slots(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stri
   if (!idx.empty() && cudaMalloc(&enc, idx.size() * per * sizeof(u64)) != cudaSuccess)
     return fgb::set_last_error(FIDES_ENOMEM, "diagonal encoding allocation failed");
   int rc = FIDES_OK;
-  if (!idx.empty()) rc = encode_many(c, r.data(), i.data(), (int)idx.size(), slots, scale, (int)towers, enc);
+  if (!idx.empty()) rc = encode_many(c, r.data(), i.data(), (int)idx.size(), slots, scale, (int)towers, ext, enc);
   u64* full = nullptr;
   if (rc == FIDES_OK && cudaMalloc(&full, nd * per * sizeof(u64)) != cudaSuccess)
     rc = fgb::set_last_error(FIDES_ENOMEM, "diagonal allocation failed");
@@ -317,14 +322,27 @@ int fides_lt_create_slots(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stri
     cudaError_t e = cudaMemsetAsync(full, 0, nd * per * sizeof(u64), c->stream);
     for (size_t k = 0; k < idx.size() && e == cudaSuccess; k++)
       e = cudaMemcpyAsync(full + idx[k] * per, enc + k * per, per * sizeof(u64), cudaMemcpyDeviceToDevice, c->stream);
+    const uint64_t* d = reinterpret_cast<const uint64_t*>(full);
     rc = e != cudaSuccess ? fgb::set_last_error(FIDES_ECUDA, cudaGetErrorString(e))
-                          : fides_lt_create_strided(ctx, bs, gs, stride, base, towers,
-                                                    reinterpret_cast<const uint64_t*>(full), present, scale, handle);
+         : ext            ? fides_lt_create_strided_ext(ctx, bs, gs, stride, base, towers, d, present, scale, handle)
+                          : fides_lt_create_strided(ctx, bs, gs, stride, base, towers, d, present, scale, handle);
   }
   cudaStreamSynchronize(c->stream);
   cudaFree(enc);
   cudaFree(full);
   return rc;
+}
+
+int fides_lt_create_slots(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
+                          const double* re, const double* im, const uint8_t* present, uint32_t slots, double scale,
+                          uint32_t* handle) {
+  return lt_create_slots(ctx, bs, gs, stride, base, towers, false, re, im, present, slots, scale, handle);
+}
+
+int fides_lt_create_slots_ext(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base,
+                              uint32_t towers, const double* re, const double* im, const uint8_t* present,
+                              uint32_t slots, double scale, uint32_t* handle) {
+  return lt_create_slots(ctx, bs, gs, stride, base, towers, true, re, im, present, slots, scale, handle);
 }
 
 }  // extern "C"

@@ -276,7 +276,8 @@ bool Context::build(const u64* roots, std::string* err) {
       }
     }
   }
-  std::vector<ulonglong2> md_phinv(np), md_pinv(nq), rs_qinv((size_t)nq * nq, make_ulonglong2(0, 0));
+  std::vector<ulonglong2> md_phinv(np), md_pinv(nq), md_pmodq(nq),
+      rs_qinv((size_t)nq * nq, make_ulonglong2(0, 0));
   std::vector<uint32_t> md_phat((size_t)np * nq * 2);
   for (int k = 0; k < np; k++) {
     const u64 pk = mod[nq + k];
@@ -300,6 +301,7 @@ bool Context::build(const u64* roots, std::string* err) {
     for (int k = 0; k < np; k++) P = hmul(P, mod[nq + k] % q, q);
     const u64 w = hinv(P, q);
     md_pinv[j] = make_ulonglong2(w, shoup_of(w, q));
+    md_pmodq[j] = make_ulonglong2(P, shoup_of(P, q));
   }
   for (int l = 1; l < nq; l++)
     for (int i = 0; i < l; i++) {
@@ -322,9 +324,11 @@ bool Context::build(const u64* roots, std::string* err) {
   crt.md_phinv = (const ulonglong2*)up(md_phinv.data(), sizeof(ulonglong2) * md_phinv.size());
   crt.md_phat = (const uint32_t*)up(md_phat.data(), sizeof(uint32_t) * md_phat.size());
   crt.md_pinv = (const ulonglong2*)up(md_pinv.data(), sizeof(ulonglong2) * md_pinv.size());
+  crt.md_pmodq = (const ulonglong2*)up(md_pmodq.data(), sizeof(ulonglong2) * md_pmodq.size());
   crt.rs_qinv = (const ulonglong2*)up(rs_qinv.data(), sizeof(ulonglong2) * rs_qinv.size());
 
-  if (!crt.mu_qhinv || !crt.mu_qhat || !crt.md_phinv || !crt.md_phat || !crt.md_pinv || !crt.rs_qinv) {
+  if (!crt.mu_qhinv || !crt.mu_qhat || !crt.md_phinv || !crt.md_phat || !crt.md_pinv || !crt.md_pmodq ||
+      !crt.rs_qinv) {
     *err = "device allocation failed";
     return false;
   }
@@ -496,7 +500,7 @@ cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
   for (int i = 0; i < n; i++) {
     const int t = reqs[i].t;
     r_off[i] = total;
-    total += (size_t)2 * (t + np) + (size_t)2 * t;
+    total += (size_t)2 * (t + np) + (reqs[i].ext_mode ? 0 : (size_t)2 * t);
   }
   u64* ws = alloc_limbs(total, s);
   if (!ws) return cudaErrorMemoryAllocation;
@@ -507,7 +511,6 @@ cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
   };
   auto inner_of = [&](int i) { return ws + r_off[i] * NN; };
   auto md_of = [&](int i) { return ws + (r_off[i] + 2 * (size_t)(reqs[i].t + np)) * NN; };
-  uint8_t pm[64];
   std::vector<const u64*> ma;
   std::vector<int> mt;
   std::vector<u64*> mcoeff, mconv;
@@ -520,9 +523,10 @@ cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
     mconv.push_back(conv_of(g));
   }
   cudaError_t err = modup(ma.data(), mt.data(), mcoeff.data(), mconv.data(), (int)ma.size(), s);
-  // 4) inner products, 5) INTT of the P rows, 6) ModDown conversion, 7) NTT, 8) epilogue
+  // 4) inner products; then 5) INTT of the P rows, 6) ModDown conversion, 7) NTT, 8) epilogue for the ordinary
+  // requests, or the extended-basis epilogue for the double-hoisted ones
   for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
-    KsBatch kb{};
+    KsBatch kb{}, md{}, ex{};
     for (int i = i0; i < n && kb.njobs < kMaxJobs; i++) {
       const KsReq& r = reqs[i];
       KsJob& j = kb.jobs[kb.njobs++];
@@ -533,39 +537,78 @@ cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
       j.coeff = coeff_of(group_of[i]);
       j.conv = conv_of(group_of[i]);
       j.inner = inner_of(i);
-      j.md = md_of(i);
+      j.md = r.ext_mode ? nullptr : md_of(i);
       j.out = r.out;
       j.t = r.t;
       j.galois_inv = r.galois_inv;
+      j.polys = 2;
+      j.ext_mode = r.ext_mode;
+      KsBatch& dst = r.ext_mode ? ex : md;
+      dst.jobs[dst.njobs++] = j;
     }
     err = launch_ks_inner(kb, ring_, crt, d_pc, s);
-    if (err != cudaSuccess) break;
-    {
-      NttQueue q(tabs, true, s);
-      for (int k = 0; k < np; k++) pm[k] = (uint8_t)(nq + k);
-      for (int b = 0; b < kb.njobs; b++) {
-        const KsJob& j = kb.jobs[b];
-        u64* p = j.inner + (size_t)j.t * NN;
-        q.add(p, p, (long long)(j.t + np) * N, (long long)(j.t + np) * N, np, 2, pm);
-      }
-      q.flush();
-      err = q.err;
+    if (err == cudaSuccess) err = moddown_jobs(md, s);
+    if (err == cudaSuccess) err = launch_ext_epilogue(ex, ring_, crt, d_pc, s);
+  }
+  free_limbs(ws, s);
+  return err;
+}
+
+cudaError_t Context::moddown_jobs(const KsBatch& kb, cudaStream_t s) {
+  if (kb.njobs <= 0) return cudaSuccess;
+  const size_t NN = (size_t)N;
+  uint8_t pm[64];
+  cudaError_t err;
+  {
+    NttQueue q(tabs, true, s);
+    for (int k = 0; k < np; k++) pm[k] = (uint8_t)(nq + k);
+    for (int b = 0; b < kb.njobs; b++) {
+      const KsJob& j = kb.jobs[b];
+      u64* p = j.inner + (size_t)j.t * NN;
+      q.add(p, p, (long long)(j.t + np) * N, (long long)(j.t + np) * N, np, j.polys ? j.polys : 2, pm);
     }
-    if (err != cudaSuccess) break;
-    err = launch_moddown_conv(kb, ring_, crt, d_pc, s);
-    if (err != cudaSuccess) break;
-    {
-      NttQueue q(tabs, false, s);
-      for (int b = 0; b < kb.njobs; b++) {
-        const KsJob& j = kb.jobs[b];
-        for (int k = 0; k < j.t; k++) pm[k] = (uint8_t)k;
-        q.add(j.md, j.md, (long long)j.t * N, (long long)j.t * N, j.t, 2, pm);
-      }
-      q.flush();
-      err = q.err;
+    q.flush();
+    err = q.err;
+  }
+  if (err == cudaSuccess) err = launch_moddown_conv(kb, ring_, crt, d_pc, s);
+  if (err == cudaSuccess) {
+    NttQueue q(tabs, false, s);
+    for (int b = 0; b < kb.njobs; b++) {
+      const KsJob& j = kb.jobs[b];
+      for (int k = 0; k < j.t; k++) pm[k] = (uint8_t)k;
+      q.add(j.md, j.md, (long long)j.t * N, (long long)j.t * N, j.t, j.polys ? j.polys : 2, pm);
     }
-    if (err != cudaSuccess) break;
-    err = launch_moddown_epilogue(kb, ring_, crt, d_pc, s);
+    q.flush();
+    err = q.err;
+  }
+  if (err == cudaSuccess) err = launch_moddown_epilogue(kb, ring_, crt, d_pc, s);
+  return err;
+}
+
+cudaError_t Context::moddown_batch(const MdReq* reqs, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const size_t NN = (size_t)N;
+  std::vector<size_t> off(n);
+  size_t total = 0;
+  for (int i = 0; i < n; i++) {
+    off[i] = total;
+    total += (size_t)reqs[i].polys * reqs[i].t;
+  }
+  u64* ws = alloc_limbs(total, s);
+  if (!ws) return cudaErrorMemoryAllocation;
+  cudaError_t err = cudaSuccess;
+  for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
+    KsBatch kb{};
+    for (int i = i0; i < n && kb.njobs < kMaxJobs; i++) {
+      KsJob& j = kb.jobs[kb.njobs++];
+      j.inner = reqs[i].x;
+      j.md = ws + off[i] * NN;
+      j.out = reqs[i].out;
+      j.t = reqs[i].t;
+      j.polys = reqs[i].polys;
+      j.galois_inv = 1;
+    }
+    err = moddown_jobs(kb, s);
   }
   free_limbs(ws, s);
   return err;
@@ -686,6 +729,7 @@ cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64*
 
 cudaError_t Context::linear_transform_batch(const u64* const* xs, int n, int t, const DevLT& lt, u64* const* outs,
                                             cudaStream_t s) {
+  if (lt.ext) return linear_transform_ext_batch(xs, n, t, lt, outs, s);
   const size_t NN = (size_t)N, CT = (size_t)2 * t * NN;
   const int bs = lt.bs, gs = lt.gs;
   if (n <= 0) return cudaSuccess;
@@ -723,7 +767,7 @@ cudaError_t Context::linear_transform_batch(const u64* const* xs, int n, int t, 
     DotBatch db{};
     db.rot_stride = (long long)CT;
     db.pt_base = lt.diags;
-    db.pt_stride = (long long)lt.t * N;
+    db.pt_stride = (long long)lt.rows * N;
     db.present = lt.present_dev;
     db.bs = bs;
     db.t = t;
@@ -778,6 +822,142 @@ cudaError_t Context::linear_transform_batch(const u64* const* xs, int n, int t, 
     }
   }
   if (err == cudaSuccess && sb.njobs) err = launch_sum(sb, ring_, d_pc, s);
+  free_limbs(ws, s);
+  return err;
+}
+
+cudaError_t Context::linear_transform_ext_batch(const u64* const* xs, int n, int t, const DevLT& lt,
+                                                u64* const* outs, cudaStream_t s) {
+  const size_t NN = (size_t)N, E = (size_t)2 * (t + np) * NN;  // one ciphertext in the extended basis
+  const int bs = lt.bs, gs = lt.gs;
+  if (n <= 0) return cudaSuccess;
+  if (t > lt.t || gs > kMaxJobs) return cudaErrorInvalidValue;
+  const std::vector<int32_t> baby_r = lt.baby_rotations(N), giant_r = lt.giant_rotations(N);
+  std::vector<int> active;  // giant steps with at least one diagonal
+  for (int g = 0; g < gs; g++) {
+    bool any = false;
+    for (int b = 0; b < bs; b++) any = any || lt.present[(size_t)g * bs + b];
+    if (any) active.push_back(g);
+  }
+  const int na = (int)active.size();
+  // per input: bs baby ciphertexts (b = 0 is the input lifted by P), na inner sums, na rotated sums, the total
+  // (all extended), and na ModDowned c1 polys (t limbs each)
+  const size_t per = (size_t)(bs + 2 * na + 1) * E + (size_t)na * t * NN;
+  u64* ws = alloc_limbs(per * n / NN, s);
+  if (!ws) return cudaErrorMemoryAllocation;
+  auto at = [&](int i) { return ws + (size_t)i * per; };
+  auto baby = [&](int i, int b) { return at(i) + (size_t)b * E; };
+  auto inner = [&](int i, int k) { return at(i) + (size_t)(bs + k) * E; };
+  auto rotd = [&](int i, int k) { return at(i) + (size_t)(bs + na + k) * E; };
+  auto total = [&](int i) { return at(i) + (size_t)(bs + 2 * na) * E; };
+  auto c1d = [&](int i, int k) { return at(i) + (size_t)(bs + 2 * na + 1) * E + (size_t)k * t * NN; };
+  cudaError_t err = cudaSuccess;
+  {  // b = 0: (P x0, P x1) on the Q rows, zero on the special rows
+    KsBatch kb{};
+    for (int i = 0; i < n && err == cudaSuccess; i++) {
+      KsJob& j = kb.jobs[kb.njobs++];
+      j.add0 = xs[i];
+      j.add1 = xs[i] + (size_t)t * NN;
+      j.out = baby(i, 0);
+      j.t = t;
+      j.galois_inv = 1;
+      j.ext_mode = 1;
+      if (kb.njobs == kMaxJobs || i == n - 1) {
+        err = launch_ext_epilogue(kb, ring_, crt, d_pc, s);
+        kb.njobs = 0;
+      }
+    }
+  }
+  if (err == cudaSuccess) {  // baby steps: one shared ModUp per input, no ModDown
+    std::vector<KsReq> rq;
+    for (int i = 0; i < n && err == cudaSuccess; i++)
+      for (int b = 1; b < bs && err == cudaSuccess; b++) {
+        if (baby_r[b - 1] == 0) {
+          err = cudaMemcpyAsync(baby(i, b), baby(i, 0), E * sizeof(u64), cudaMemcpyDeviceToDevice, s);
+          continue;
+        }
+        const uint32_t g = galois_for_index(N, baby_r[b - 1]);
+        auto it = rot_keys.find(g);
+        if (it == rot_keys.end()) {
+          err = cudaErrorInvalidValue;
+          break;
+        }
+        KsReq r{xs[i] + (size_t)t * NN, t, it->second, xs[i], nullptr, baby(i, b), galois_inverse(g)};
+        r.ext_mode = 1;
+        rq.push_back(r);
+      }
+    if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
+  }
+  if (err == cudaSuccess) {  // inner sums in the extended basis
+    DotBatch db{};
+    db.rot_stride = (long long)E;
+    db.pt_base = lt.diags;
+    db.pt_stride = (long long)lt.rows * N;
+    db.present = lt.present_dev;
+    db.bs = bs;
+    db.t = t;
+    db.np = np;
+    db.nq = nq;
+    db.pt_prow = lt.t;
+    for (int i = 0; i < n && err == cudaSuccess; i++)
+      for (int k = 0; k < na; k++) {
+        db.jobs[db.njobs++] = DotJob{inner(i, k), baby(i, 0), bs > 1 ? baby(i, 1) : nullptr, active[k]};
+        if (db.njobs == kMaxJobs) {
+          err = launch_ptdot(db, ring_, d_pc, s);
+          db.njobs = 0;
+          if (err != cudaSuccess) break;
+        }
+      }
+    if (err == cudaSuccess && db.njobs) err = launch_ptdot(db, ring_, d_pc, s);
+  }
+  // giant steps: ModDown of each sum's c1, then its rotation without ModDown (c0 stays extended)
+  std::vector<int> nrot(n, 0);
+  std::vector<std::vector<const u64*>> plain(n);
+  std::vector<MdReq> md;
+  std::vector<KsReq> rq;
+  for (int i = 0; i < n && err == cudaSuccess; i++)
+    for (int k = 0; k < na; k++) {
+      const int g = active[k];
+      if (giant_r[g] == 0) {
+        plain[i].push_back(inner(i, k));
+        continue;
+      }
+      const uint32_t gl = galois_for_index(N, giant_r[g]);
+      auto it = rot_keys.find(gl);
+      if (it == rot_keys.end()) {
+        err = cudaErrorInvalidValue;
+        break;
+      }
+      md.push_back(MdReq{inner(i, k) + (size_t)(t + np) * NN, t, 1, c1d(i, k)});
+      KsReq r{c1d(i, k), t, it->second, inner(i, k), nullptr, rotd(i, nrot[i]++), galois_inverse(gl)};
+      r.ext_mode = 2;
+      rq.push_back(r);
+    }
+  if (err == cudaSuccess) err = moddown_batch(md.data(), (int)md.size(), s);
+  if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
+  // totals (rotated terms contiguous at rotd(i, 0..), the first unrotated one as `first`), then one ModDown each
+  SumBatch sb{};
+  sb.nq = nq;
+  std::vector<MdReq> fin;
+  for (int i = 0; i < n && err == cudaSuccess; i++) {
+    int k = nrot[i];
+    for (size_t p = 1; p < plain[i].size() && err == cudaSuccess; p++, k++)
+      err = cudaMemcpyAsync(rotd(i, k), plain[i][p], E * sizeof(u64), cudaMemcpyDeviceToDevice, s);
+    if (err != cudaSuccess) break;
+    if (k == 0 && plain[i].empty()) {
+      err = cudaMemsetAsync(outs[i], 0, (size_t)2 * t * NN * sizeof(u64), s);
+      continue;
+    }
+    sb.jobs[sb.njobs++] = SumJob{rotd(i, 0), (long long)E, k, plain[i].empty() ? nullptr : plain[i][0], total(i), t,
+                                 np};
+    fin.push_back(MdReq{total(i), t, 2, outs[i]});
+    if (sb.njobs == kMaxJobs) {
+      err = launch_sum(sb, ring_, d_pc, s);
+      sb.njobs = 0;
+    }
+  }
+  if (err == cudaSuccess && sb.njobs) err = launch_sum(sb, ring_, d_pc, s);
+  if (err == cudaSuccess) err = moddown_batch(fin.data(), (int)fin.size(), s);
   free_limbs(ws, s);
   return err;
 }

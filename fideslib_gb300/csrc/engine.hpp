@@ -51,6 +51,8 @@ struct DevLT {
   std::vector<uint8_t> present;
   int bs = 0, gs = 0, t = 0;
   int stride = 1, base = 0;
+  bool ext = false;  // diagonals hold t + np rows (Q towers, then the special primes): double-hoisted evaluation
+  int rows = 0;      // rows per diagonal: t, or t + np when ext
   double scale = 1.0;
   // slot-rotation indices the transform needs keys for (nonzero modulo N/2)
   std::vector<int32_t> baby_rotations(int N) const;
@@ -91,9 +93,22 @@ class Context {
     u64* out;
     uint32_t galois_inv;
     const u64* digits = nullptr;  // precomputed ModUp of `a` (modup()'s conv layout); skips the ModUp
+    // 1, 2: no ModDown; out ([2][t+np][N], extended basis Q_t ∪ P) = automorph(inner + lift), where the lift is
+    // (P*add0, P*add1) on the Q rows (mode 1, add0 / add1 in Q_t layout) or add0 in the extended layout added to
+    // poly 0 (mode 2, add1 unused).  Double hoisting (the linear transforms of bootstrapping).
+    int ext_mode = 0;
   };
   // All requests in one pipeline: requests with the same (a, t) share one ModUp (hoisting).
   cudaError_t keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s);
+  // ModDown of `polys` polys of x ([polys][t+np][N], extended basis, evaluation form) into out ([polys][t][N]).
+  // x's special rows are left in coefficient form (used as scratch).
+  struct MdReq {
+    u64* x;
+    int t;
+    int polys;
+    u64* out;
+  };
+  cudaError_t moddown_batch(const MdReq* reqs, int n, cudaStream_t s);
   // ModUp of ng inputs a[g] (t[g] towers, evaluation form): coeff[g] (t limbs) is scratch, conv[g] receives the
   // beta (t + np) limbs of extended digits (digit d at conv + d (t+np) N; its own towers are not written).
   cudaError_t modup(const u64* const* a, const int* ts, u64* const* coeff, u64* const* conv, int ng, cudaStream_t s);
@@ -128,6 +143,11 @@ class Context {
   // The same transform of n ciphertexts with t towers each, every stage batched over all of them.
   cudaError_t linear_transform_batch(const u64* const* xs, int n, int t, const DevLT& lt, u64* const* outs,
                                      cudaStream_t s);
+  // The double-hoisted form for transforms whose diagonals carry the special primes (lt.ext): baby steps stay in
+  // the extended basis Q_t ∪ P (no ModDown), the inner sums run there, each giant-step sum is ModDowned in c1
+  // only before its rotation (which again skips the ModDown), and one ModDown of the total ends the transform.
+  cudaError_t linear_transform_ext_batch(const u64* const* xs, int n, int t, const DevLT& lt, u64* const* outs,
+                                         cudaStream_t s);
   cudaError_t mult_monomial(const u64* x, int t, unsigned k, u64* out, cudaStream_t s);
   // Raise a ciphertext's tower 0 to T towers (centred lift) — the first step of bootstrapping.
   cudaError_t mod_raise(const u64* x, int t_in, int T, u64* out, cudaStream_t s);
@@ -157,6 +177,9 @@ class Context {
   bool build(const u64* roots, std::string* err);
   std::vector<void*> owned_;  // device allocations freed at destruction
   void* dmalloc(size_t bytes);
+  // INTT of the special rows, ModDown conversion, NTT and epilogue for the jobs of kb (inner, md, out, t, polys,
+  // add0 / add1, galois_inv set).
+  cudaError_t moddown_jobs(const KsBatch& kb, cudaStream_t s);
 
   Ring ring_{};
 };

@@ -261,6 +261,44 @@ __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_const
   }
 }
 
+// Extended-basis key-switch output (double hoisting, no ModDown): rows 2 (t + np) per job over Q_t ∪ P,
+// out[p][j] = automorph(inner[p][j] + a_p[j]) with a_0 = P * add0 on the Q rows (ext_mode 1) or add0 in the
+// extended layout (ext_mode 2), a_1 = P * add1 on the Q rows (ext_mode 1); inner may be null (zero), which lifts
+// a Q-basis ciphertext into the extended basis.
+__global__ void __launch_bounds__(kT) ext_epilogue_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
+                                                          const PrimeConst* __restrict__ pc) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const KsJob& J = b.jobs[z];
+  const int t = J.t, ext = t + c.np, row = (int)blockIdx.y - b.row_begin[z];
+  const int poly = row >= ext ? 1 : 0, j = row - poly * ext;
+  const int tower = j < t ? j : c.nq + (j - t);
+  const u64 q = pc[tower].p;
+  const int n = (blockIdx.x * kT + threadIdx.x) * 2;
+  const size_t N = r.N;
+  ulonglong2 v = J.inner ? *reinterpret_cast<const ulonglong2*>(J.inner + ((size_t)poly * ext + j) * N + n)
+                         : make_ulonglong2(0, 0);
+  const u64* add = poly == 0 ? J.add0 : J.add1;
+  if (add && J.ext_mode == 2) {
+    const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(add + (size_t)j * N + n);
+    v = make_ulonglong2(add_mod(v.x, a.x, q), add_mod(v.y, a.y, q));
+  } else if (add && j < t) {
+    const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(add + (size_t)j * N + n);
+    const ulonglong2 w = c.md_pmodq[j];
+    v = make_ulonglong2(add_mod(v.x, shoup(a.x, w.x, w.y, q), q), add_mod(v.y, shoup(a.y, w.x, w.y, q), q));
+  }
+  u64* out = J.out + ((size_t)poly * ext + j) * N;
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    uint32_t pos = n + e;
+    if (J.galois_inv != 1) {
+      const uint32_t idx = brev_n(n + e, r.logN);
+      const uint32_t jj = (uint32_t)((((2ull * idx + 1) * J.galois_inv) & (2ull * N - 1)) >> 1);
+      pos = brev_n(jj, r.logN);
+    }
+    out[pos] = e ? v.y : v.x;
+  }
+}
+
 __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ TensorBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
@@ -383,15 +421,16 @@ __global__ void __launch_bounds__(kT) monomial_kernel(const __grid_constant__ Mo
   J.out[o] = v;
 }
 
-// grid rows per job: 2*t (poly-major).
+// grid rows per job: 2*(t+np) (poly-major; np = 0 outside the extended basis).
 __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBatch b, Ring r,
                                                    const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const DotJob& J = b.jobs[z];
   const int row = (int)blockIdx.y - b.row_begin[z];
-  const int t = b.t, poly = row >= t ? 1 : 0, j = row - poly * t;
+  const int t = b.t, rows = t + b.np, poly = row >= rows ? 1 : 0, j = row - poly * rows;
+  const int tower = j < t ? j : b.nq + (j - t), prow = j < t ? j : b.pt_prow + (j - t);
   const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
-  const size_t co = ((size_t)poly * t + j) * r.N + n, po = (size_t)j * r.N + n;
+  const size_t co = ((size_t)poly * rows + j) * r.N + n, po = (size_t)prow * r.N + n;
   u64 hi = 0, lo = 0;
   Acc4 A{0, 0, 0, 0};
   int terms = 0;
@@ -409,7 +448,7 @@ __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBa
     }
   }
   acc4_fold(A, hi, lo);
-  J.out[co] = reduce128_fast(hi, lo, pc[j]);
+  J.out[co] = reduce128_fast(hi, lo, pc[tower]);
 }
 
 __global__ void __launch_bounds__(kT) sum_kernel(const __grid_constant__ SumBatch b, Ring r,
@@ -417,9 +456,9 @@ __global__ void __launch_bounds__(kT) sum_kernel(const __grid_constant__ SumBatc
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const SumJob& J = b.jobs[z];
   const int row = (int)blockIdx.y - b.row_begin[z];
-  const int t = J.t, poly = row >= t ? 1 : 0, j = row - poly * t;
-  const size_t o = ((size_t)poly * t + j) * r.N + (size_t)blockIdx.x * kT + threadIdx.x;
-  const u64 q = pc[j].p;
+  const int t = J.t, rows = t + J.np, poly = row >= rows ? 1 : 0, j = row - poly * rows;
+  const size_t o = ((size_t)poly * rows + j) * r.N + (size_t)blockIdx.x * kT + threadIdx.x;
+  const u64 q = pc[j < t ? j : b.nq + (j - t)].p;
   u64 acc = J.first ? J.first[o] : 0;
 #pragma unroll 4
   for (int k = 0; k < J.n; k++) acc = add_mod(acc, J.base[(size_t)k * J.stride + o], q);
@@ -510,7 +549,7 @@ cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables
   if (b.njobs <= 0) return cudaSuccess;
   const size_t smem = sizeof(uint2) * c.np * max_t(b);
   KsBatch bb;
-  const int rows = with_rows(b, bb, [](const KsJob&) { return 2; });
+  const int rows = with_rows(b, bb, [](const KsJob& j) { return j.polys ? j.polys : 2; });
   dim3 grid(r.N / kT, rows, 1);
   switch (c.np) {
 #define FGB_MD_CASE(K_)                                                    \
@@ -532,9 +571,21 @@ cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTa
                                     cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
   KsBatch bb;
-  const int rows = with_rows(b, bb, [](const KsJob& j) { return 2 * j.t; });
+  const int rows = with_rows(b, bb, [](const KsJob& j) { return (j.polys ? j.polys : 2) * j.t; });
   dim3 grid(r.N / (2 * kT), rows, 1);
   moddown_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ext_epilogue(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
+                                cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  KsBatch bb;
+  const int np = c.np;
+  const int rows = with_rows(b, bb, [np](const KsJob& j) { return 2 * (j.t + np); });
+  dim3 grid(r.N / (2 * kT), rows, 1);
+  ext_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -615,7 +666,7 @@ cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc,
   if (b.njobs <= 0) return cudaSuccess;
   DotBatch bb = b;
   bb.row_begin[0] = 0;
-  for (int i = 0; i < b.njobs; i++) bb.row_begin[i + 1] = bb.row_begin[i] + 2 * b.t;
+  for (int i = 0; i < b.njobs; i++) bb.row_begin[i + 1] = bb.row_begin[i] + 2 * (b.t + b.np);
   ptdot_kernel<<<dim3(r.N / kT, bb.row_begin[b.njobs], 1), kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
@@ -624,7 +675,7 @@ cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc,
 cudaError_t launch_sum(const SumBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
   SumBatch bb;
-  const int rows = with_rows(b, bb, [](const SumJob& j) { return 2 * j.t; });
+  const int rows = with_rows(b, bb, [](const SumJob& j) { return 2 * (j.t + j.np); });
   sum_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();

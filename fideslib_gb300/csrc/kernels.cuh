@@ -20,6 +20,7 @@ struct CrtTables {
   const ulonglong2* md_phinv;  // [k] = {[Phat_k^-1]_{p_k}, shoup}
   const uint32_t* md_phat;     // [(k*nq + j)*2 + {0,1}] = 30-bit slices of [Phat_k]_{q_j}
   const ulonglong2* md_pinv;   // [j] = {[P^-1]_{q_j}, shoup}
+  const ulonglong2* md_pmodq;  // [j] = {[P]_{q_j}, shoup} (lifting Q-basis values into the extended basis)
   // Rescale: top tower l, target i < l
   const ulonglong2* rs_qinv;   // [l*nq + i] = {[q_l^-1]_{q_i}, shoup}
 };
@@ -30,6 +31,9 @@ struct Ring {
 
 // One key switch: ModUp(a) (shared by jobs with the same input), inner product with `key`, ModDown of both
 // halves, + add0/add1, automorphism scatter by galois_inv (1 = none) into out.
+// ext_mode 1 / 2 (double hoisting) skips the ModDown: out = automorph(inner + add) stays in the extended basis
+// Q_t ∪ P ([2][t+np][N]); mode 1 adds P*add0 (and P*add1) on the Q rows (add0 / add1 in Q_t layout), mode 2 adds
+// add0 given in the extended layout to poly 0.  A ModDown-only job (moddown_batch) has polys = 1 or 2.
 struct KsJob {
   const u64* a;      // [t][N] evaluation form (the digit's own towers are read from here)
   const u64* add0;   // [t][N] or null
@@ -42,6 +46,8 @@ struct KsJob {
   u64* out;          // [2][t][N]
   int t;
   uint32_t galois_inv;
+  int polys;     // polys the ModDown kernels process (0 means 2)
+  int ext_mode;  // 0: ModDown output; 1, 2: extended output (see above)
 };
 
 struct KsBatch {
@@ -143,6 +149,9 @@ struct DotBatch {
   long long pt_stride;
   const uint8_t* present;  // device [gs*bs]
   int bs, t;
+  // extended basis (np > 0): ciphertexts are [2][t+np][N], row t+k is special prime nq+k and reads plaintext
+  // row pt_prow+k
+  int np, nq, pt_prow;
   DotJob jobs[kMaxJobs];
 };
 
@@ -154,8 +163,10 @@ struct SumJob {
   const u64* first;  // added too when non-null
   u64* out;
   int t;
+  int np;  // rows t..t+np-1 are the special primes (extended-basis sums), else 0
 };
 struct SumBatch {
+  int nq;
   int njobs;
   int row_begin[kMaxJobs + 1];
   SumJob jobs[kMaxJobs];
@@ -203,6 +214,8 @@ cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables
                                 cudaStream_t s);
 cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                                     cudaStream_t s);
+cudaError_t launch_ext_epilogue(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
+                                cudaStream_t s);
 cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, const PrimeConst* pc,

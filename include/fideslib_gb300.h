@@ -209,6 +209,16 @@ int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, c
  * a zero rotation needs no key). */
 int fides_lt_create_strided(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
                             const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle);
+/* The same with every diagonal also given at the special primes (plaintexts raised to the extended basis, the
+ * reference's ModUp'd LT plaintexts, src/CKKS/LinearTransform.cu:93-99): diags = u64[gs*bs][towers + np][N], the
+ * towers Q rows then the np special rows.  Such a transform is evaluated double-hoisted (LinearTransform's
+ * MODDOWN_HOIST / ONLY_C1 path, src/CKKS/LinearTransform.cu:104-190): the baby-step rotations skip their ModDown
+ * and the inner sums run in the extended basis Q_t ∪ P, each giant-step sum has only its c1 ModDowned before its
+ * rotation (which again skips the ModDown), and one ModDown of the total ends the transform, so a transform does
+ * one ModUp per baby-step input and per giant step and gs + 1 ModDowns instead of bs + gs - 1. */
+int fides_lt_create_strided_ext(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base,
+                                uint32_t towers, const uint64_t* diags, const uint8_t* present, double scale,
+                                uint32_t* handle);
 int fides_lt_free(fides_ctx* ctx, uint32_t handle);
 int fides_eval_linear_transform(fides_ctx* ctx, uint32_t a, uint32_t lt, uint32_t* out);
 /* The same transform of n ciphertexts with equal tower counts, each stage (baby-step rotations, inner sums,
@@ -235,6 +245,10 @@ int fides_pt_store(fides_ctx* ctx, uint32_t pt, uint64_t* data);
 int fides_lt_create_slots(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base, uint32_t towers,
                           const double* re, const double* im, const uint8_t* present, uint32_t slots, double scale,
                           uint32_t* handle);
+/* The same encoded at the special primes too: a double-hoisted transform (fides_lt_create_strided_ext). */
+int fides_lt_create_slots_ext(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, int32_t base,
+                              uint32_t towers, const double* re, const double* im, const uint8_t* present,
+                              uint32_t slots, double scale, uint32_t* handle);
 
 /* EvalChebyshevSeries (api/CryptoContext.hpp:154-156, src/CKKS/ApproxModEval.cu:138-370):
  * p(x) = sum_k coeffs[k] T_k((2x - lo - hi)/(hi - lo)), k < n, constants encoded at const_scale.  The exact op

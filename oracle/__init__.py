@@ -104,6 +104,9 @@ def lib():
         L.orc_rot_keygen.argtypes = [C.c_void_p, C.c_uint64, i64p, C.c_uint32, u64p]
         L.orc_encode.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int, C.c_double,
                                  C.c_int, u64p]
+        L.orc_encode_ids.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
+                                     C.c_double, C.c_int, i32p, u64p]
+        L.orc_ew_ids.argtypes = [C.c_void_p, u64p, u64p, C.c_int, C.c_int, C.c_int, i32p, C.c_int, u64p]
         L.orc_decode.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]
         L.orc_encrypt_sk.argtypes = [C.c_void_p, C.c_uint64, i64p, u64p, C.c_int, u64p]
@@ -348,13 +351,33 @@ class Ctx:
         lib().orc_rot_keygen(self._h, seed, _p(s, i64p), galois, _p(k))
         return k
 
-    def encode(self, z: np.ndarray, scale: float, t: int) -> np.ndarray:
+    def encode(self, z: np.ndarray, scale: float, t: int, tower_ids=None) -> np.ndarray:
+        """Encoding into t rows (Q towers 0..t-1, or the rows tower_ids)."""
         z = np.asarray(z, dtype=np.complex128)
         re = np.ascontiguousarray(z.real)
         im = np.ascontiguousarray(z.imag)
         out = self.zeros(t)
-        lib().orc_encode(self._h, _p(re, C.POINTER(C.c_double)), _p(im, C.POINTER(C.c_double)), len(z), scale, t,
-                         _p(out))
+        dp = C.POINTER(C.c_double)
+        if tower_ids is None:
+            lib().orc_encode(self._h, _p(re, dp), _p(im, dp), len(z), scale, t, _p(out))
+        else:
+            ids = np.ascontiguousarray(tower_ids, dtype=np.int32)
+            lib().orc_encode_ids(self._h, _p(re, dp), _p(im, dp), len(z), scale, t, _p(ids, i32p), _p(out))
+        return out
+
+    def ext_ids(self, t: int) -> list[int]:
+        """Tower ids of the extended basis Q_t ∪ P (rows of an extended ciphertext)."""
+        return list(range(t)) + list(range(self.nq, self.nq + self.np))
+
+    def ew(self, x: np.ndarray, y: np.ndarray, tower_ids, op: int) -> np.ndarray:
+        """x * y (op 0) or x + y (op 1) limb-wise modulo tower_ids; x [polys][nl][N], y [nl][N] or like x."""
+        x = np.ascontiguousarray(x, dtype=np.uint64)
+        y = np.ascontiguousarray(y, dtype=np.uint64)
+        nl = len(tower_ids)
+        out = np.zeros_like(x)
+        ids = np.ascontiguousarray(tower_ids, dtype=np.int32)
+        lib().orc_ew_ids(self._h, _p(x), _p(y), nl, x.size // (nl * self.N), y.size // (nl * self.N), _p(ids, i32p),
+                         op, _p(out))
         return out
 
     def decode(self, pt: np.ndarray, scale: float, slots: int) -> np.ndarray:

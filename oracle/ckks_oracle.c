@@ -821,7 +821,8 @@ static void fft_inplace(double* re, double* im, uint64_t n, int sign) {
   }
 }
 
-void orc_encode(const orc_ctx* c, const double* zr, const double* zi, int slots, double scale, int t, uint64_t* pt) {
+void orc_encode_ids(const orc_ctx* c, const double* zr, const double* zi, int slots, double scale, int nt,
+                    const int* tower_ids, uint64_t* pt) {
   uint64_t N = c->N, M = 2 * N;
   double* re = (double*)calloc(M, sizeof(double));
   double* im = (double*)calloc(M, sizeof(double));
@@ -834,16 +835,35 @@ void orc_encode(const orc_ctx* c, const double* zr, const double* zi, int slots,
   }
   /* m_i = (1/N) sum_k v_k zeta^{-ik}: forward DFT (negative exponent) of length 2N */
   fft_inplace(re, im, M, -1);
-  for (int j = 0; j < t; j++) {
-    uint64_t q = c->mod[j];
+  for (int j = 0; j < nt; j++) {
+    uint64_t q = c->mod[tower_ids ? tower_ids[j] : j];
     for (uint64_t k = 0; k < N; k++) {
       int64_t v = (int64_t)llround(re[k] / (double)N * scale);
       pt[(size_t)j * N + k] = to_residue(v, q);
     }
   }
-  orc_to_eval(c, pt, t, NULL);
+  orc_to_eval(c, pt, nt, tower_ids);
   free(re);
   free(im);
+}
+
+void orc_encode(const orc_ctx* c, const double* zr, const double* zi, int slots, double scale, int t, uint64_t* pt) {
+  orc_encode_ids(c, zr, zi, slots, scale, t, NULL, pt);
+}
+
+/* Element-wise x (op) y on npolys polys of nl limbs, limb j modulo tower_ids[j] (op 0 = product, 1 = sum); y has
+ * ypolys polys (1 = the same plaintext for every poly of x).  The extended-basis arithmetic of the double-hoisted
+ * linear transform (pt products and sums over Q_t ∪ P). */
+void orc_ew_ids(const orc_ctx* c, const uint64_t* x, const uint64_t* y, int nl, int npolys, int ypolys,
+                const int* tower_ids, int op, uint64_t* out) {
+  uint64_t N = c->N;
+  for (int poly = 0; poly < npolys; poly++)
+    for (int j = 0; j < nl; j++) {
+      uint64_t p = c->mod[tower_ids[j]];
+      size_t xo = ((size_t)poly * nl + j) * N, yo = ((size_t)(ypolys == 1 ? 0 : poly) * nl + j) * N;
+      for (uint64_t k = 0; k < N; k++)
+        out[xo + k] = op == 0 ? orc_mulmod(x[xo + k], y[yo + k], p) : addmod(x[xo + k], y[yo + k], p);
+    }
 }
 
 /* CRT reconstruction to a centred double (multi-word integer arithmetic). */

@@ -98,6 +98,12 @@ void orc_ksk_gen(const orc_ctx* c, uint64_t seed, const int64_t* s_from, const i
 void orc_relin_keygen(const orc_ctx* c, uint64_t seed, const int64_t* s, uint64_t* key);
 void orc_rot_keygen(const orc_ctx* c, uint64_t seed, const int64_t* s, uint32_t galois, uint64_t* key);
 void orc_encode(const orc_ctx* c, const double* re, const double* im, int slots, double scale, int t, uint64_t* pt);
+/* The same into nt rows modulo tower_ids[j] (NULL: 0..nt-1), e.g. Q towers followed by special primes. */
+void orc_encode_ids(const orc_ctx* c, const double* re, const double* im, int slots, double scale, int nt,
+                    const int* tower_ids, uint64_t* pt);
+/* Element-wise product (op 0) or sum (op 1) over limbs with explicit tower ids; ypolys = 1 broadcasts y. */
+void orc_ew_ids(const orc_ctx* c, const uint64_t* x, const uint64_t* y, int nl, int npolys, int ypolys,
+                const int* tower_ids, int op, uint64_t* out);
 void orc_decode(const orc_ctx* c, const uint64_t* pt, int t, double scale, int slots, double* re, double* im);
 void orc_encrypt_sk(const orc_ctx* c, uint64_t seed, const int64_t* s, const uint64_t* pt, int t, uint64_t* ct);
 void orc_decrypt(const orc_ctx* c, const int64_t* s, const uint64_t* ct, int t, uint64_t* pt);

@@ -4,7 +4,8 @@ Ring N=2^12, q_0 of 60 bits and 55-bit towers, 4 special primes of 60 bits (P ab
 Two shapes: 16 sparse slots with a one-factor level budget, and 2048 full slots with the level budget {3, 3}
 and sparse-secret encapsulation (main secret of Hamming weight 192, encapsulated under weight 32).  The
 CoeffsToSlots / SlotsToCoeffs factors come from the factored special FFT (tests/boot_plan.py) and are encoded by
-the oracle, the way the reference receives its bootstrap plaintexts from OpenFHE.  Every output residue is
+the oracle, the way the reference receives its bootstrap plaintexts from OpenFHE; the full-slot shape uses
+double-hoisted factors (diagonals also at the special primes), the sparse one the ModDown-per-rotation form.  Every output residue is
 checked against an op-for-op oracle replay of the recipe documented in fideslib_gb300/csrc/bootstrap.cu, and
 the decrypted slots against the input message (precision stated).  A batch of bootstraps in flight together
 must give exactly the single-call results."""
@@ -28,8 +29,9 @@ B_RANGE = 12.5
 
 
 class Setup:
-    def __init__(self, slots, budget, sse, seed):
+    def __init__(self, slots, budget, sse, seed, ext=False):
         import fideslib_gb300 as F
+        from fideslib_gb300.bootplan import ext_baby_steps
         self.F, self.slots = F, slots
         self.mods = O.make_moduli(LOGN, [60] + [55] * (NQ - 1), [60] * NP)
         self.gpu = F.CryptoContext(LOGN, self.mods, NP, DNUM)
@@ -43,9 +45,10 @@ class Setup:
             self.sse = (orc.switch_key(seed + 3, self.s, s_sparse), orc.switch_key(seed + 4, s_sparse, self.s))
             self.gpu.load_switch_key(10, self.sse[0])
             self.gpu.load_switch_key(11, self.sse[1])
-        self.cts = [BP.Factor(orc, M, slots, stride, r, NQ, DELTA_PT)
+        bs = ext_baby_steps if ext else (lambda r: None)  # noqa: E731
+        self.cts = [BP.Factor(orc, M, slots, stride, r, NQ, DELTA_PT, ext=ext, bs=bs(r))
                     for M, stride, r in BP.factors(slots, budget[0], inverse=True, scale=slots / N)]
-        self.stc = [BP.Factor(orc, M, slots, stride, r, NQ, DELTA_PT)
+        self.stc = [BP.Factor(orc, M, slots, stride, r, NQ, DELTA_PT, ext=ext, bs=bs(r))
                     for M, stride, r in BP.factors(slots, budget[1], inverse=False)]
         need = set()
         for f in self.cts + self.stc:
@@ -132,7 +135,8 @@ def test_bootstrap_sparse_slots():
 
 
 def test_bootstrap_full_slots_level_budget_sse_and_batch():
-    st = Setup(slots=N // 2, budget=(3, 3), sse=True, seed=0x5EED0015)
+    """Double-hoisted CoeffsToSlots / SlotsToCoeffs factors (diagonals at the special primes too)."""
+    st = Setup(slots=N // 2, budget=(3, 3), sse=True, seed=0x5EED0015, ext=True)
     z, ct = st.message(78)
     got, meta = check(st, z, ct, 2e-5)
     assert meta.towers >= 2
@@ -151,7 +155,7 @@ def test_bootstrap_full_slots_level_budget_sse_and_batch():
 def test_bootstrap_requests_through_the_server():
     """Bootstrap requests submitted to the continuous-batching server run in flight together and give exactly the
     single-call results."""
-    st = Setup(slots=N // 2, budget=(3, 3), sse=True, seed=0x5EED0025)
+    st = Setup(slots=N // 2, budget=(3, 3), sse=True, seed=0x5EED0025, ext=True)
     gpu, F = st.gpu, st.F
     msgs = [st.message(90 + i) for i in range(3)]
     hs = [gpu.load_ciphertext(ct, DELTA_M) for _, ct in msgs]

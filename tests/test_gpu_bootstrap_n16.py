@@ -3,7 +3,8 @@ encapsulation (main secret of Hamming weight 192, encapsulated under weight 32).
 
 Moduli: q_0 of 60 bits and 24 towers of 55 bits (the scaling factor 2^55 sits on the towers, q_0 / scale = 32),
 5 special primes of 60 bits (P above each 5-tower digit), dnum 5.  Keys come from the oracle; the CoeffsToSlots /
-SlotsToCoeffs diagonals are encoded on the GPU (fides_lt_create_slots).  Residue-exact replay at this size is too
+SlotsToCoeffs diagonals are encoded on the GPU at the special primes too (fides_lt_create_slots_ext: double-hoisted
+factors with twice the default baby steps, as in the config-5 benchmark).  Residue-exact replay at this size is too
 slow for the oracle (the N = 2^12 tests replay the same recipe op for op); this test states the decrypted
 precision."""
 import numpy as np
@@ -38,11 +39,12 @@ def test_bootstrap_full_slots_n16(engine_lib):
     need = set()
     for inverse in (True, False):
         for M, stride, r in BP.factors(n, 3, inverse, scale=n / N if inverse else 1.0):
-            bs, gs, base, slots = BP.bsgs_layout(M, n, stride, r)
+            bs, gs, base, slots = BP.bsgs_layout(M, n, stride, r, bs=BP.ext_baby_steps(r))
             need |= BP.rotation_indices(n, N, stride, bs, gs, base, slots)
             present = np.array([x is not None for x in slots])
             diag = np.array([x if x is not None else np.zeros(n) for x in slots])
-            lts[inverse].append(gpu.lt_create_slots(bs, gs, diag, present, DELTA, NQ, stride=stride, base=base))
+            lts[inverse].append(gpu.lt_create_slots(bs, gs, diag, present, DELTA, NQ, stride=stride, base=base,
+                                                    ext=True))
     for i, idx in enumerate(sorted(need)):
         g = orc.galois(idx)
         gpu.load_rotation_key(g, orc.rot_key(100 + i, s, g))

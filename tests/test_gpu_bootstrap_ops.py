@@ -131,3 +131,34 @@ def test_linear_transform_bsgs(env):
     err = np.abs(dec(env, got, sc * sc) - expect).max()
     assert err < 1e-5, err
     gpu.lt_free(lt)
+
+
+@pytest.mark.parametrize("towers", [8, 5])
+def test_linear_transform_double_hoisted(env, towers):
+    """A strided SlotsToCoeffs factor whose diagonals carry the special primes (fides_lt_create_strided_ext): the
+    double-hoisted evaluation (baby steps and inner sums in the extended basis, giant-step sums ModDowned in c1
+    only, one final ModDown) is bit-exact against its oracle replay for a batch of three ciphertexts, also below
+    the transform's top level, and decrypts to the factor's matrix-vector product."""
+    from fideslib_gb300 import bootplan as B
+    from tests import boot_plan as BP
+    gpu, orc, N, s = env["gpu"], env["orc"], env["N"], env["s"]
+    n, sc = N // 2, env["scale"]
+    M, stride, r = BP.factors(n, 3, inverse=False)[1]
+    f = BP.Factor(orc, M, n, stride, r, 8, sc, ext=True, bs=B.ext_baby_steps(r))
+    assert f.diags.shape[1] == 8 + 4
+    keys = {}
+    for i, idx in enumerate(sorted(f.rotations(n, N))):
+        g = orc.galois(idx)
+        keys[idx] = (g, orc.rot_key(500 + i, s, g))
+        gpu.load_rotation_key(g, keys[idx][1])
+    lt = f.create(gpu, sc)
+    rng = np.random.default_rng(31 + towers)
+    zs = [(rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)) * 0.5 for _ in range(3)]
+    cts = [orc.encrypt(40 + k, s, orc.encode(z, sc, towers)) for k, z in enumerate(zs)]
+    outs = gpu.eval_linear_transform_batch([gpu.load_ciphertext(c, sc) for c in cts], lt)
+    for c, z, o in zip(cts, zs, outs):
+        got = gpu.store_ciphertext(o)
+        assert np.array_equal(got, f.replay(orc, c, keys, N))
+        err = np.abs(dec(env, got, sc * sc) - B.apply(M, z)).max()
+        assert err < 1e-6, err
+    gpu.lt_free(lt)
