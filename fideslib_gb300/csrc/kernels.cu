@@ -10,6 +10,7 @@
 // The basis conversions accumulate sum_i y_i * c_ij exactly: both factors are < 2^60 and are split into
 // 30-bit halves, so each product is four 32x32->64 multiply-adds into four 64-bit accumulators (at most 16
 // terms per accumulator before folding into a 128-bit total), then one 128-bit reduction per output.
+#include <algorithm>
 #include <atomic>
 
 #include "kernels.cuh"
@@ -150,19 +151,27 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
 #undef FGB_MODUP_CASE
 }
 
-// Key inner product: grid (N/512, nq+np, njobs), row j of the extended basis Q_t ∪ P, two coefficients per
-// thread (16-byte loads).  Every digit's value and both key halves are loaded before any arithmetic, so a thread
-// has 3 beta loads in flight; MAXB bounds beta at compile time.  Digits and key values are split into 30-bit
-// halves and accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max).
+// Key inner product: grid (N/512, rows), two coefficients per thread (16-byte loads).  Jobs are grouped by key;
+// group g owns (tmax_g + np) * m_g rows, tmax_g its largest tower count and m_g its job count, ordered (tower row,
+// job) with the job fastest, so the m_g blocks that read the same key values are scheduled back to back and a key
+// shared by several ciphertexts (one rotation of a lock-step batch, the relinearisation key of a batch of
+// products) is read from HBM about once, the other reads hitting L2.  A block whose tower lies above its job's
+// level exits.  Every digit's value and both key halves are loaded before any arithmetic (3 beta loads in
+// flight); digits and key values are split into 30-bit halves and accumulated in one Acc4 per half-key (at most
+// 8 digits, 16 terms max); MAXB bounds beta at compile time.
 template <int MAXB>
 __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                       const PrimeConst* __restrict__ pc) {
-  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
-  const KsJob& J = b.jobs[z];
-  const int t = J.t, j = (int)blockIdx.y - b.row_begin[z];
-  const int ext = t + c.np;
-  if (j >= ext) return;
-  const int tower = j < t ? j : c.nq + (j - t);
+  const int G = find_job(b.row_begin, b.ngroups, (int)blockIdx.y);
+  const int m = b.grp_begin[G + 1] - b.grp_begin[G];
+  const int local = (int)blockIdx.y - b.row_begin[G];
+  const int rr = local / m;
+  const int tmax = (b.row_begin[G + 1] - b.row_begin[G]) / m - c.np;
+  const KsJob& J = b.jobs[b.grp_begin[G] + (local - rr * m)];
+  const int t = J.t;
+  const int tower = rr < tmax ? rr : c.nq + (rr - tmax);
+  if (tower < c.nq && tower >= t) return;  // a Q tower above this job's level
+  const int ext = t + c.np, j = tower < c.nq ? tower : t + (tower - c.nq);
   const int n = (blockIdx.x * kT + threadIdx.x) * 2;
   const size_t N = r.N;
   const int beta = (t + c.alpha - 1) / c.alpha;
@@ -525,9 +534,26 @@ cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& 
 cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                             cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
-  KsBatch bb;
-  const int np = c.np;
-  const int rows = with_rows(b, bb, [np](const KsJob& j) { return j.t + np; });
+  // jobs reordered so that those with the same key are adjacent (first-appearance order of the keys)
+  KsBatch bb = b;
+  bool used[kMaxJobs] = {};
+  int k = 0, rows = 0;
+  bb.ngroups = 0;
+  bb.row_begin[0] = 0;
+  for (int i = 0; i < b.njobs; i++) {
+    if (used[i]) continue;
+    bb.grp_begin[bb.ngroups] = k;
+    int tmax = 0;
+    for (int q = i; q < b.njobs; q++)
+      if (!used[q] && b.jobs[q].key == b.jobs[i].key) {
+        used[q] = true;
+        bb.jobs[k++] = b.jobs[q];
+        tmax = std::max(tmax, b.jobs[q].t);
+      }
+    rows += (tmax + c.np) * (k - bb.grp_begin[bb.ngroups]);
+    bb.row_begin[++bb.ngroups] = rows;
+  }
+  bb.grp_begin[bb.ngroups] = k;
   dim3 grid(r.N / (2 * kT), rows, 1);
   switch (c.dnum) {  // beta <= dnum: size the register arrays exactly (fewer registers, more resident warps)
 #define FGB_KSI_CASE(B_)                                   \

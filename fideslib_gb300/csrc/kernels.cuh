@@ -52,7 +52,10 @@ struct KsJob {
 
 struct KsBatch {
   int njobs;
-  int row_begin[kMaxJobs + 1];  // filled by each launcher: prefix sums of that kernel's rows per job
+  int row_begin[kMaxJobs + 1];  // filled by each launcher: prefix sums of that kernel's rows per job (per key
+                                // group for the key inner product)
+  int ngroups;                  // key inner product: jobs grp_begin[g] .. grp_begin[g+1]-1 share one key
+  int grp_begin[kMaxJobs + 1];
   KsJob jobs[kMaxJobs];
 };
 

@@ -16,7 +16,8 @@
 // For N = 2^13 .. 2^16 the forward transform uses a radix-16 variant of the same cluster layout (ntt16_fwd_kernel
 // below: four radix-16 passes, 16 residues per thread, three CTAs per SM).
 // Butterflies are Harvey-lazy with a cheaper quotient estimate (shoup_lazy4, products in [0, 4p)): forward
-// values live in [0, 8p), inverse in [0, 4p); outputs are reduced to [0, p).  Needs p < 2^61.  Shared memory is
+// values live in [0, 16p) (the compare-and-subtract on every other stage), inverse in [0, 4p); outputs are reduced
+// to [0, p).  Needs p < 2^60.  Shared memory is
 // XOR-swizzled (word l stored at l ^ ((l >> 5) & 15)) so every pass reads and writes with at most the
 // two-wavefront minimum of 64-bit accesses.
 #include <cooperative_groups.h>
@@ -32,9 +33,13 @@ constexpr int kThreads = 256;
 
 __device__ __forceinline__ int swz(int l) { return l ^ ((l >> 5) & 15); }
 
-// Forward (CT): X, Y in [0, 8p) -> X + wY, X - wY + 4p in [0, 8p)  (wY from shoup_lazy4 lies in [0, 4p)).
+// Forward (CT): x + wY, x - wY + 4p with wY from shoup_lazy4 in [0, 4p).  Values stay below 16p (< 2^64 for
+// p < 2^60): a stage with the correction maps X in [0, 16p) to x in [0, 8p) (X - 8p when X >= 8p) and outputs
+// [0, 12p); a stage without it takes X in [0, 12p) and outputs [0, 16p).  Stages alternate (correction on even global
+// stages), so half the butterflies skip the compare-and-subtract.
+template <bool CORR>
 __device__ __forceinline__ void ct_bfly(u64& X, u64& Y, const ulonglong2& w, u64 negp, u64 p4) {
-  const u64 x = X >= p4 ? X - p4 : X;
+  const u64 x = CORR ? (X >= 2 * p4 ? X - 2 * p4 : X) : X;
   const u64 t = shoup_lazy4(Y, w.x, w.y, negp);
   X = x + t;
   Y = x - t + p4;
@@ -64,7 +69,10 @@ __device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulon
     for (int k = 0; k < (1 << LOGR); k++) {
       if (k & (1 << kb)) continue;
       const ulonglong2 w = __ldg(row + (k >> (kb + 1)));
-      ct_bfly(x[k], x[k + (1 << kb)], w, negp, p4);
+      if ((s & 1) == 0)
+        ct_bfly<true>(x[k], x[k + (1 << kb)], w, negp, p4);
+      else
+        ct_bfly<false>(x[k], x[k + (1 << kb)], w, negp, p4);
     }
   }
 }
@@ -202,8 +210,8 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_const
 #pragma unroll
     for (int k = 0; k < 16; k += 2) {
       ulonglong2 v;
-      v.x = csub(csub(csub(x[k], p4), p2), p);
-      v.y = csub(csub(csub(x[k + 1], p4), p2), p);
+      v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
+      v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
       out[k / 2] = v;
     }
   }
@@ -399,8 +407,8 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
 #pragma unroll
     for (int k = 0; k < 16; k += 2) {
       ulonglong2 v;
-      v.x = csub(csub(csub(x[k], p4), p2), p);
-      v.y = csub(csub(csub(x[k + 1], p4), p2), p);
+      v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
+      v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
       out[k / 2] = v;
     }
   }
