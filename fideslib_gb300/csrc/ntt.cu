@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
 }
 
 // Inverse of the same shape (Gentleman–Sande, passes C^-1, B^-1, A^-1, then the cross-CTA phase X^-1 reading
-// the peers' shared memory; N^-1 applied on the way out).  Used with LOGE = 12 for small batches.
+// the peers' shared memory; N^-1 applied on the way out), with LOGE = 12 or 13 (autotuned).
 template <int LOGN, int LOGE>
 __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_constant__ NttBatch b,
                                                                  const __grid_constant__ DeviceTables T) {
@@ -565,21 +565,26 @@ cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, c
     case 11: return launch_t<11>(b, t, inverse, s);
     case 12: return launch_t<12>(b, t, inverse, s);
     // the variants tune_ntt picked for this direction and batch size (forward: 0 = radix-16 / 8192 per CTA,
-    // 1 = radix-32/16, 2 = radix-16 / 4096 per CTA; inverse: 0 = radix-32/16, 1 = radix-16 / 4096 per CTA)
+    // 1 = radix-32/16, 2 = radix-16 / 4096 per CTA; inverse: 0 = radix-32/16, 1 = radix-16 / 4096 per CTA,
+    // 2 = radix-16 / 8192 per CTA)
     case 13:
-      if (inverse) return v ? launch16<13, 12>(b, t, true, s) : launch_t<13>(b, t, true, s);
+      if (inverse) return v == 0 ? launch_t<13>(b, t, true, s) : v == 1 ? launch16<13, 12>(b, t, true, s)
+                                                         : launch16<13, 13>(b, t, true, s);
       return v == 1 ? launch_t<13>(b, t, false, s) : v == 0 ? launch16<13, 13>(b, t, false, s)
                                                            : launch16<13, 12>(b, t, false, s);
     case 14:
-      if (inverse) return v ? launch16<14, 12>(b, t, true, s) : launch_t<14>(b, t, true, s);
+      if (inverse) return v == 0 ? launch_t<14>(b, t, true, s) : v == 1 ? launch16<14, 12>(b, t, true, s)
+                                                         : launch16<14, 13>(b, t, true, s);
       return v == 1 ? launch_t<14>(b, t, false, s) : v == 0 ? launch16<14, 13>(b, t, false, s)
                                                            : launch16<14, 12>(b, t, false, s);
     case 15:
-      if (inverse) return v ? launch16<15, 12>(b, t, true, s) : launch_t<15>(b, t, true, s);
+      if (inverse) return v == 0 ? launch_t<15>(b, t, true, s) : v == 1 ? launch16<15, 12>(b, t, true, s)
+                                                         : launch16<15, 13>(b, t, true, s);
       return v == 1 ? launch_t<15>(b, t, false, s) : v == 0 ? launch16<15, 13>(b, t, false, s)
                                                            : launch16<15, 12>(b, t, false, s);
     case 16:
-      if (inverse) return v ? launch16<16, 12>(b, t, true, s) : launch_t<16>(b, t, true, s);
+      if (inverse) return v == 0 ? launch_t<16>(b, t, true, s) : v == 1 ? launch16<16, 12>(b, t, true, s)
+                                                         : launch16<16, 13>(b, t, true, s);
       return v == 1 ? launch_t<16>(b, t, false, s) : v == 0 ? launch16<16, 13>(b, t, false, s)
                                                            : launch16<16, 12>(b, t, false, s);
     default: return cudaErrorInvalidValue;

@@ -44,7 +44,7 @@ struct DeviceTables {
   int inv_variant_small = 0;
 };
 constexpr int kNttFwdVariants = 3;
-constexpr int kNttInvVariants = 2;
+constexpr int kNttInvVariants = 3;
 constexpr long long kSmallNttWork = 128ll << 16;  // residues per launch (128 limbs at N = 2^16)
 
 // Forward (inverse=false: coefficient -> evaluation, bit-reversed) or inverse transform of every job.

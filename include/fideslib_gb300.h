@@ -90,8 +90,9 @@ int fides_ctx_set_stream(fides_ctx* ctx, void* stream);
  * most / more than 128 limbs' worth (the key-switch stages of single ops / of batches).  variant[0..3] = forward
  * small, forward large, inverse small, inverse large; forward variants: 0 = radix-16 passes with 8192 residues
  * per CTA, 1 = radix-32/16 passes, 2 = radix-16 passes with 4096 residues per CTA (twice the CTAs per limb);
- * inverse: 0 = radix-32/16, 1 = radix-16 with 4096 per CTA.  ms[0..9] = forward small v0..v2, forward large
- * v0..v2, inverse small v0..v1, inverse large v0..v1 (-1 where a single kernel applies, N < 2^13). */
+ * inverse: 0 = radix-32/16, 1 = radix-16 with 4096 per CTA, 2 = radix-16 with 8192 per CTA.  ms[0..11] =
+ * forward small v0..v2, forward large v0..v2, inverse small v0..v2, inverse large v0..v2 (-1 where a single
+ * kernel applies, N < 2^13). */
 int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms);
 /* Device-memory budget of the context (the reference's pool has a release threshold only, Context.cu:74-80):
  * ciphertexts and per-op workspaces come from the stream-ordered pool and are counted; an op whose allocation
