@@ -100,12 +100,12 @@ def factors(n: int, budget: int, inverse: bool, scale: complex = 1.0):
 
 def bsgs_layout(M: dict, n: int, stride: int, r: int, bs: int | None = None):
     """(bs, gs, base, D list of length bs*gs with None for absent diagonals) for diagonals at multiples of stride
-    within +-(2^r - 1) stride.  bs defaults to 2^ceil((r+1)/2); a double-hoisted transform, whose baby steps cost
-    no NTT, runs faster with more baby steps (ext_baby_steps)."""
+    within +-(2^r - 1) stride.  bs defaults to 2^ceil((r+1)/2) (at most 16, the engine's limit); a double-hoisted
+    transform, whose baby steps cost no NTT, runs faster with more baby steps (ext_baby_steps)."""
     D = 2 ** (r + 1) - 1
     base = -(2 ** r - 1) * stride
     if bs is None:
-        bs = 1 << ((r + 2) // 2)
+        bs = min(16, 1 << ((r + 2) // 2))
     gs = -(-D // bs)
     slots = [None] * (bs * gs)
     for o, d in M.items():
@@ -123,8 +123,9 @@ def bsgs_layout(M: dict, n: int, stride: int, r: int, bs: int | None = None):
 
 
 def ext_baby_steps(r: int) -> int:
-    """Baby-step count for a double-hoisted factor of 2^(r+1) - 1 diagonals: twice the default (gs about halves)."""
-    return 1 << ((r + 2) // 2 + 1)
+    """Baby-step count for a double-hoisted factor of 2^(r+1) - 1 diagonals: twice the default (gs about halves),
+    at most 16."""
+    return min(16, 1 << ((r + 2) // 2 + 1))
 
 
 def eval_layout(v: np.ndarray, n: int, stride: int, bs: int, gs: int, base: int, slots) -> np.ndarray:

@@ -1011,8 +1011,8 @@ static int lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, int32_t stride, i
                      const uint64_t* diags, const uint8_t* present, double scale, uint32_t* handle) {
   if (!valid_ctx(ctx) || !diags || !present || !handle) return fail(FIDES_EINVAL, "null argument");
   fgb::Context* c = ctx->c;
-  if (bs < 1 || gs < 1 || gs > (uint32_t)fgb::kMaxJobs || towers < 1 || towers > (uint32_t)c->nq)
-    return fail(FIDES_EINVAL, "need bs >= 1, 1 <= gs <= 64, 1 <= towers <= nq");
+  if (bs < 1 || bs > 16 || gs < 1 || gs > (uint32_t)fgb::kMaxJobs || towers < 1 || towers > (uint32_t)c->nq)
+    return fail(FIDES_EINVAL, "need 1 <= bs <= 16, 1 <= gs <= 64, 1 <= towers <= nq");
   if (bs > 1 && stride == 0) return fail(FIDES_EINVAL, "stride must be nonzero");
   fgb::DevLT lt;
   lt.bs = (int)bs;

@@ -727,6 +727,26 @@ cudaError_t Context::linear_transform(const u64* x, int t, const DevLT& lt, u64*
   return linear_transform_batch(&x, 1, t, lt, &out, s);
 }
 
+// Inner sums of n inputs: one job per (input, chunk of at most kDotG consecutive giant steps), kMaxJobs jobs per
+// launch; rot0(i) / rot1(i) are input i's baby-step ciphertexts b = 0 / b = 1 (the rest follow at db.rot_stride),
+// out(i, g) its inner sum of giant step g (chunks write consecutive giant steps at db.out_stride).
+template <class R0, class R1, class O>
+static cudaError_t inner_sums(DotBatch& db, int n, int gs, R0 rot0, R1 rot1, O out, const Ring& ring,
+                              const PrimeConst* pc, cudaStream_t s) {
+  cudaError_t err = cudaSuccess;
+  db.njobs = 0;
+  for (int i = 0; i < n && err == cudaSuccess; i++)
+    for (int g = 0; g < gs && err == cudaSuccess; g += kDotG) {
+      db.jobs[db.njobs++] = DotJob{out(i, g), rot0(i), rot1(i), g, std::min(kDotG, gs - g), 0ull};
+      if (db.njobs == kMaxJobs) {
+        err = launch_ptdot(db, ring, pc, s);
+        db.njobs = 0;
+      }
+    }
+  if (err == cudaSuccess && db.njobs) err = launch_ptdot(db, ring, pc, s);
+  return err;
+}
+
 cudaError_t Context::linear_transform_batch(const u64* const* xs, int n, int t, const DevLT& lt, u64* const* outs,
                                             cudaStream_t s) {
   if (lt.ext) return linear_transform_ext_batch(xs, n, t, lt, outs, s);
@@ -763,24 +783,17 @@ cudaError_t Context::linear_transform_batch(const u64* const* xs, int n, int t, 
       }
     if (err == cudaSuccess) err = keyswitch_batch(rq.data(), (int)rq.size(), s);
   }
-  {  // inner sums: one job per (input, active giant step), up to kMaxJobs per launch
+  if (err == cudaSuccess) {  // inner sums: one job per (input, chunk of kDotG giant steps)
     DotBatch db{};
     db.rot_stride = (long long)CT;
+    db.out_stride = (long long)CT;
     db.pt_base = lt.diags;
     db.pt_stride = (long long)lt.rows * N;
-    db.present = lt.present_dev;
+    db.present = lt.present.data();
     db.bs = bs;
     db.t = t;
-    for (int i = 0; i < n && err == cudaSuccess; i++)
-      for (int g : active) {
-        db.jobs[db.njobs++] = DotJob{inner(i, g), xs[i], bs > 1 ? baby(i, 1) : nullptr, g};
-        if (db.njobs == kMaxJobs) {
-          err = launch_ptdot(db, ring_, d_pc, s);
-          db.njobs = 0;
-          if (err != cudaSuccess) break;
-        }
-      }
-    if (err == cudaSuccess && db.njobs) err = launch_ptdot(db, ring_, d_pc, s);
+    err = inner_sums(db, n, gs, [&](int i) { return xs[i]; }, [&](int i) { return bs > 1 ? baby(i, 1) : nullptr; },
+                     [&](int i, int g) { return inner(i, g); }, ring_, d_pc, s);
   }
   std::vector<int> nrot(n, 0);
   std::vector<std::vector<const u64*>> plain(n);
@@ -840,17 +853,17 @@ cudaError_t Context::linear_transform_ext_batch(const u64* const* xs, int n, int
     if (any) active.push_back(g);
   }
   const int na = (int)active.size();
-  // per input: bs baby ciphertexts (b = 0 is the input lifted by P), na inner sums, na rotated sums, the total
+  // per input: bs baby ciphertexts (b = 0 is the input lifted by P), gs inner sums, na rotated sums, the total
   // (all extended), and na ModDowned c1 polys (t limbs each)
-  const size_t per = (size_t)(bs + 2 * na + 1) * E + (size_t)na * t * NN;
+  const size_t per = (size_t)(bs + gs + na + 1) * E + (size_t)na * t * NN;
   u64* ws = alloc_limbs(per * n / NN, s);
   if (!ws) return cudaErrorMemoryAllocation;
   auto at = [&](int i) { return ws + (size_t)i * per; };
   auto baby = [&](int i, int b) { return at(i) + (size_t)b * E; };
-  auto inner = [&](int i, int k) { return at(i) + (size_t)(bs + k) * E; };
-  auto rotd = [&](int i, int k) { return at(i) + (size_t)(bs + na + k) * E; };
-  auto total = [&](int i) { return at(i) + (size_t)(bs + 2 * na) * E; };
-  auto c1d = [&](int i, int k) { return at(i) + (size_t)(bs + 2 * na + 1) * E + (size_t)k * t * NN; };
+  auto inner = [&](int i, int g) { return at(i) + (size_t)(bs + g) * E; };
+  auto rotd = [&](int i, int k) { return at(i) + (size_t)(bs + gs + k) * E; };
+  auto total = [&](int i) { return at(i) + (size_t)(bs + gs + na) * E; };
+  auto c1d = [&](int i, int k) { return at(i) + (size_t)(bs + gs + na + 1) * E + (size_t)k * t * NN; };
   cudaError_t err = cudaSuccess;
   {  // b = 0: (P x0, P x1) on the Q rows, zero on the special rows
     KsBatch kb{};
@@ -891,24 +904,18 @@ cudaError_t Context::linear_transform_ext_batch(const u64* const* xs, int n, int
   if (err == cudaSuccess) {  // inner sums in the extended basis
     DotBatch db{};
     db.rot_stride = (long long)E;
+    db.out_stride = (long long)E;
     db.pt_base = lt.diags;
     db.pt_stride = (long long)lt.rows * N;
-    db.present = lt.present_dev;
+    db.present = lt.present.data();
     db.bs = bs;
     db.t = t;
     db.np = np;
     db.nq = nq;
     db.pt_prow = lt.t;
-    for (int i = 0; i < n && err == cudaSuccess; i++)
-      for (int k = 0; k < na; k++) {
-        db.jobs[db.njobs++] = DotJob{inner(i, k), baby(i, 0), bs > 1 ? baby(i, 1) : nullptr, active[k]};
-        if (db.njobs == kMaxJobs) {
-          err = launch_ptdot(db, ring_, d_pc, s);
-          db.njobs = 0;
-          if (err != cudaSuccess) break;
-        }
-      }
-    if (err == cudaSuccess && db.njobs) err = launch_ptdot(db, ring_, d_pc, s);
+    err = inner_sums(db, n, gs, [&](int i) { return baby(i, 0); },
+                     [&](int i) { return bs > 1 ? baby(i, 1) : nullptr; }, [&](int i, int g) { return inner(i, g); },
+                     ring_, d_pc, s);
   }
   // giant steps: ModDown of each sum's c1, then its rotation without ModDown (c0 stays extended)
   std::vector<int> nrot(n, 0);
@@ -919,7 +926,7 @@ cudaError_t Context::linear_transform_ext_batch(const u64* const* xs, int n, int
     for (int k = 0; k < na; k++) {
       const int g = active[k];
       if (giant_r[g] == 0) {
-        plain[i].push_back(inner(i, k));
+        plain[i].push_back(inner(i, g));
         continue;
       }
       const uint32_t gl = galois_for_index(N, giant_r[g]);
@@ -928,8 +935,8 @@ cudaError_t Context::linear_transform_ext_batch(const u64* const* xs, int n, int
         err = cudaErrorInvalidValue;
         break;
       }
-      md.push_back(MdReq{inner(i, k) + (size_t)(t + np) * NN, t, 1, c1d(i, k)});
-      KsReq r{c1d(i, k), t, it->second, inner(i, k), nullptr, rotd(i, nrot[i]++), galois_inverse(gl)};
+      md.push_back(MdReq{inner(i, g) + (size_t)(t + np) * NN, t, 1, c1d(i, k)});
+      KsReq r{c1d(i, k), t, it->second, inner(i, g), nullptr, rotd(i, nrot[i]++), galois_inverse(gl)};
       r.ext_mode = 2;
       rq.push_back(r);
     }

@@ -430,34 +430,56 @@ __global__ void __launch_bounds__(kT) monomial_kernel(const __grid_constant__ Mo
   J.out[o] = v;
 }
 
-// grid rows per job: 2*(t+np) (poly-major; np = 0 outside the extended basis).
+// Inner sums: grid (N/256, 2 (t+np) njobs), ordered (row, job, poly) with the poly and the job fastest, so that
+// the blocks reading the same plaintext rows (both polys of every input of a batch) run back to back and share
+// them through L2.  A thread takes one coefficient of one poly for up to kDotG giant steps: each baby-step value
+// is read once, and four baby steps' loads (value and plaintexts) are issued before their products so that
+// enough loads are in flight to cover HBM latency.  One Acc4 per giant step holds at most 16 products (bs <= 16),
+// folded and reduced once at the end.
 __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBatch b, Ring r,
                                                    const PrimeConst* __restrict__ pc) {
-  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
-  const DotJob& J = b.jobs[z];
-  const int row = (int)blockIdx.y - b.row_begin[z];
-  const int t = b.t, rows = t + b.np, poly = row >= rows ? 1 : 0, j = row - poly * rows;
+  const int y = (int)blockIdx.y, poly = y & 1, job = (y >> 1) % b.njobs, j = (y >> 1) / b.njobs;
+  const DotJob& J = b.jobs[job];
+  const int t = b.t, rows = t + b.np;
   const int tower = j < t ? j : b.nq + (j - t), prow = j < t ? j : b.pt_prow + (j - t);
   const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
   const size_t co = ((size_t)poly * rows + j) * r.N + n, po = (size_t)prow * r.N + n;
-  u64 hi = 0, lo = 0;
-  Acc4 A{0, 0, 0, 0};
-  int terms = 0;
+  const unsigned long long pm = J.pmask;
+  Acc4 A[kDotG];
+#pragma unroll
+  for (int g = 0; g < kDotG; g++) A[g] = Acc4{0, 0, 0, 0};
 #pragma unroll 1
-  for (int bb = 0; bb < b.bs; bb++) {
-    const int i = J.g * b.bs + bb;
-    if (!b.present[i]) continue;
-    const u64* ct = bb == 0 ? J.rot0 : J.rot_base + (size_t)(bb - 1) * b.rot_stride;
-    const u64 x = ct[co], w = b.pt_base[(size_t)i * b.pt_stride + po];
-    acc4_mac(A, (uint32_t)(x & kMask30), (uint32_t)(x >> 30), (uint32_t)(w & kMask30), (uint32_t)(w >> 30));
-    if (++terms == 16) {
-      acc4_fold(A, hi, lo);
-      A = Acc4{0, 0, 0, 0};
-      terms = 0;
+  for (int b0 = 0; b0 < b.bs; b0 += 4) {
+    u64 x[4], w[4][kDotG];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int bb = b0 + u;
+      bool any = false;
+#pragma unroll
+      for (int g = 0; g < kDotG; g++) {
+        const bool on = bb < b.bs && ((pm >> (g * 16 + (bb & 15))) & 1ull);
+        any = any || on;
+        w[u][g] = on ? b.pt_base[(size_t)((J.g + g) * b.bs + bb) * b.pt_stride + po] : 0ull;
+      }
+      const u64* ct = bb == 0 ? J.rot0 : J.rot_base + (size_t)(bb - 1) * b.rot_stride;
+      x[u] = any ? ct[co] : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t xl = (uint32_t)(x[u] & kMask30), xh = (uint32_t)(x[u] >> 30);
+#pragma unroll
+      for (int g = 0; g < kDotG; g++)
+        acc4_mac(A[g], xl, xh, (uint32_t)(w[u][g] & kMask30), (uint32_t)(w[u][g] >> 30));
     }
   }
-  acc4_fold(A, hi, lo);
-  J.out[co] = reduce128_fast(hi, lo, pc[tower]);
+  const PrimeConst& P = pc[tower];
+#pragma unroll
+  for (int g = 0; g < kDotG; g++) {
+    if (g >= J.ng) break;
+    u64 hi = 0, lo = 0;
+    acc4_fold(A[g], hi, lo);
+    J.out[(size_t)g * b.out_stride + co] = reduce128_fast(hi, lo, P);
+  }
 }
 
 __global__ void __launch_bounds__(kT) sum_kernel(const __grid_constant__ SumBatch b, Ring r,
@@ -690,10 +712,17 @@ cudaError_t launch_monomial(const MonoBatch& b, const Ring& r, const PrimeConst*
 
 cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
   if (b.njobs <= 0) return cudaSuccess;
+  if (b.bs > 16) return cudaErrorInvalidValue;
   DotBatch bb = b;
-  bb.row_begin[0] = 0;
-  for (int i = 0; i < b.njobs; i++) bb.row_begin[i + 1] = bb.row_begin[i] + 2 * (b.t + b.np);
-  ptdot_kernel<<<dim3(r.N / kT, bb.row_begin[b.njobs], 1), kT, 0, s>>>(bb, r, pc);
+  for (int i = 0; i < b.njobs; i++) {
+    DotJob& J = bb.jobs[i];
+    if (J.ng < 1 || J.ng > kDotG) return cudaErrorInvalidValue;
+    J.pmask = 0;
+    for (int g = 0; g < J.ng; g++)
+      for (int k = 0; k < b.bs; k++)
+        if (b.present[(J.g + g) * b.bs + k]) J.pmask |= 1ull << (g * 16 + k);
+  }
+  ptdot_kernel<<<dim3(r.N / kT, 2 * (b.t + b.np) * b.njobs, 1), kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }

@@ -135,22 +135,28 @@ struct ScalarBatch {
   ScalarSet sets[kMaxScalarSets];
 };
 
-// Baby-step/giant-step inner sums: job (x, g) writes out[p][j] = sum_{b<bs, present} rot[b][p][j] (.) pt[g*bs+b][j]
-// with rot[0] = rot0 (the input itself), rot[b] = rot_base + (b-1)*rot_stride ([2][t][N] each) and
-// pt[i] = pt_base + i*pt_stride ([>=t][N] each).
+// Baby-step/giant-step inner sums: job (x, g, ng) writes, for the giant steps g .. g+ng-1,
+// out + k*out_stride ([2][rows][N]) = sum_{b<bs, present} rot[b] (.) pt[(g+k)*bs+b] with rot[0] = rot0 (the input
+// itself), rot[b] = rot_base + (b-1)*rot_stride ([2][rows][N] each) and pt[i] = pt_base + i*pt_stride.  One thread
+// reads each rot[b] value once for all ng giant steps (ng <= kDotG, bs <= 16); rows = t (+ np).  pmask bit
+// k*16 + b marks diagonal (g+k)*bs + b present (filled by launch_ptdot from `present`).
+constexpr int kDotG = 4;
 struct DotJob {
   u64* out;
   const u64* rot0;
   const u64* rot_base;
   int g;
+  int ng;
+  unsigned long long pmask;
 };
 struct DotBatch {
   int njobs;
   int row_begin[kMaxJobs + 1];
   long long rot_stride;
+  long long out_stride;
   const u64* pt_base;
   long long pt_stride;
-  const uint8_t* present;  // device [gs*bs]
+  const uint8_t* present;  // host [gs*bs] (read by launch_ptdot)
   int bs, t;
   // extended basis (np > 0): ciphertexts are [2][t+np][N], row t+k is special prime nq+k and reads plaintext
   // row pt_prow+k

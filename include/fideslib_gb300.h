@@ -197,8 +197,8 @@ int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* ou
 int fides_mod_raise(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out);
 /* Baby-step/giant-step linear transform (EvalLinearTransform, src/CKKS/LinearTransform.cu:63-256):
  * diags = u64[gs*bs][towers][N] evaluation form, diagonal i = g*bs + b already rotated by -g*bs;
- * present[i] = 0 marks a zero diagonal.  Needs rotation keys for 1..bs-1 and for g*bs.  `diags` may be host
- * or device memory (copied into the transform). */
+ * present[i] = 0 marks a zero diagonal; 1 <= bs <= 16, gs <= 64.  Needs rotation keys for 1..bs-1 and for g*bs.
+ * `diags` may be host or device memory (copied into the transform). */
 int fides_lt_create(fides_ctx* ctx, uint32_t bs, uint32_t gs, uint32_t towers, const uint64_t* diags,
                     const uint8_t* present, double scale, uint32_t* handle);
 /* The same over the diagonals at slot offsets base + k*stride (k = g*bs + b), the form of one level of a
