@@ -329,6 +329,7 @@ def run_ours(args, rank, world, dist):
     b.synchronize()
     hoisted_ms = a.elapsed_time(b) / reps
 
+    cfg1 = cfg1_bench(args, dev)
     served = None if args.no_served else served_bench(args, dev)
     boot = None if args.no_bootstrap else boot_bench(args, dev)
 
@@ -371,6 +372,7 @@ def run_ours(args, rank, world, dist):
                         "batched_over_per_op": round(hmult_per_op_ms / hmult_ms, 3)},
         "hoisted_cfg3a": {"ms_for_32_rotations": round(hoisted_ms, 4),
                           "ops_per_s": round(32 / (hoisted_ms / 1e3), 2)},
+        "hmult_cfg1": cfg1,
         "ntt_cfg2": ntt["summary"],
         "ntt_autotune_n16": ctx.ntt_tuning(),
         "roofline": ntt["roofline"],
@@ -379,6 +381,77 @@ def run_ours(args, rank, world, dist):
         "clocks": clocks,
     }
     return result
+
+
+def cfg1_bench(args, dev):
+    """Config 1: HMult + relinearisation + Rescale of one ciphertext pair at N = 2^13, 6 towers (one 60-bit and five
+    40-bit primes), dnum 2, three 60-bit special primes: the latency of one op on the per-op path (CUDA events
+    around each call, 200 calls), and 64 pairs as one batch."""
+    import torch
+
+    import fideslib_gb300 as F
+    logn, n13, nq, npr, dnum = 13, 1 << 13, 6, 3, 2
+    mods = gen_primes_host(60, 1, 2 * n13)
+    mods += gen_primes_host(40, nq - 1, 2 * n13, exclude=mods)
+    mods += gen_primes_host(60, npr, 2 * n13, exclude=mods)
+    ctx = F.CryptoContext(logn, mods, npr, dnum)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0x5EED0001)
+    modt = torch.tensor(mods, dtype=torch.int64, device=dev)
+    k = torch.randint(0, 1 << 62, (2, dnum, nq + npr, n13), dtype=torch.int64, device=dev, generator=gen)
+    ctx.load_eval_mult_key_device((k % modt.view(1, 1, -1, 1)).data_ptr())
+    hs = []
+    for _ in range(128):
+        x = torch.randint(0, 1 << 62, (2, nq, n13), dtype=torch.int64, device=dev, generator=gen) % modt[:nq].view(1, -1, 1)
+        hs.append(ctx.load_ciphertext_device(x.data_ptr(), nq, scale=2.0 ** 40))
+    torch.cuda.synchronize()
+
+    def one(i):
+        p = ctx.eval_mult(hs[2 * i], hs[2 * i + 1])
+        r = ctx.rescale(p)
+        ctx.free(p)
+        ctx.free(r)
+
+    for i in range(20):
+        one(i % 64)
+    torch.cuda.synchronize()
+    lat = []
+    for i in range(200):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        one(i % 64)
+        b.record(stream)
+        b.synchronize()
+        lat.append(a.elapsed_time(b))
+    lat.sort()
+    t0 = time.perf_counter()
+    for i in range(200):
+        one(i % 64)
+    torch.cuda.synchronize()
+    per_op_ms = (time.perf_counter() - t0) * 1e3 / 200
+
+    def batched():
+        prods = ctx.eval_batch([(F.OP_MULT, hs[2 * i], hs[2 * i + 1], 0) for i in range(64)])
+        outs = ctx.eval_batch([(F.OP_RESCALE, p, 0, 0) for p in prods])
+        for o in prods + outs:
+            ctx.free(o)
+
+    for _ in range(3):
+        batched()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(10):
+        batched()
+    b.record(stream)
+    b.synchronize()
+    batch_ms = a.elapsed_time(b) / 10
+    ctx.close()
+    return {"workload": "cfg1: HMult + relinearise + Rescale, N=2^13, 6 towers (60 + 5 x 40 bits), dnum 2, 3 special",
+            "latency_ms_p50": round(lat[len(lat) // 2], 4), "latency_ms_p99": round(lat[int(0.99 * len(lat))], 4),
+            "per_op_ops_per_s": round(1e3 / per_op_ms, 1),
+            "batched_64_ops_per_s": round(64 / (batch_ms / 1e3), 1)}
 
 
 def served_bench(args, dev):

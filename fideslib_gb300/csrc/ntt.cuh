@@ -54,7 +54,7 @@ cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, c
 // stream-ordered pool, synchronising `s`) — a small one (32 limbs' worth of residues at N = 2^16) and a large one
 // (640 limbs' worth) — for both directions, and stores the fastest variant of each in t.fwd_variant_small /
 // t.fwd_variant / t.inv_variant_small / t.inv_variant.  The times in ms (forward small v0..v2, forward large
-// v0..v2, inverse small v0..v1, inverse large v0..v1) are written to ms[0..9] when ms is non-null (-1 where a
+// v0..v2, inverse small v0..v2, inverse large v0..v2) are written to ms[0..11] when ms is non-null (-1 where a
 // single kernel applies).
 cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms);
 
