@@ -423,13 +423,14 @@ class CryptoContext:
 
     def ntt_tuning(self) -> dict:
         """The forward-NTT variants the autotuner chose at creation (small / large launches) and the timings."""
-        v = (C.c_int32 * 4)()
-        ms = (C.c_float * 12)()
+        v = (C.c_int32 * 6)()
+        ms = (C.c_float * 18)()
         _check(lib().fides_ctx_ntt_tuning(self._h, v, ms))
         r = lambda a, b: [round(ms[i], 4) for i in range(a, b)]  # noqa: E731
-        return {"fwd_variant_small": v[0], "fwd_variant_large": v[1], "inv_variant_small": v[2],
-                "inv_variant_large": v[3], "fwd_ms_small": r(0, 3), "fwd_ms_large": r(3, 6),
-                "inv_ms_small": r(6, 9), "inv_ms_large": r(9, 12)}
+        return {"fwd_variant_tiny": v[0], "fwd_variant_small": v[1], "fwd_variant_large": v[2],
+                "inv_variant_tiny": v[3], "inv_variant_small": v[4], "inv_variant_large": v[5],
+                "fwd_ms_tiny": r(0, 3), "fwd_ms_small": r(3, 6), "fwd_ms_large": r(6, 9),
+                "inv_ms_tiny": r(9, 12), "inv_ms_small": r(12, 15), "inv_ms_large": r(15, 18)}
 
     def set_mem_limit(self, nbytes: int):
         _check(lib().fides_ctx_set_mem_limit(self._h, nbytes))

@@ -79,13 +79,16 @@ int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
   const fgb::DeviceTables& t = ctx->c->tabs;
   if (variant) {
-    variant[0] = t.fwd_variant_small;
-    variant[1] = t.fwd_variant;
-    variant[2] = t.inv_variant_small;
-    variant[3] = t.inv_variant;
+    variant[0] = t.fwd_variant_tiny;
+    variant[1] = t.fwd_variant_small;
+    variant[2] = t.fwd_variant;
+    variant[3] = t.inv_variant_tiny;
+    variant[4] = t.inv_variant_small;
+    variant[5] = t.inv_variant;
   }
   if (ms)
-    for (int i = 0; i < 2 * (fgb::kNttFwdVariants + fgb::kNttInvVariants); i++) ms[i] = ctx->c->ntt_tune_ms[i];
+    for (int i = 0; i < fgb::kNttSizeClasses * (fgb::kNttFwdVariants + fgb::kNttInvVariants); i++)
+      ms[i] = ctx->c->ntt_tune_ms[i];
   return FIDES_OK;
 }
 
@@ -105,13 +108,13 @@ int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant, int32_t inv_va
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
   if (fwd_variant < 0 || fwd_variant >= fgb::kNttFwdVariants || inv_variant < 0 ||
       inv_variant >= fgb::kNttInvVariants)
-    return fail(FIDES_EINVAL, "forward variant must be 0, 1 or 2 and inverse variant 0 or 1");
+    return fail(FIDES_EINVAL, "forward and inverse variants must be 0, 1 or 2");
   if (ctx->c->logN < 13 && (fwd_variant != 1 || inv_variant != 0))
     return fail(FIDES_EINVAL, "below N = 2^13 only forward variant 1 and inverse variant 0 exist");
   cudaStreamSynchronize(ctx->c->stream);
   fgb::DeviceTables& t = ctx->c->tabs;
-  t.fwd_variant = t.fwd_variant_small = fwd_variant;
-  t.inv_variant = t.inv_variant_small = inv_variant;
+  t.fwd_variant = t.fwd_variant_small = t.fwd_variant_tiny = fwd_variant;
+  t.inv_variant = t.inv_variant_small = t.inv_variant_tiny = inv_variant;
   return FIDES_OK;
 }
 

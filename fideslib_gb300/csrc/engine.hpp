@@ -73,7 +73,7 @@ class Context {
   cudaStream_t copy_in = nullptr, copy_out = nullptr;  // copy streams of the pipelined host batch (lazily made)
 
   DeviceTables tabs{};
-  float ntt_tune_ms[2 * (kNttFwdVariants + kNttInvVariants)] = {};  // tune_ntt timings
+  float ntt_tune_ms[kNttSizeClasses * (kNttFwdVariants + kNttInvVariants)] = {};  // tune_ntt timings
   CrtTables crt{};
   PrimeConst* d_pc = nullptr;
 

@@ -558,8 +558,10 @@ cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cud
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   if (b.njobs <= 0 || b.limb_begin[b.njobs] <= 0) return cudaSuccess;
   if (b.njobs > kMaxNttJobs || b.limb_begin[b.njobs] > 65535) return cudaErrorInvalidValue;
-  const bool small = ((long long)b.limb_begin[b.njobs] << t.logN) <= kSmallNttWork;
-  const int v = inverse ? (small ? t.inv_variant_small : t.inv_variant) : (small ? t.fwd_variant_small : t.fwd_variant);
+  const long long work = (long long)b.limb_begin[b.njobs] << t.logN;
+  const int cls = work <= kTinyNttWork ? 0 : work <= kSmallNttWork ? 1 : 2;
+  const int v = inverse ? (cls == 0 ? t.inv_variant_tiny : cls == 1 ? t.inv_variant_small : t.inv_variant)
+                        : (cls == 0 ? t.fwd_variant_tiny : cls == 1 ? t.fwd_variant_small : t.fwd_variant);
   switch (t.logN) {
     case 10: return launch_t<10>(b, t, inverse, s);
     case 11: return launch_t<11>(b, t, inverse, s);
@@ -592,12 +594,14 @@ cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, c
 }
 
 cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
-  constexpr int kSlots = 2 * (kNttFwdVariants + kNttInvVariants);
+  constexpr int kSlots = kNttSizeClasses * (kNttFwdVariants + kNttInvVariants);
   if (ms)
     for (int i = 0; i < kSlots; i++) ms[i] = -1.f;
   if (t.logN < 13) return cudaSuccess;  // one kernel per direction below 2^13
   const size_t n = (size_t)1 << t.logN;
-  const int small = (int)((32ll << 16) >> t.logN), large = (int)((640ll << 16) >> t.logN);
+  const int sizes[kNttSizeClasses] = {(int)((8ll << 16) >> t.logN), (int)((32ll << 16) >> t.logN),
+                                      (int)((640ll << 16) >> t.logN)};
+  const int large = sizes[kNttSizeClasses - 1];
   u64* buf = nullptr;
   cudaError_t e = cudaMallocAsync(&buf, (size_t)large * n * sizeof(u64), s);
   if (e != cudaSuccess) return e;
@@ -605,18 +609,19 @@ cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
   cudaEvent_t ev[2];
   cudaEventCreate(&ev[0]);
   cudaEventCreate(&ev[1]);
-  int slot = 0;  // ms layout: forward small, forward large, inverse small, inverse large
+  int slot = 0;  // ms layout: forward tiny, small, large, then inverse tiny, small, large
   for (int inverse = 0; inverse < 2 && e == cudaSuccess; inverse++) {
     const int nv = inverse ? kNttInvVariants : kNttFwdVariants;
-    for (int size = 0; size < 2 && e == cudaSuccess; size++) {
+    for (int size = 0; size < kNttSizeClasses && e == cudaSuccess; size++) {
       NttBatch b{};
       uint8_t pm[1] = {0};
-      ntt_add_job(b, buf, buf, (long long)n, (long long)n, 1, size ? large : small, pm);
+      ntt_add_job(b, buf, buf, (long long)n, (long long)n, 1, sizes[size], pm);
       float best = 0;
       int pick = 0;
       for (int v = 0; v < nv && e == cudaSuccess; v++, slot++) {
         DeviceTables tv = t;
-        tv.fwd_variant = tv.fwd_variant_small = tv.inv_variant = tv.inv_variant_small = v;
+        tv.fwd_variant = tv.fwd_variant_small = tv.fwd_variant_tiny = v;
+        tv.inv_variant = tv.inv_variant_small = tv.inv_variant_tiny = v;
         e = launch_ntt(b, tv, inverse, s);  // warm-up
         if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
         for (int r = 0; r < 3 && e == cudaSuccess; r++) e = launch_ntt(b, tv, inverse, s);
@@ -632,8 +637,9 @@ cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
         }
       }
       if (e == cudaSuccess) {
-        int& dst = inverse ? (size ? t.inv_variant : t.inv_variant_small) : (size ? t.fwd_variant : t.fwd_variant_small);
-        dst = pick;
+        int* dst[2][kNttSizeClasses] = {{&t.fwd_variant_tiny, &t.fwd_variant_small, &t.fwd_variant},
+                                        {&t.inv_variant_tiny, &t.inv_variant_small, &t.inv_variant}};
+        *dst[inverse][size] = pick;
       }
     }
   }

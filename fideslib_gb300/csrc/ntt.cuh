@@ -37,25 +37,28 @@ struct DeviceTables {
   int logN;
   // forward kernel for N >= 2^13 (0 = radix-16 with 8192 residues per CTA; 1 = radix-32/16; 2 = radix-16 with 4096
   // residues per CTA, twice the CTAs per limb), chosen by tune_ntt separately for launches of at most
-  // kSmallNttWork residues (latency-bound) and larger ones (throughput-bound)
+  // kTinyNttWork residues (one op: latency-bound), at most kSmallNttWork and larger ones (throughput-bound)
   int fwd_variant = 0;
   int fwd_variant_small = 0;
-  int inv_variant = 0;  // inverse: 0 = radix-32/16, 1 = radix-16 with 4096 residues per CTA
+  int fwd_variant_tiny = 0;
+  int inv_variant = 0;  // inverse: 0 = radix-32/16, 1 = radix-16 with 4096, 2 = with 8192 residues per CTA
   int inv_variant_small = 0;
+  int inv_variant_tiny = 0;
 };
 constexpr int kNttFwdVariants = 3;
 constexpr int kNttInvVariants = 3;
-constexpr long long kSmallNttWork = 128ll << 16;  // residues per launch (128 limbs at N = 2^16)
+constexpr int kNttSizeClasses = 3;                // tiny, small, large
+constexpr long long kTinyNttWork = 16ll << 16;    // residues per launch (16 limbs at N = 2^16)
+constexpr long long kSmallNttWork = 128ll << 16;  // 128 limbs at N = 2^16
 
 // Forward (inverse=false: coefficient -> evaluation, bit-reversed) or inverse transform of every job.
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s);
 
-// Autotuner: times the forward kernel variants on scratch batches of this ring (device memory from the
-// stream-ordered pool, synchronising `s`) — a small one (32 limbs' worth of residues at N = 2^16) and a large one
-// (640 limbs' worth) — for both directions, and stores the fastest variant of each in t.fwd_variant_small /
-// t.fwd_variant / t.inv_variant_small / t.inv_variant.  The times in ms (forward small v0..v2, forward large
-// v0..v2, inverse small v0..v2, inverse large v0..v2) are written to ms[0..11] when ms is non-null (-1 where a
-// single kernel applies).
+// Autotuner: times every kernel variant of both directions on scratch batches of this ring (device memory from the
+// stream-ordered pool, synchronising `s`) of 8, 32 and 640 limbs' worth of residues at N = 2^16 (tiny, small,
+// large) and stores the fastest variant of each class in t.*_variant_tiny / *_small / *_variant.  The times in ms
+// (forward tiny v0..v2, small v0..v2, large v0..v2, then the same for the inverse) are written to
+// ms[0..2*3*3-1] when ms is non-null (-1 where a single kernel applies).
 cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms);
 
 // Job owning flattened row `row` of a prefix-sum table begin[0..njobs] (uniform per block / cluster).

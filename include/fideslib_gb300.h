@@ -85,13 +85,13 @@ int fides_synchronize(fides_ctx* ctx);
 void* fides_ctx_stream(fides_ctx* ctx);
 int fides_ctx_set_stream(fides_ctx* ctx, void* stream);
 /* The NTT autotuner's choices for this ring (no counterpart in the reference, whose NTT kernels are fixed at build
- * time): at context creation every forward and inverse kernel variant is timed on a small and a large scratch
- * batch (32 and 640 limbs' worth of residues at N = 2^16) and the fastest one of each is used for launches of at
- * most / more than 128 limbs' worth (the key-switch stages of single ops / of batches).  variant[0..3] = forward
- * small, forward large, inverse small, inverse large; forward variants: 0 = radix-16 passes with 8192 residues
- * per CTA, 1 = radix-32/16 passes, 2 = radix-16 passes with 4096 residues per CTA (twice the CTAs per limb);
- * inverse: 0 = radix-32/16, 1 = radix-16 with 4096 per CTA, 2 = radix-16 with 8192 per CTA.  ms[0..11] =
- * forward small v0..v2, forward large v0..v2, inverse small v0..v2, inverse large v0..v2 (-1 where a single
+ * time): at context creation every forward and inverse kernel variant is timed on a tiny, a small and a large
+ * scratch batch (8, 32 and 640 limbs' worth of residues at N = 2^16) and the fastest one of each is used for
+ * launches of at most 16 limbs' worth (one op: latency-bound), at most 128 limbs' worth and more (batches).
+ * variant[0..5] = forward tiny, small, large, inverse tiny, small, large; forward variants: 0 = radix-16 passes
+ * with 8192 residues per CTA, 1 = radix-32/16 passes, 2 = radix-16 passes with 4096 residues per CTA (twice the
+ * CTAs per limb); inverse: 0 = radix-32/16, 1 = radix-16 with 4096 per CTA, 2 = radix-16 with 8192 per CTA.
+ * ms[0..17] = forward tiny v0..v2, small v0..v2, large v0..v2, then the inverse the same way (-1 where a single
  * kernel applies, N < 2^13). */
 int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms);
 /* Device-memory budget of the context (the reference's pool has a release threshold only, Context.cu:74-80):

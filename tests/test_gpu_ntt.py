@@ -85,9 +85,9 @@ def test_all_ntt_variants_and_autotuner(engine_lib, logN):
     N = 1 << logN
     ctx, mods = make_ctx(logN, 2, bits=60)
     tune = ctx.ntt_tuning()
-    assert tune["fwd_variant_small"] in (0, 1, 2) and tune["fwd_variant_large"] in (0, 1, 2)
-    assert tune["inv_variant_small"] in (0, 1, 2) and tune["inv_variant_large"] in (0, 1, 2)
-    assert min(tune["fwd_ms_small"] + tune["fwd_ms_large"] + tune["inv_ms_small"] + tune["inv_ms_large"]) > 0
+    for cls in ("tiny", "small", "large"):
+        assert tune[f"fwd_variant_{cls}"] in (0, 1, 2) and tune[f"inv_variant_{cls}"] in (0, 1, 2)
+        assert min(tune[f"fwd_ms_{cls}"] + tune[f"inv_ms_{cls}"]) > 0
     rng = np.random.default_rng(logN + 100)
     data = np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(2)])[None]
     data[0, 0, :7] = mods[0] - 1
