@@ -264,6 +264,7 @@ static int load_key(fides_ctx* ctx, const uint64_t* key, bool device, fgb::u64**
   }
   CK(cudaMemcpyAsync(*slot, key, bytes, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
      "key copy");
+  CK(fgb::launch_key_split(*slot, bytes / sizeof(uint64_t), c->stream), "key layout");
   CK(cudaStreamSynchronize(c->stream), "key copy");
   return FIDES_OK;
 }

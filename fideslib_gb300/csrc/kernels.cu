@@ -151,17 +151,18 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
 #undef FGB_MODUP_CASE
 }
 
-// Key inner product: grid (N/512, rows), two coefficients per thread (16-byte loads).  Jobs are grouped by key;
-// group g owns (tmax_g + np) * m_g rows, tmax_g its largest tower count and m_g its job count, ordered (tower row,
-// job) with the job fastest, so the m_g blocks that read the same key values are scheduled back to back and a key
-// shared by several ciphertexts (one rotation of a lock-step batch, the relinearisation key of a batch of
-// products) is read from HBM about once, the other reads hitting L2.  A block whose tower lies above its job's
-// level exits.  Every digit's value and both key halves are loaded before any arithmetic (3 beta loads in
-// flight); digits and key values are split into 30-bit halves and accumulated in one Acc4 per half-key (at most
-// 8 digits, 16 terms max); MAXB bounds beta at compile time.
+// Key inner product: grid (N / (512 iters), rows); a thread takes `iters` pairs of coefficients (16-byte loads),
+// with its job, tower and row pointers worked out once.  Jobs are grouped by key; group g owns (tmax_g + np) * m_g
+// rows, tmax_g its largest tower count and m_g its job count, ordered (tower row, job) with the job fastest, so the
+// m_g blocks that read the same key values are scheduled back to back and a key shared by several ciphertexts (one
+// rotation of a lock-step batch, the relinearisation key of a batch of products) is read from HBM about once, the
+// other reads hitting L2.  A block whose tower lies above its job's level exits.  Every digit's value and both key
+// halves are loaded before any arithmetic; digits are split into 30-bit halves here and key values come split
+// (launch_key_split), accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max); MAXB bounds beta at
+// compile time.  Outputs are left in [0, 4p): the ModDown INTT takes them as they are and both epilogues reduce.
 template <int MAXB>
-__global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
-                                                      const PrimeConst* __restrict__ pc) {
+__global__ void __launch_bounds__(kT, 2) ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
+                                                         const PrimeConst* __restrict__ pc, int iters) {
   const int G = find_job(b.row_begin, b.ngroups, (int)blockIdx.y);
   const int m = b.grp_begin[G + 1] - b.grp_begin[G];
   const int local = (int)blockIdx.y - b.row_begin[G];
@@ -172,43 +173,66 @@ __global__ void __launch_bounds__(kT) ks_inner_kernel(const __grid_constant__ Ks
   const int tower = rr < tmax ? rr : c.nq + (rr - tmax);
   if (tower < c.nq && tower >= t) return;  // a Q tower above this job's level
   const int ext = t + c.np, j = tower < c.nq ? tower : t + (tower - c.nq);
-  const int n = (blockIdx.x * kT + threadIdx.x) * 2;
   const size_t N = r.N;
   const int beta = (t + c.alpha - 1) / c.alpha;
-  ulonglong2 D[MAXB], KA[MAXB], KB[MAXB];
+  const size_t khalf = (size_t)c.dnum * c.ntow * N, kstep = (size_t)c.ntow * N;
+  const u64* src[MAXB];
+  const u64* key = J.key + (size_t)tower * N;
 #pragma unroll
   for (int d = 0; d < MAXB; d++) {
     if (d >= beta) break;
     const int start = d * c.alpha;
     const int s = min(c.alpha, t - start);
-    const u64* src;
     if (j >= start && j < start + s) {
-      src = J.a + (size_t)j * N;
+      src[d] = J.a + (size_t)j * N;
     } else {
       const int jj = j < start ? j : j - s;
-      src = J.conv + ((size_t)d * ext + jj) * N;
+      src[d] = J.conv + ((size_t)d * ext + jj) * N;
     }
-    D[d] = *reinterpret_cast<const ulonglong2*>(src + n);
-    KA[d] = *reinterpret_cast<const ulonglong2*>(J.key + ((size_t)(0 * c.dnum + d) * c.ntow + tower) * N + n);
-    KB[d] = *reinterpret_cast<const ulonglong2*>(J.key + ((size_t)(1 * c.dnum + d) * c.ntow + tower) * N + n);
   }
+  u64* out0 = J.inner + (size_t)j * N;
+  u64* out1 = J.inner + ((size_t)ext + j) * N;
   const PrimeConst& P = pc[tower];
-#pragma unroll
-  for (int e = 0; e < 2; e++) {
-    Acc4 A0{0, 0, 0, 0}, A1{0, 0, 0, 0};
+  const u64 p4 = 4 * P.p;
+#pragma unroll 1
+  for (int it = 0; it < iters; it++) {
+    const int n = (((int)blockIdx.x * iters + it) * kT + (int)threadIdx.x) * 2;
+    ulonglong2 D[MAXB], KA[MAXB], KB[MAXB];
 #pragma unroll
     for (int d = 0; d < MAXB; d++) {
       if (d >= beta) break;
-      const u64 Dv = e ? D[d].y : D[d].x, ka = e ? KA[d].y : KA[d].x, kb = e ? KB[d].y : KB[d].x;
-      const uint32_t dl = (uint32_t)(Dv & kMask30), dh = (uint32_t)(Dv >> 30);
-      acc4_mac(A0, dl, dh, (uint32_t)(kb & kMask30), (uint32_t)(kb >> 30));
-      acc4_mac(A1, dl, dh, (uint32_t)(ka & kMask30), (uint32_t)(ka >> 30));
+      D[d] = *reinterpret_cast<const ulonglong2*>(src[d] + n);
+      KA[d] = *reinterpret_cast<const ulonglong2*>(key + d * kstep + n);
+      KB[d] = *reinterpret_cast<const ulonglong2*>(key + d * kstep + khalf + n);
     }
-    u64 h0 = 0, l0 = 0, h1 = 0, l1 = 0;
-    acc4_fold(A0, h0, l0);
-    acc4_fold(A1, h1, l1);
-    J.inner[(size_t)j * N + n + e] = reduce128_fast(h0, l0, P);
-    J.inner[((size_t)ext + j) * N + n + e] = reduce128_fast(h1, l1, P);
+    u64 v0[2], v1[2];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      Acc4 A0{0, 0, 0, 0}, A1{0, 0, 0, 0};
+#pragma unroll
+      for (int d = 0; d < MAXB; d++) {
+        if (d >= beta) break;
+        const u64 Dv = e ? D[d].y : D[d].x, ka = e ? KA[d].y : KA[d].x, kb = e ? KB[d].y : KB[d].x;
+        const uint32_t dl = (uint32_t)(Dv & kMask30), dh = (uint32_t)(Dv >> 30);
+        acc4_mac(A0, dl, dh, (uint32_t)kb, (uint32_t)(kb >> 32));
+        acc4_mac(A1, dl, dh, (uint32_t)ka, (uint32_t)(ka >> 32));
+      }
+      u64 h0 = 0, l0 = 0, h1 = 0, l1 = 0;
+      acc4_fold(A0, h0, l0);
+      acc4_fold(A1, h1, l1);
+      v0[e] = csub(reduce128_lazy8(h0, l0, P), p4);
+      v1[e] = csub(reduce128_lazy8(h1, l1, P), p4);
+    }
+    *reinterpret_cast<ulonglong2*>(out0 + n) = make_ulonglong2(v0[0], v0[1]);
+    *reinterpret_cast<ulonglong2*>(out1 + n) = make_ulonglong2(v1[0], v1[1]);
+  }
+}
+
+// Keys in the form the inner product reads: residue k (< 2^60) stored as (k mod 2^30) | (floor(k / 2^30) << 32).
+__global__ void __launch_bounds__(kT) key_split_kernel(u64* __restrict__ k, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * kT + threadIdx.x; i < n; i += (size_t)gridDim.x * kT) {
+    const u64 v = k[i];
+    k[i] = (v & kMask30) | ((v >> 30) << 32);
   }
 }
 
@@ -240,7 +264,7 @@ __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant_
   conv_rows<K>(yl, yh, cs, t, J.md + (size_t)poly * t * r.N + n, (size_t)r.N, pc, [](int j) { return j; });
 }
 
-// out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/256, nq, 2*njobs).
+// out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/512, rows); inner_Q arrives in [0, 4p).
 __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_constant__ KsBatch b, Ring r,
                                                               CrtTables c, const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
@@ -251,7 +275,8 @@ __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_const
   const size_t N = r.N;
   const u64 q = pc[j].p;
   const ulonglong2 w = c.md_pinv[j];
-  const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(J.inner + ((size_t)poly * (t + c.np) + j) * N + n);
+  ulonglong2 x = *reinterpret_cast<const ulonglong2*>(J.inner + ((size_t)poly * (t + c.np) + j) * N + n);
+  x = make_ulonglong2(csub(csub(x.x, 2 * q), q), csub(csub(x.y, 2 * q), q));  // inner products are in [0, 4p)
   const ulonglong2 y = *reinterpret_cast<const ulonglong2*>(J.md + ((size_t)poly * t + j) * N + n);
   const u64* add = poly == 0 ? J.add0 : J.add1;
   const ulonglong2 a = add ? *reinterpret_cast<const ulonglong2*>(add + (size_t)j * N + n) : make_ulonglong2(0, 0);
@@ -286,6 +311,7 @@ __global__ void __launch_bounds__(kT) ext_epilogue_kernel(const __grid_constant_
   const size_t N = r.N;
   ulonglong2 v = J.inner ? *reinterpret_cast<const ulonglong2*>(J.inner + ((size_t)poly * ext + j) * N + n)
                          : make_ulonglong2(0, 0);
+  v = make_ulonglong2(csub(csub(v.x, 2 * q), q), csub(csub(v.y, 2 * q), q));  // inner products are in [0, 4p)
   const u64* add = poly == 0 ? J.add0 : J.add1;
   if (add && J.ext_mode == 2) {
     const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(add + (size_t)j * N + n);
@@ -576,11 +602,12 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
     bb.row_begin[++bb.ngroups] = rows;
   }
   bb.grp_begin[bb.ngroups] = k;
-  dim3 grid(r.N / (2 * kT), rows, 1);
+  const int iters = std::min(4, r.N / (2 * kT));  // N / 512 is a power of two >= 2
+  dim3 grid(r.N / (2 * kT * iters), rows, 1);
   switch (c.dnum) {  // beta <= dnum: size the register arrays exactly (fewer registers, more resident warps)
-#define FGB_KSI_CASE(B_)                                   \
-  case B_:                                                 \
-    ks_inner_kernel<B_><<<grid, kT, 0, s>>>(bb, r, c, pc); \
+#define FGB_KSI_CASE(B_)                                          \
+  case B_:                                                        \
+    ks_inner_kernel<B_><<<grid, kT, 0, s>>>(bb, r, c, pc, iters); \
     break;
     FGB_KSI_CASE(1) FGB_KSI_CASE(2) FGB_KSI_CASE(3) FGB_KSI_CASE(4) FGB_KSI_CASE(5) FGB_KSI_CASE(6)
     FGB_KSI_CASE(7) FGB_KSI_CASE(8)
@@ -588,6 +615,12 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
     default:
       return cudaErrorInvalidValue;
   }
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_key_split(u64* key, size_t n, cudaStream_t s) {
+  key_split_kernel<<<1024, kT, 0, s>>>(key, n);
   count_launch();
   return cudaGetLastError();
 }

@@ -38,7 +38,7 @@ struct KsJob {
   const u64* a;      // [t][N] evaluation form (the digit's own towers are read from here)
   const u64* add0;   // [t][N] or null
   const u64* add1;   // [t][N] or null
-  const u64* key;    // [2][dnum][ntow][N] (0 = a vectors, 1 = b vectors)
+  const u64* key;    // [2][dnum][ntow][N] (0 = a vectors, 1 = b vectors), split form (launch_key_split)
   const u64* coeff;  // [t][N] coefficient form of a (ModUp input)
   u64* conv;         // digit d: conv + d*(t+np)*N, rows = the t - s_d + np converted towers
   u64* inner;        // [2][t+np][N]
@@ -225,6 +225,8 @@ cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTa
                                     cudaStream_t s);
 cudaError_t launch_ext_epilogue(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                                 cudaStream_t s);
+// In place: every key residue k becomes (k mod 2^30) | (floor(k / 2^30) << 32), the form ks_inner_kernel reads.
+cudaError_t launch_key_split(u64* key, size_t n, cudaStream_t s);
 cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, const PrimeConst* pc,
