@@ -161,8 +161,9 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
 // (launch_key_split), accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max); MAXB bounds beta at
 // compile time.  Outputs are left in [0, 4p): the ModDown INTT takes them as they are and both epilogues reduce.
 template <int MAXB>
-__global__ void __launch_bounds__(kT, 2) ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
-                                                         const PrimeConst* __restrict__ pc, int iters) {
+__global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
+    ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c, const PrimeConst* __restrict__ pc,
+                    int iters) {
   const int G = find_job(b.row_begin, b.ngroups, (int)blockIdx.y);
   const int m = b.grp_begin[G + 1] - b.grp_begin[G];
   const int local = (int)blockIdx.y - b.row_begin[G];
