@@ -63,52 +63,90 @@ __device__ __forceinline__ int conv_tower(int jj, int start, int s, int t, int n
 }
 
 // ---------------------------------------------------------------------------------------------------------
-// Basis conversion core: for one coefficient, outputs sum_{i<S} y_i * c_{i,jj} mod m_jj for jj < nout, with the
-// S inputs y_i (already multiplied by the Qhat^-1 / Phat^-1 factor) held in registers as 30-bit halves and the
-// constants c_{i,jj} staged in shared memory as 30-bit halves.  S is a compile-time constant so no multiply-add
-// is issued for absent towers.  Every output feeds a forward NTT, which accepts residues in [0, 8p), so the
-// outputs are left unreduced in that range (the NTT's own output is fully reduced).
-template <int S, class TowerOf>
-__device__ __forceinline__ void conv_rows(const uint32_t (&yl)[S], const uint32_t (&yh)[S], const uint2* cs, int nout,
-                                          u64* out, size_t stride, const PrimeConst* __restrict__ pc, TowerOf tower_of) {
+// Basis conversion core: for NC adjacent coefficients (NC = 1 or 2), outputs sum_{i<S} y_i * c_{i,jj} mod m_jj for
+// jj < nout, with the S inputs y_i (already multiplied by the Qhat^-1 / Phat^-1 factor) held in registers as 30-bit
+// halves and the constants c_{i,jj} staged in shared memory as 30-bit halves (one shared load serves the NC
+// coefficients).  S is a compile-time constant so no multiply-add is issued for absent towers.  Every output feeds
+// a forward NTT, which accepts residues in [0, 8p), so the outputs are left unreduced in that range (the NTT's own
+// output is fully reduced).
+template <int S, int NC, class TowerOf>
+__device__ __forceinline__ void conv_rows(const uint32_t (&yl)[NC][S], const uint32_t (&yh)[NC][S], const uint2* cs,
+                                          int nout, u64* out, size_t stride, const PrimeConst* __restrict__ pc,
+                                          TowerOf tower_of) {
 #pragma unroll 1
   for (int jj = 0; jj < nout; jj++) {
-    u64 hi = 0, lo = 0;
+    u64 hi[NC], lo[NC];
+#pragma unroll
+    for (int k = 0; k < NC; k++) hi[k] = lo[k] = 0;
 #pragma unroll
     for (int i0 = 0; i0 < S; i0 += 16) {
-      Acc4 A{0, 0, 0, 0};
+      Acc4 A[NC];
+#pragma unroll
+      for (int k = 0; k < NC; k++) A[k] = Acc4{0, 0, 0, 0};
 #pragma unroll
       for (int i = i0; i < i0 + 16 && i < S; i++) {
         const uint2 cc = cs[i * nout + jj];
-        acc4_mac(A, yl[i], yh[i], cc.x, cc.y);
+#pragma unroll
+        for (int k = 0; k < NC; k++) acc4_mac(A[k], yl[k][i], yh[k][i], cc.x, cc.y);
       }
-      acc4_fold(A, hi, lo);
+#pragma unroll
+      for (int k = 0; k < NC; k++) acc4_fold(A[k], hi[k], lo[k]);
     }
-    out[(size_t)jj * stride] = reduce128_lazy8(hi, lo, pc[tower_of(jj)]);
+    const PrimeConst& P = pc[tower_of(jj)];
+    if constexpr (NC == 2)
+      *reinterpret_cast<ulonglong2*>(out + (size_t)jj * stride) =
+          make_ulonglong2(reduce128_lazy8(hi[0], lo[0], P), reduce128_lazy8(hi[1], lo[1], P));
+    else
+      out[(size_t)jj * stride] = reduce128_lazy8(hi[0], lo[0], P);
   }
 }
 
-template <int S>
+// Loads NC adjacent residues of row x (16 bytes when NC = 2), multiplies them by the Shoup constant w and splits
+// them into 30-bit halves.
+template <int NC>
+__device__ __forceinline__ void load_split(const u64* x, ulonglong2 w, u64 p, uint32_t* lo, uint32_t* hi) {
+  u64 y[NC];
+  if constexpr (NC == 2) {
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(x);
+    y[0] = v.x;
+    y[1] = v.y;
+  } else {
+    y[0] = x[0];
+  }
+#pragma unroll
+  for (int k = 0; k < NC; k++) {
+    const u64 z = shoup(y[k], w.x, w.y, p);
+    lo[k] = (uint32_t)(z & kMask30);
+    hi[k] = (uint32_t)(z >> 30);
+  }
+}
+
+template <int S, int NC>
 __device__ __forceinline__ void modup_body(const KsJob& J, const Ring& r, const CrtTables& c,
                                            const PrimeConst* __restrict__ pc, int d, int start, int t, int nout,
                                            int base, const uint2* cs) {
-  const int n = blockIdx.x * kT + threadIdx.x;
-  uint32_t yl[S], yh[S];
+  const int n = (blockIdx.x * kT + threadIdx.x) * NC;
+  uint32_t yl[NC][S], yh[NC][S];
 #pragma unroll
   for (int i = 0; i < S; i++) {
-    const ulonglong2 w = c.mu_qhinv[base + i];
-    const u64 y = shoup(J.coeff[(size_t)(start + i) * r.N + n], w.x, w.y, pc[start + i].p);
-    yl[i] = (uint32_t)(y & kMask30);
-    yh[i] = (uint32_t)(y >> 30);
+    uint32_t lo[NC], hi[NC];
+    load_split<NC>(J.coeff + (size_t)(start + i) * r.N + n, c.mu_qhinv[base + i], pc[start + i].p, lo, hi);
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+      yl[k][i] = lo[k];
+      yh[k][i] = hi[k];
+    }
   }
   const int nq = c.nq;
-  conv_rows<S>(yl, yh, cs, nout, J.conv + (size_t)d * (t + c.np) * r.N + n, (size_t)r.N, pc,
-               [=](int jj) { return conv_tower(jj, start, S, t, nq); });
+  conv_rows<S, NC>(yl, yh, cs, nout, J.conv + (size_t)d * (t + c.np) * r.N + n, (size_t)r.N, pc,
+                   [=](int jj) { return conv_tower(jj, start, S, t, nq); });
 }
 
-// ModUp basis conversion: grid (N/256, dnum, njobs), one thread per coefficient, all converted rows of one
-// digit.  The digit's 30-bit-sliced [Qhat_i]_{m_j} constants are staged in shared memory.
-template <bool WIDE>
+// ModUp basis conversion: grid (N/512 (N/256 when MAXS > 16), rows = digits), two adjacent coefficients per thread
+// (one for digits of more than 16 towers), all converted rows of one digit.  MAXS bounds the digit size the
+// instance compiles (8, 12, 16 or 32), so the common small digits do not pay for the registers of large ones.  The
+// digit's 30-bit-sliced [Qhat_i]_{m_j} constants are staged in shared memory.
+template <int MAXS>
 __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                         const PrimeConst* __restrict__ pc) {
   extern __shared__ uint2 cs[];
@@ -126,27 +164,18 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
     cs[idx] = make_uint2(src[0], src[1]);
   }
   __syncthreads();
-#define FGB_MODUP_CASE(S_) \
-  case S_:                 \
-    modup_body<S_>(J, r, c, pc, d, start, t, nout, base, cs); \
+  constexpr int NC = MAXS <= 16 ? 2 : 1;
+#define FGB_MODUP_CASE(S_)                                              \
+  case S_:                                                              \
+    if constexpr (S_ <= MAXS) modup_body<S_, NC>(J, r, c, pc, d, start, t, nout, base, cs); \
     break;
-  if constexpr (!WIDE) {  // digits of at most 16 towers (kept separate so the common case stays register-light)
-    switch (s) {
-      FGB_MODUP_CASE(1) FGB_MODUP_CASE(2) FGB_MODUP_CASE(3) FGB_MODUP_CASE(4) FGB_MODUP_CASE(5) FGB_MODUP_CASE(6)
-      FGB_MODUP_CASE(7) FGB_MODUP_CASE(8) FGB_MODUP_CASE(9) FGB_MODUP_CASE(10) FGB_MODUP_CASE(11)
-      FGB_MODUP_CASE(12) FGB_MODUP_CASE(13) FGB_MODUP_CASE(14) FGB_MODUP_CASE(15) FGB_MODUP_CASE(16)
-      default:  // not reached: launch_modup_conv routes other sizes to the wide variant
-        break;
-    }
-  } else {
-    switch (s) {
-      FGB_MODUP_CASE(1) FGB_MODUP_CASE(2) FGB_MODUP_CASE(3) FGB_MODUP_CASE(4) FGB_MODUP_CASE(5) FGB_MODUP_CASE(6)
-      FGB_MODUP_CASE(7) FGB_MODUP_CASE(8) FGB_MODUP_CASE(9) FGB_MODUP_CASE(10) FGB_MODUP_CASE(11)
-      FGB_MODUP_CASE(12) FGB_MODUP_CASE(13) FGB_MODUP_CASE(14) FGB_MODUP_CASE(15) FGB_MODUP_CASE(16)
-      FGB_MODUP_CASE(20) FGB_MODUP_CASE(24) FGB_MODUP_CASE(28) FGB_MODUP_CASE(32)
-      default:  // not reached: launch_modup_conv rejects digit sizes without a compiled body
-        break;
-    }
+  switch (s) {  // sizes above MAXS are not reached: launch_modup_conv picks the instance from alpha
+    FGB_MODUP_CASE(1) FGB_MODUP_CASE(2) FGB_MODUP_CASE(3) FGB_MODUP_CASE(4) FGB_MODUP_CASE(5) FGB_MODUP_CASE(6)
+    FGB_MODUP_CASE(7) FGB_MODUP_CASE(8) FGB_MODUP_CASE(9) FGB_MODUP_CASE(10) FGB_MODUP_CASE(11)
+    FGB_MODUP_CASE(12) FGB_MODUP_CASE(13) FGB_MODUP_CASE(14) FGB_MODUP_CASE(15) FGB_MODUP_CASE(16)
+    FGB_MODUP_CASE(20) FGB_MODUP_CASE(24) FGB_MODUP_CASE(28) FGB_MODUP_CASE(32)
+    default:
+      break;
   }
 #undef FGB_MODUP_CASE
 }
@@ -237,7 +266,8 @@ __global__ void __launch_bounds__(kT) key_split_kernel(u64* __restrict__ k, size
   }
 }
 
-// ModDown basis conversion P -> Q_t: grid (N/256, 2, njobs); reads the (coefficient-form) P rows of inner.
+// ModDown basis conversion P -> Q_t: grid (N/512 (N/256 for more than 16 special primes), polys per job), two
+// adjacent coefficients per thread (one above 16 special primes); reads the (coefficient-form) P rows of inner.
 template <int K>
 __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                           const PrimeConst* __restrict__ pc) {
@@ -252,17 +282,21 @@ __global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant_
   }
   __syncthreads();
   const int poly = (int)blockIdx.y - b.row_begin[z];
-  const int n = blockIdx.x * kT + threadIdx.x;
+  constexpr int NC = K <= 16 ? 2 : 1;
+  const int n = (blockIdx.x * kT + threadIdx.x) * NC;
   const u64* x = J.inner + ((size_t)poly * ext + t) * r.N + n;
-  uint32_t yl[K], yh[K];
+  uint32_t yl[NC][K], yh[NC][K];
 #pragma unroll
   for (int i = 0; i < K; i++) {
-    const ulonglong2 w = c.md_phinv[i];
-    const u64 y = shoup(x[(size_t)i * r.N], w.x, w.y, pc[c.nq + i].p);
-    yl[i] = (uint32_t)(y & kMask30);
-    yh[i] = (uint32_t)(y >> 30);
+    uint32_t lo[NC], hi[NC];
+    load_split<NC>(x + (size_t)i * r.N, c.md_phinv[i], pc[c.nq + i].p, lo, hi);
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+      yl[k][i] = lo[k];
+      yh[k][i] = hi[k];
+    }
   }
-  conv_rows<K>(yl, yh, cs, t, J.md + (size_t)poly * t * r.N + n, (size_t)r.N, pc, [](int j) { return j; });
+  conv_rows<K, NC>(yl, yh, cs, t, J.md + (size_t)poly * t * r.N + n, (size_t)r.N, pc, [](int j) { return j; });
 }
 
 // out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/512, rows); inner_Q arrives in [0, 4p).
@@ -571,11 +605,15 @@ cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& 
   KsBatch bb;
   const int alpha = c.alpha;
   const int rows = with_rows(b, bb, [alpha](const KsJob& j) { return (j.t + alpha - 1) / alpha; });
-  dim3 grid(r.N / kT, rows, 1);
-  if (c.alpha <= 16)
-    modup_conv_kernel<false><<<grid, kT, smem, s>>>(bb, r, c, pc);
+  dim3 grid(r.N / (c.alpha <= 16 ? 2 * kT : kT), rows, 1);
+  if (c.alpha <= 8)
+    modup_conv_kernel<8><<<grid, kT, smem, s>>>(bb, r, c, pc);
+  else if (c.alpha <= 12)
+    modup_conv_kernel<12><<<grid, kT, smem, s>>>(bb, r, c, pc);
+  else if (c.alpha <= 16)
+    modup_conv_kernel<16><<<grid, kT, smem, s>>>(bb, r, c, pc);
   else
-    modup_conv_kernel<true><<<grid, kT, smem, s>>>(bb, r, c, pc);
+    modup_conv_kernel<32><<<grid, kT, smem, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -632,7 +670,7 @@ cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables
   const size_t smem = sizeof(uint2) * c.np * max_t(b);
   KsBatch bb;
   const int rows = with_rows(b, bb, [](const KsJob& j) { return j.polys ? j.polys : 2; });
-  dim3 grid(r.N / kT, rows, 1);
+  dim3 grid(r.N / (c.np <= 16 ? 2 * kT : kT), rows, 1);
   switch (c.np) {
 #define FGB_MD_CASE(K_)                                                    \
   case K_:                                                                 \
