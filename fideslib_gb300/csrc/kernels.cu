@@ -144,7 +144,7 @@ __device__ __forceinline__ void modup_body(const KsJob& J, const Ring& r, const 
 
 // ModUp basis conversion: grid (N/512 (N/256 when MAXS > 16), rows = digits), two adjacent coefficients per thread
 // (one for digits of more than 16 towers), all converted rows of one digit.  MAXS bounds the digit size the
-// instance compiles (8, 12, 16 or 32), so the common small digits do not pay for the registers of large ones.  The
+// instance compiles (8, 10, 12, 16 or 32), so the common small digits do not pay for the registers of large ones.  The
 // digit's 30-bit-sliced [Qhat_i]_{m_j} constants are staged in shared memory.
 template <int MAXS>
 __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
@@ -608,6 +608,8 @@ cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& 
   dim3 grid(r.N / (c.alpha <= 16 ? 2 * kT : kT), rows, 1);
   if (c.alpha <= 8)
     modup_conv_kernel<8><<<grid, kT, smem, s>>>(bb, r, c, pc);
+  else if (c.alpha <= 10)
+    modup_conv_kernel<10><<<grid, kT, smem, s>>>(bb, r, c, pc);
   else if (c.alpha <= 12)
     modup_conv_kernel<12><<<grid, kT, smem, s>>>(bb, r, c, pc);
   else if (c.alpha <= 16)
