@@ -87,6 +87,13 @@ _SIGS = {
     "fides_eval_mult_int": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int64, u32p]),
     "fides_eval_mult_scalar": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, C.c_double, u32p]),
     "fides_eval_add_scalar": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, u32p]),
+    "fides_eval_fast_rotation_ext": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_int32),
+                                               C.c_int32, u32p]),
+    "fides_ext_add": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_pt_load_ext": (C.c_int, [C.c_void_p, u64p, C.c_uint32, C.c_double, u32p]),
+    "fides_ext_mult_plain": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
+    "fides_key_switch_down": (C.c_int, [C.c_void_p, C.c_uint32, u32p]),
+    "fides_ext_store": (C.c_int, [C.c_void_p, C.c_uint32, u64p, C.c_void_p]),
     "fides_eval_many_to_one": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, u32p, u32p,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double), u32p]),
     "fides_level_reduce": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
@@ -385,6 +392,36 @@ class CryptoContext:
         _check(lib().fides_eval_many_to_one(self._h, op, nb, stride, ptr(a_arr, u32), ptr(b_arr, u32),
                                             ptr(v_arr, f64), ptr(s_arr, f64), ptr(outs, u32)))
         return None if in_place else [int(x) for x in outs]
+
+    # --- extended-basis ciphertexts (EvalFastRotationExt / KeySwitchDown) ---
+    def eval_fast_rotation_ext(self, a: int, indices, add_first: bool = True, pre: int = 0) -> list[int]:
+        idx = np.ascontiguousarray(np.array(indices, dtype=np.int32))
+        outs = np.zeros(len(idx), dtype=np.uint32)
+        _check(lib().fides_eval_fast_rotation_ext(self._h, a, pre, len(idx), idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  1 if add_first else 0, _p(outs, u32p)))
+        return [int(x) for x in outs]
+
+    def ext_add(self, a: int, b: int) -> int:
+        return self._un(lib().fides_ext_add, a, b)
+
+    def load_plaintext_ext(self, pt: np.ndarray, towers: int, scale: float = 1.0) -> int:
+        """pt: u64[towers + np][N] (Q rows, then the special rows)."""
+        pt = np.ascontiguousarray(pt, dtype=np.uint64)
+        assert pt.shape[0] == towers + self.np
+        h = C.c_uint32()
+        _check(lib().fides_pt_load_ext(self._h, _p(pt), towers, scale, C.byref(h)))
+        return h.value
+
+    def ext_mult_plain(self, a: int, pt: int) -> int:
+        return self._un(lib().fides_ext_mult_plain, a, pt)
+
+    def key_switch_down(self, a: int) -> int:
+        return self._un(lib().fides_key_switch_down, a)
+
+    def store_ext(self, h: int, towers: int) -> np.ndarray:
+        out = np.zeros((2, towers + self.np, self.N), dtype=np.uint64)
+        _check(lib().fides_ext_store(self._h, h, _p(out), None))
+        return out
 
     def level_reduce(self, a: int, towers: int) -> int:
         return self._un(lib().fides_level_reduce, a, towers)

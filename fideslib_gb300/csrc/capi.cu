@@ -364,11 +364,14 @@ int fides_ct_store(fides_ctx* ctx, uint32_t handle, uint64_t* data, fides_ct_met
 
 int fides_ct_free(fides_ctx* ctx, uint32_t handle) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
-  auto it = ctx->c->cts.find(handle);
-  if (it == ctx->c->cts.end()) return fail(FIDES_EINVAL, "unknown ciphertext handle");
-  ctx->c->free_limbs(it->second.data, ctx->c->stream);
-  ctx->c->cts.erase(it);
-  return FIDES_OK;
+  for (auto* map : {&ctx->c->cts, &ctx->c->ext_cts}) {
+    auto it = map->find(handle);
+    if (it == map->end()) continue;
+    ctx->c->free_limbs(it->second.data, ctx->c->stream);
+    map->erase(it);
+    return FIDES_OK;
+  }
+  return fail(FIDES_EINVAL, "unknown ciphertext handle");
 }
 
 // Plaintext jobs, kMaxJobs per launch.
@@ -1138,6 +1141,204 @@ int fides_eval_mult_monomial(fides_ctx* ctx, uint32_t a, uint32_t k, uint32_t* o
   if (rc) return rc;
   CK(c->mult_monomial(A->data, A->t, k, r.data, c->stream), "monomial multiplication");
   *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+
+// ---------------------------------------------------------------------------------------------------------
+// Extended-basis ciphertexts (EvalFastRotationExt / KeySwitchDown)
+// ---------------------------------------------------------------------------------------------------------
+
+static uint32_t register_ext(fides_ctx* ctx, const fgb::DevCt& ct) {
+  uint32_t h = ctx->c->next_handle++;
+  if (ctx->c->next_handle == 0) ctx->c->next_handle = 1;
+  ctx->c->ext_cts[h] = ct;
+  return h;
+}
+
+static fgb::DevCt* find_ext(fides_ctx* ctx, uint32_t h) {
+  auto it = ctx->c->ext_cts.find(h);
+  return it == ctx->c->ext_cts.end() ? nullptr : &it->second;
+}
+
+int fides_eval_fast_rotation_ext(fides_ctx* ctx, uint32_t a, uint32_t pre, uint32_t n, const int32_t* indices,
+                                 int32_t add_first, uint32_t* outs) {
+  if (!valid_ctx(ctx) || (n && (!indices || !outs))) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ct(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(a));
+  const fgb::DevModUp* M = nullptr;
+  if (pre) {
+    auto it = c->modups.find(pre);
+    if (it == c->modups.end()) return fail(FIDES_EINVAL, "unknown precomputation handle");
+    if (it->second.t != A->t) return fail(FIDES_EINVAL, "precomputation was made at a different tower count");
+    M = &it->second;
+  }
+  if (int rc = check_ks_shape(ctx)) return rc;
+  const int t = A->t;
+  const size_t NN = (size_t)c->N, rows = (size_t)2 * (t + c->np);
+  std::vector<fgb::DevCt> res(n);
+  std::vector<fgb::Context::KsReq> rq;
+  fgb::KsBatch lift{};
+  int rc = FIDES_OK;
+  for (uint32_t i = 0; i < n && rc == FIDES_OK; i++) {
+    res[i] = *A;
+    res[i].data = c->alloc_limbs(rows, c->stream);
+    if (!res[i].data) {
+      rc = fail(FIDES_ENOMEM, "ciphertext allocation failed");
+      break;
+    }
+    const uint32_t g = fgb::Context::galois_for_index(c->N, indices[i]);
+    if (g == 1) {  // no rotation: the input itself, lifted by P
+      fgb::KsJob& j = lift.jobs[lift.njobs++];
+      j.add0 = add_first ? A->data : nullptr;
+      j.add1 = A->data + (size_t)t * NN;
+      j.out = res[i].data;
+      j.t = t;
+      j.galois_inv = 1;
+      j.ext_mode = 1;
+      if (lift.njobs == fgb::kMaxJobs) rc = fail(FIDES_EINVAL, "at most 64 zero rotations per call");
+      continue;
+    }
+    auto kt = c->rot_keys.find(g);
+    if (kt == c->rot_keys.end()) {
+      rc = fail(FIDES_ENOKEY, "no rotation key for Galois element " + std::to_string(g));
+      break;
+    }
+    fgb::Context::KsReq r{M ? M->c1 : A->data + (size_t)t * NN, t, kt->second, add_first ? A->data : nullptr, nullptr,
+                          res[i].data, c->galois_inverse(g), M ? M->digits : nullptr};
+    r.ext_mode = 1;
+    rq.push_back(r);
+  }
+  cudaError_t e = cudaSuccess;
+  if (rc == FIDES_OK) {
+    const fgb::Ring ring{c->N, c->logN};
+    e = fgb::launch_ext_epilogue(lift, ring, c->crt, c->d_pc, c->stream);
+    if (e == cudaSuccess) e = c->keyswitch_batch(rq.data(), (int)rq.size(), c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "fast rotation (extended basis)");
+  }
+  if (rc != FIDES_OK) {
+    for (auto& r : res) c->free_limbs(r.data, c->stream);
+    return rc;
+  }
+  for (uint32_t i = 0; i < n; i++) outs[i] = register_ext(ctx, res[i]);
+  return FIDES_OK;
+}
+
+int fides_ext_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ext(ctx, a);
+  fgb::DevCt* B = find_ext(ctx, b);
+  if (!A || !B) return fail(FIDES_EINVAL, "unknown extended-basis ciphertext handle");
+  if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
+  fgb::DevCt r = *A;
+  r.noise_deg = std::max(A->noise_deg, B->noise_deg);
+  r.data = c->alloc_limbs((size_t)2 * (A->t + c->np), c->stream);
+  if (!r.data) return fail(FIDES_ENOMEM, "ciphertext allocation failed");
+  fgb::SumBatch sb{};
+  sb.nq = c->nq;
+  sb.njobs = 1;
+  sb.jobs[0] = fgb::SumJob{B->data, 0, 1, A->data, r.data, A->t, c->np};
+  const fgb::Ring ring{c->N, c->logN};
+  const cudaError_t e = fgb::launch_sum(sb, ring, c->d_pc, c->stream);
+  if (e != cudaSuccess) {
+    c->free_limbs(r.data, c->stream);
+    return cuda_fail(e, "extended-basis add");
+  }
+  *out = register_ext(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_pt_load_ext(fides_ctx* ctx, const uint64_t* data, uint32_t towers, double scale, uint32_t* handle) {
+  if (!valid_ctx(ctx) || !data || !handle) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  if (towers < 1 || towers > (uint32_t)c->nq) return fail(FIDES_EINVAL, "towers out of range");
+  fgb::DevPt p;
+  p.t = (int)towers;
+  p.prows = c->np;
+  p.scale = scale;
+  const size_t rows = (size_t)towers + c->np;
+  p.data = c->alloc_limbs(rows, c->stream);
+  if (!p.data) return fail(FIDES_ENOMEM, "plaintext allocation failed");
+  CK(cudaMemcpyAsync(p.data, data, rows * c->N * sizeof(uint64_t), cudaMemcpyDefault, c->stream), "plaintext copy");
+  const uint32_t h = c->next_handle++;
+  c->pts[h] = p;
+  *handle = h;
+  return FIDES_OK;
+}
+
+int fides_ext_mult_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ext(ctx, a);
+  fgb::DevPt* P = find_pt(ctx, pt);
+  if (!A || !P) return fail(FIDES_EINVAL, "unknown extended-basis ciphertext or plaintext handle");
+  if (P->prows != c->np) return fail(FIDES_EINVAL, "the plaintext has no special-prime rows (fides_pt_load_ext)");
+  if (P->t < A->t) return fail(FIDES_EINVAL, "plaintext has fewer towers than the ciphertext");
+  fgb::DevCt r = *A;
+  r.scale = A->scale * P->scale;
+  r.noise_deg = A->noise_deg + 1;
+  r.data = c->alloc_limbs((size_t)2 * (A->t + c->np), c->stream);
+  if (!r.data) return fail(FIDES_ENOMEM, "ciphertext allocation failed");
+  static const uint8_t kOne[1] = {1};
+  fgb::DotBatch db{};
+  db.pt_base = P->data;
+  db.pt_stride = (long long)(P->t + P->prows) * c->N;
+  db.present = kOne;
+  db.bs = 1;
+  db.t = A->t;
+  db.np = c->np;
+  db.nq = c->nq;
+  db.pt_prow = P->t;
+  db.njobs = 1;
+  db.jobs[0] = fgb::DotJob{r.data, A->data, nullptr, 0, 1, 0ull};
+  const fgb::Ring ring{c->N, c->logN};
+  const cudaError_t e = fgb::launch_ptdot(db, ring, c->d_pc, c->stream);
+  if (e != cudaSuccess) {
+    c->free_limbs(r.data, c->stream);
+    return cuda_fail(e, "extended-basis plaintext product");
+  }
+  *out = register_ext(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_key_switch_down(fides_ctx* ctx, uint32_t a, uint32_t* out) {
+  if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ext(ctx, a);
+  if (!A) return fail(FIDES_EINVAL, "unknown extended-basis ciphertext handle");
+  const size_t rows = (size_t)2 * (A->t + c->np);
+  fgb::u64* tmp = c->alloc_limbs(rows, c->stream);  // the ModDown leaves its input's special rows in coefficient form
+  fgb::DevCt r;
+  int rc = new_ct(ctx, A->t, *A, &r);
+  if (rc || !tmp) {
+    c->free_limbs(tmp, c->stream);
+    if (!rc) c->free_limbs(r.data, c->stream);
+    return rc ? rc : fail(FIDES_ENOMEM, "workspace allocation failed");
+  }
+  cudaError_t e = cudaMemcpyAsync(tmp, A->data, rows * c->N * sizeof(uint64_t), cudaMemcpyDeviceToDevice, c->stream);
+  const fgb::Context::MdReq m{tmp, A->t, 2, r.data};
+  if (e == cudaSuccess) e = c->moddown_batch(&m, 1, c->stream);
+  c->free_limbs(tmp, c->stream);
+  if (e != cudaSuccess) {
+    c->free_limbs(r.data, c->stream);
+    return cuda_fail(e, "key switch down");
+  }
+  *out = register_ct(ctx, r);
+  return FIDES_OK;
+}
+
+int fides_ext_store(fides_ctx* ctx, uint32_t h, uint64_t* data, fides_ct_meta* meta) {
+  if (!valid_ctx(ctx) || !data) return fail(FIDES_EINVAL, "null argument");
+  fgb::Context* c = ctx->c;
+  fgb::DevCt* A = find_ext(ctx, h);
+  if (!A) return fail(FIDES_EINVAL, "unknown extended-basis ciphertext handle");
+  CK(cudaMemcpyAsync(data, A->data, (size_t)2 * (A->t + c->np) * c->N * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                     c->stream),
+     "ciphertext store");
+  CK(cudaStreamSynchronize(c->stream), "ciphertext store");
+  if (meta) *meta = fides_ct_meta{(uint32_t)A->t, (uint32_t)A->noise_deg, (uint32_t)A->slots, 0, A->scale};
   return FIDES_OK;
 }
 

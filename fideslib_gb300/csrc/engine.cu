@@ -114,6 +114,8 @@ Context::~Context() {
     if (kv.second.data) cudaFree(kv.second.data);
   for (auto& kv : pts)
     if (kv.second.data) cudaFree(kv.second.data);
+  for (auto& kv : ext_cts)
+    if (kv.second.data) cudaFree(kv.second.data);
   for (auto& kv : modups) {
     if (kv.second.c1) cudaFree(kv.second.c1);
     if (kv.second.digits) cudaFree(kv.second.digits);

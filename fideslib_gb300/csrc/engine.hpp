@@ -36,9 +36,10 @@ struct DevModUp {
 };
 
 struct DevPt {
-  u64* data = nullptr;  // [t][N] evaluation form
+  u64* data = nullptr;  // [t + prows][N] evaluation form
   int t = 0;
   double scale = 1.0;
+  int prows = 0;  // special-prime rows after the t Q rows (np for an extended-basis plaintext, else 0)
 };
 
 // Baby-step / giant-step linear transform over the diagonals at slot offsets base + k*stride, k = g*bs + b:
@@ -161,6 +162,7 @@ class Context {
   // --- object registry (handles as in api/CryptoContext.hpp:233-246) ---
   std::mutex mu;
   std::unordered_map<uint32_t, DevCt> cts;
+  std::unordered_map<uint32_t, DevCt> ext_cts;  // extended basis Q_t ∪ P: data [2][t+np][N]
   uint32_t next_handle = 1;
   std::map<uint32_t, u64*> rot_keys;  // Galois element -> key
   std::unordered_map<uint32_t, DevPt> pts;

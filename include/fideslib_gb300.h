@@ -161,6 +161,25 @@ int fides_fast_rotation_precompute(fides_ctx* ctx, uint32_t a, uint32_t* pre);
  * fides_eval_rotate. */
 int fides_eval_fast_rotation_precomputed(fides_ctx* ctx, uint32_t a, uint32_t pre, int32_t index, uint32_t* out);
 int fides_precompute_free(fides_ctx* ctx, uint32_t pre);
+/* Extended-basis ciphertexts, u64[2][t+np][N] over Q_t ∪ P (the key-switch output before its ModDown), for
+ * hoisted linear maps with one ModDown at the end:
+ *   EvalFastRotationExt (api/CryptoContext.cpp:1497-1526, 1575-1617; OpenFHE KeySwitchHYBRID::EvalFastRotationExt):
+ *     per index, the inner product of the digits of c1 (`pre` from fides_fast_rotation_precompute, or 0 to ModUp
+ *     here once for all indices) with the rotation key, plus P*c0 on the Q rows when add_first, then the
+ *     automorphism; index 0 gives (add_first ? P*c0 : 0, P*c1).  Handles go to outs[n] (free with fides_ct_free).
+ *   fides_ext_add: sum of two extended ciphertexts with the same towers.
+ *   fides_pt_load_ext + fides_ext_mult_plain: product with a plaintext given at the towers Q rows and the np special
+ *     rows (u64[towers+np][N], towers >= the ciphertext's), the extended plaintexts of OpenFHE's hoisted
+ *     EvalLinearTransform; the scale is multiplied.
+ *   fides_key_switch_down (OpenFHE KeySwitchDown): ModDown of both polys, a regular ciphertext again.
+ *   fides_ext_store: u64[2][t+np][N] to host memory. */
+int fides_eval_fast_rotation_ext(fides_ctx* ctx, uint32_t a, uint32_t pre, uint32_t n, const int32_t* indices,
+                                 int32_t add_first, uint32_t* outs);
+int fides_ext_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out);
+int fides_pt_load_ext(fides_ctx* ctx, const uint64_t* data, uint32_t towers, double scale, uint32_t* handle);
+int fides_ext_mult_plain(fides_ctx* ctx, uint32_t a, uint32_t pt, uint32_t* out);
+int fides_key_switch_down(fides_ctx* ctx, uint32_t a, uint32_t* out);
+int fides_ext_store(fides_ctx* ctx, uint32_t h, uint64_t* data, fides_ct_meta* meta);
 
 /* Plaintexts (RawPlainText / LoadPlaintext, RawCiphertext.cuh:37-48, api/CryptoContext.cpp:250-269):
  * u64[towers][N] evaluation form at scaling factor `scale`. */
