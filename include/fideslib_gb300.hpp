@@ -3,9 +3,9 @@
 // Mirrors the method names and argument meaning of the reference's fideslib::CryptoContextImpl<DCRTPoly>
 // (api/CryptoContext.hpp:43-203) for the evaluation hot path, on raw residues instead of OpenFHE objects:
 // LoadContext (the constructor), LoadCiphertext / LoadPlaintext, EvalAdd / EvalSub / EvalMult / EvalSquare,
-// EvalRotate, EvalFastRotationPrecompute / EvalFastRotation, the *InPlace forms, Rescale, EvalChebyshevSeries,
-// EvalBootstrap, Synchronize.  Like the reference
-// API it reports failures by throwing (fideslib_gb300::Error carries the C status code and message); the C ABI
+// EvalRotate, EvalFastRotationPrecompute / EvalFastRotation / EvalFastRotationExt + KeySwitchDown, the *InPlace
+// forms, Rescale, EvalChebyshevSeries, EvalBootstrap, Synchronize.  Like the reference API it reports failures by
+// throwing (fideslib_gb300::Error carries the C status code and message); the C ABI
 // underneath never throws or exits.  Ciphertext is a shared, reference-counted device handle
 // (the reference's Ciphertext<DCRTPoly> is a shared_ptr, api/Ciphertext.hpp:13-58).
 #pragma once
@@ -97,6 +97,26 @@ class Plaintext {
     uint32_t id;
   };
   Plaintext(fides_ctx* ctx, uint32_t id) : h_(std::make_shared<Handle>(ctx, id)) {}
+  std::shared_ptr<Handle> h_;
+};
+
+// A ciphertext in the extended basis Q_t ∪ P (EvalFastRotationExt's result, consumed by KeySwitchDown).
+class ExtCiphertext {
+ public:
+  ExtCiphertext() = default;
+  uint32_t handle() const { return h_ ? h_->id : 0; }
+
+ private:
+  friend class CryptoContext;
+  struct Handle {
+    Handle(fides_ctx* c, uint32_t i) : ctx(c), id(i) {}
+    Handle(const Handle&) = delete;
+    Handle& operator=(const Handle&) = delete;
+    ~Handle() { fides_ct_free(ctx, id); }
+    fides_ctx* ctx;
+    uint32_t id;
+  };
+  ExtCiphertext(fides_ctx* ctx, uint32_t id) : h_(std::make_shared<Handle>(ctx, id)) {}
   std::shared_ptr<Handle> h_;
 };
 
@@ -196,6 +216,35 @@ class CryptoContext {
   Ciphertext EvalFastRotation(const Ciphertext& a, int32_t index, uint32_t /*m*/, const Precomputation& pre) {
     return wrap(fides_eval_fast_rotation_precomputed(ctx_, a.handle(), pre.handle(), index, &tmp_));
   }
+  // EvalFastRotationExt (api/CryptoContext.cpp:1497-1617): the rotations left in the extended basis, with or
+  // without P * c0; products with plaintexts loaded by LoadPlaintextExt and sums stay there; KeySwitchDown ends.
+  std::vector<ExtCiphertext> EvalFastRotationExt(const Ciphertext& a, const std::vector<int32_t>& indices,
+                                                 const Precomputation& pre, bool addFirst) {
+    std::vector<uint32_t> h(indices.size());
+    check(fides_eval_fast_rotation_ext(ctx_, a.handle(), pre.handle(), (uint32_t)indices.size(), indices.data(),
+                                       addFirst ? 1 : 0, h.data()));
+    std::vector<ExtCiphertext> out;
+    for (uint32_t x : h) out.push_back(ExtCiphertext(ctx_, x));
+    return out;
+  }
+  ExtCiphertext EvalFastRotationExt(const Ciphertext& a, int32_t index, const Precomputation& pre, bool addFirst) {
+    return EvalFastRotationExt(a, std::vector<int32_t>{index}, pre, addFirst)[0];
+  }
+  // data = u64[towers + np][N]: the Q rows, then the special-prime rows.
+  Plaintext LoadPlaintextExt(const uint64_t* data, uint32_t towers, double scale) {
+    uint32_t h;
+    check(fides_pt_load_ext(ctx_, data, towers, scale, &h));
+    return Plaintext(ctx_, h);
+  }
+  ExtCiphertext EvalMult(const ExtCiphertext& a, const Plaintext& pt) {
+    check(fides_ext_mult_plain(ctx_, a.handle(), pt.handle(), &tmp_));
+    return ExtCiphertext(ctx_, tmp_);
+  }
+  ExtCiphertext EvalAdd(const ExtCiphertext& a, const ExtCiphertext& b) {
+    check(fides_ext_add(ctx_, a.handle(), b.handle(), &tmp_));
+    return ExtCiphertext(ctx_, tmp_);
+  }
+  Ciphertext KeySwitchDown(const ExtCiphertext& a) { return wrap(fides_key_switch_down(ctx_, a.handle(), &tmp_)); }
   // In-place forms (EvalAddInPlace, EvalMultInPlace, EvalSquareInPlace, RescaleInPlace, EvalRotateInPlace): the
   // handle is replaced by the result's.
   void EvalAddInPlace(Ciphertext& a, const Ciphertext& b) { a = EvalAdd(a, b); }

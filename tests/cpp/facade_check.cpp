@@ -61,6 +61,10 @@ int main() {
     Ciphertext c = a;
     cc.EvalRotateInPlace(c, 1);
     same(c, hoisted[0], "in-place rotation");
+    // index 0 of EvalFastRotationExt is (P c0, P c1); KeySwitchDown divides P out exactly
+    auto ext = cc.EvalFastRotationExt(a, {0, 1}, pre, true);
+    same(cc.KeySwitchDown(ext[0]), a, "KeySwitchDown(EvalFastRotationExt(a, 0))");
+    same(cc.KeySwitchDown(cc.EvalAdd(ext[0], ext[0])), cc.EvalAdd(a, a), "KeySwitchDown of a sum");
   }
   if (cc.StoreCiphertext(cc.EvalSub(cc.EvalAdd(a, b), b)) != ha) {
     std::printf("mismatch: (a + b) - b\n");
