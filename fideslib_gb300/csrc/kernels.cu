@@ -493,44 +493,71 @@ __global__ void __launch_bounds__(kT) monomial_kernel(const __grid_constant__ Mo
 
 // Inner sums: grid (N/256, 2 (t+np) njobs), ordered (row, job, poly) with the poly and the job fastest, so that
 // the blocks reading the same plaintext rows (both polys of every input of a batch) run back to back and share
-// them through L2.  A thread takes one coefficient of one poly for up to kDotG giant steps: each baby-step value
-// is read once, and four baby steps' loads (value and plaintexts) are issued before their products so that
-// enough loads are in flight to cover HBM latency.  One Acc4 per giant step holds at most 16 products (bs <= 16),
-// folded and reduced once at the end.
+// them through L2.  A thread takes one coefficient of one poly for up to kDotG giant steps, in rounds of four
+// baby steps: each round's baby-step value and plaintext values (20 words) are copied to shared memory with
+// cp.async (zero-filled where a diagonal is absent) one round ahead of the products, so two rounds of loads are in
+// flight per thread without holding them in registers.  Each thread only reads back the words it copied itself,
+// so completion (cp.async.wait_group) needs no block barrier.  One Acc4 per giant step holds at most 16 products
+// (bs <= 16), folded and reduced once at the end.
+constexpr int kDotWords = 4 + 4 * kDotG;  // per thread and round: 4 baby-step values, 4 x kDotG plaintext values
+
+__device__ __forceinline__ void cp_async8(u64* dst, const u64* src, bool on) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(on ? 8 : 0) : "memory");
+}
+
 __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBatch b, Ring r,
                                                    const PrimeConst* __restrict__ pc) {
+  extern __shared__ __align__(16) u64 stage[];  // [2 rounds][kDotWords][kT]
   const int y = (int)blockIdx.y, poly = y & 1, job = (y >> 1) % b.njobs, j = (y >> 1) / b.njobs;
   const DotJob& J = b.jobs[job];
   const int t = b.t, rows = t + b.np;
   const int tower = j < t ? j : b.nq + (j - t), prow = j < t ? j : b.pt_prow + (j - t);
-  const size_t n = (size_t)blockIdx.x * kT + threadIdx.x;
+  const int tid = threadIdx.x;
+  const size_t n = (size_t)blockIdx.x * kT + tid;
   const size_t co = ((size_t)poly * rows + j) * r.N + n, po = (size_t)prow * r.N + n;
   const unsigned long long pm = J.pmask;
-  Acc4 A[kDotG];
-#pragma unroll
-  for (int g = 0; g < kDotG; g++) A[g] = Acc4{0, 0, 0, 0};
-#pragma unroll 1
-  for (int b0 = 0; b0 < b.bs; b0 += 4) {
-    u64 x[4], w[4][kDotG];
+  const int rounds = (b.bs + 3) / 4;
+  auto issue = [&](int round) {
+    u64* buf = stage + (size_t)(round & 1) * kDotWords * kT + tid;
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const int bb = b0 + u;
+      const int bb = round * 4 + u;
       bool any = false;
 #pragma unroll
       for (int g = 0; g < kDotG; g++) {
         const bool on = bb < b.bs && ((pm >> (g * 16 + (bb & 15))) & 1ull);
         any = any || on;
-        w[u][g] = on ? b.pt_base[(size_t)((J.g + g) * b.bs + bb) * b.pt_stride + po] : 0ull;
+        const u64* src = on ? b.pt_base + (size_t)((J.g + g) * b.bs + bb) * b.pt_stride + po : b.pt_base;
+        cp_async8(buf + (4 + u * kDotG + g) * kT, src, on);
       }
-      const u64* ct = bb == 0 ? J.rot0 : J.rot_base + (size_t)(bb - 1) * b.rot_stride;
-      x[u] = any ? ct[co] : 0ull;
+      const u64* ct = !any ? J.rot0 : bb == 0 ? J.rot0 + co : J.rot_base + (size_t)(bb - 1) * b.rot_stride + co;
+      cp_async8(buf + u * kT, ct, any);
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  Acc4 A[kDotG];
+#pragma unroll
+  for (int g = 0; g < kDotG; g++) A[g] = Acc4{0, 0, 0, 0};
+  issue(0);
+#pragma unroll 1
+  for (int round = 0; round < rounds; round++) {
+    if (round + 1 < rounds) {
+      issue(round + 1);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    const u64* buf = stage + (size_t)(round & 1) * kDotWords * kT + tid;
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const uint32_t xl = (uint32_t)(x[u] & kMask30), xh = (uint32_t)(x[u] >> 30);
+      const u64 x = buf[u * kT];
+      const uint32_t xl = (uint32_t)(x & kMask30), xh = (uint32_t)(x >> 30);
 #pragma unroll
-      for (int g = 0; g < kDotG; g++)
-        acc4_mac(A[g], xl, xh, (uint32_t)(w[u][g] & kMask30), (uint32_t)(w[u][g] >> 30));
+      for (int g = 0; g < kDotG; g++) {
+        const u64 w = buf[(4 + u * kDotG + g) * kT];
+        acc4_mac(A[g], xl, xh, (uint32_t)(w & kMask30), (uint32_t)(w >> 30));
+      }
     }
   }
   const PrimeConst& P = pc[tower];
@@ -796,7 +823,14 @@ cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc,
       for (int k = 0; k < b.bs; k++)
         if (b.present[(J.g + g) * b.bs + k]) J.pmask |= 1ull << (g * 16 + k);
   }
-  ptdot_kernel<<<dim3(r.N / kT, 2 * (b.t + b.np) * b.njobs, 1), kT, 0, s>>>(bb, r, pc);
+  const size_t smem = sizeof(u64) * 2 * kDotWords * kT;
+  static bool attr_done = false;
+  if (!attr_done) {
+    const cudaError_t e = cudaFuncSetAttribute(ptdot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  ptdot_kernel<<<dim3(r.N / kT, 2 * (b.t + b.np) * b.njobs, 1), kT, smem, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }

@@ -166,3 +166,19 @@ def test_many_to_one_errors(env):
         gpu.eval_many_to_one(F.OP_ROTATE, [hs[0]], values=[1.0])
     # a failed call leaves its inputs untouched
     assert np.array_equal(gpu.store_ciphertext(hs[0]), arrs[0])
+
+
+def test_plaintext_requests_through_the_server(env):
+    """*_PLAIN requests admitted by the continuous-batching server give the direct results."""
+    F, gpu = env.F, env.gpu
+    arrs, hs = env.cts([NQ, 4, 2, 6])
+    parr, ph = env.pts(2)
+    reqs = [(F.OP_MULT_PLAIN, hs[0], ph[0]), (F.OP_ADD_PLAIN, hs[1], ph[1]), (F.OP_SUB_PLAIN, hs[2], ph[0]),
+            (F.OP_MULT_PLAIN, hs[3], ph[1])]
+    direct = [gpu.store_ciphertext(gpu.eval_batch([(op, a, b, 0)])[0]) for op, a, b in reqs]
+    srv = F.Server(gpu, max_batch=8, max_inflight=2, mem_budget=1 << 30)
+    tickets = [srv.submit(op, a, b) for op, a, b in reqs]
+    outs = [srv.wait(t)[0] for t in tickets]
+    srv.close()
+    for o, d in zip(outs, direct):
+        assert np.array_equal(gpu.store_ciphertext(o), d)
