@@ -491,15 +491,15 @@ __global__ void __launch_bounds__(kT) monomial_kernel(const __grid_constant__ Mo
   J.out[o] = v;
 }
 
-// Inner sums: grid (N/256, 2 (t+np) njobs), ordered (row, job, poly) with the poly and the job fastest, so that
-// the blocks reading the same plaintext rows (both polys of every input of a batch) run back to back and share
-// them through L2.  A thread takes one coefficient of one poly for up to kDotG giant steps, in rounds of four
-// baby steps: each round's baby-step value and plaintext values (20 words) are copied to shared memory with
-// cp.async (zero-filled where a diagonal is absent) one round ahead of the products, so two rounds of loads are in
-// flight per thread without holding them in registers.  Each thread only reads back the words it copied itself,
-// so completion (cp.async.wait_group) needs no block barrier.  One Acc4 per giant step holds at most 16 products
-// (bs <= 16), folded and reduced once at the end.
-constexpr int kDotWords = 4 + 4 * kDotG;  // per thread and round: 4 baby-step values, 4 x kDotG plaintext values
+// Inner sums: grid (N/256, (t+np) njobs), ordered (row, job) with the job fastest, so that the blocks reading the
+// same plaintext rows (every input of a batch) run back to back and share them through L2.  A thread takes one
+// coefficient of both polys for up to kDotG giant steps, in rounds of four baby steps: each round's baby-step
+// values (both polys) and plaintext values (24 words) are copied to shared memory with cp.async (zero-filled where
+// a diagonal is absent) one round ahead of the products, so two rounds of loads are in flight per thread without
+// holding them in registers, and each plaintext value is read once for both polys.  Each thread only reads back
+// the words it copied itself, so completion (cp.async.wait_group) needs no block barrier.  One Acc4 per (giant
+// step, poly) holds at most 16 products (bs <= 16), folded and reduced once at the end.
+constexpr int kDotWords = 8 + 4 * kDotG;  // per thread and round: 4 x 2 baby-step values, 4 x kDotG plaintexts
 
 __device__ __forceinline__ void cp_async8(u64* dst, const u64* src, bool on) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -509,13 +509,13 @@ __device__ __forceinline__ void cp_async8(u64* dst, const u64* src, bool on) {
 __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBatch b, Ring r,
                                                    const PrimeConst* __restrict__ pc) {
   extern __shared__ __align__(16) u64 stage[];  // [2 rounds][kDotWords][kT]
-  const int y = (int)blockIdx.y, poly = y & 1, job = (y >> 1) % b.njobs, j = (y >> 1) / b.njobs;
+  const int y = (int)blockIdx.y, job = y % b.njobs, j = y / b.njobs;
   const DotJob& J = b.jobs[job];
   const int t = b.t, rows = t + b.np;
   const int tower = j < t ? j : b.nq + (j - t), prow = j < t ? j : b.pt_prow + (j - t);
   const int tid = threadIdx.x;
   const size_t n = (size_t)blockIdx.x * kT + tid;
-  const size_t co = ((size_t)poly * rows + j) * r.N + n, po = (size_t)prow * r.N + n;
+  const size_t c0 = (size_t)j * r.N + n, c1 = ((size_t)rows + j) * r.N + n, po = (size_t)prow * r.N + n;
   const unsigned long long pm = J.pmask;
   const int rounds = (b.bs + 3) / 4;
   auto issue = [&](int round) {
@@ -529,16 +529,17 @@ __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBa
         const bool on = bb < b.bs && ((pm >> (g * 16 + (bb & 15))) & 1ull);
         any = any || on;
         const u64* src = on ? b.pt_base + (size_t)((J.g + g) * b.bs + bb) * b.pt_stride + po : b.pt_base;
-        cp_async8(buf + (4 + u * kDotG + g) * kT, src, on);
+        cp_async8(buf + (8 + u * kDotG + g) * kT, src, on);
       }
-      const u64* ct = !any ? J.rot0 : bb == 0 ? J.rot0 + co : J.rot_base + (size_t)(bb - 1) * b.rot_stride + co;
-      cp_async8(buf + u * kT, ct, any);
+      const u64* ct = !any ? J.rot0 : bb == 0 ? J.rot0 : J.rot_base + (size_t)(bb - 1) * b.rot_stride;
+      cp_async8(buf + (2 * u) * kT, any ? ct + c0 : ct, any);
+      cp_async8(buf + (2 * u + 1) * kT, any ? ct + c1 : ct, any);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  Acc4 A[kDotG];
+  Acc4 A[kDotG][2];
 #pragma unroll
-  for (int g = 0; g < kDotG; g++) A[g] = Acc4{0, 0, 0, 0};
+  for (int g = 0; g < kDotG; g++) A[g][0] = A[g][1] = Acc4{0, 0, 0, 0};
   issue(0);
 #pragma unroll 1
   for (int round = 0; round < rounds; round++) {
@@ -551,12 +552,15 @@ __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBa
     const u64* buf = stage + (size_t)(round & 1) * kDotWords * kT + tid;
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const u64 x = buf[u * kT];
-      const uint32_t xl = (uint32_t)(x & kMask30), xh = (uint32_t)(x >> 30);
+      const u64 x0 = buf[(2 * u) * kT], x1 = buf[(2 * u + 1) * kT];
+      const uint32_t l0 = (uint32_t)(x0 & kMask30), h0 = (uint32_t)(x0 >> 30);
+      const uint32_t l1 = (uint32_t)(x1 & kMask30), h1 = (uint32_t)(x1 >> 30);
 #pragma unroll
       for (int g = 0; g < kDotG; g++) {
-        const u64 w = buf[(4 + u * kDotG + g) * kT];
-        acc4_mac(A[g], xl, xh, (uint32_t)(w & kMask30), (uint32_t)(w >> 30));
+        const u64 w = buf[(8 + u * kDotG + g) * kT];
+        const uint32_t wl = (uint32_t)(w & kMask30), wh = (uint32_t)(w >> 30);
+        acc4_mac(A[g][0], l0, h0, wl, wh);
+        acc4_mac(A[g][1], l1, h1, wl, wh);
       }
     }
   }
@@ -565,8 +569,11 @@ __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBa
   for (int g = 0; g < kDotG; g++) {
     if (g >= J.ng) break;
     u64 hi = 0, lo = 0;
-    acc4_fold(A[g], hi, lo);
-    J.out[(size_t)g * b.out_stride + co] = reduce128_fast(hi, lo, P);
+    acc4_fold(A[g][0], hi, lo);
+    J.out[(size_t)g * b.out_stride + c0] = reduce128_fast(hi, lo, P);
+    hi = lo = 0;
+    acc4_fold(A[g][1], hi, lo);
+    J.out[(size_t)g * b.out_stride + c1] = reduce128_fast(hi, lo, P);
   }
 }
 
@@ -830,7 +837,7 @@ cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc,
     if (e != cudaSuccess) return e;
     attr_done = true;
   }
-  ptdot_kernel<<<dim3(r.N / kT, 2 * (b.t + b.np) * b.njobs, 1), kT, smem, s>>>(bb, r, pc);
+  ptdot_kernel<<<dim3(r.N / kT, (b.t + b.np) * b.njobs, 1), kT, smem, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
