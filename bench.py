@@ -773,7 +773,7 @@ def ntt_bench(args, dev, stream):
                     "ntt_gbs": round(ach, 1), "intt_gbs": round(algo / (i_ms / 1e3) / 1e9, 1),
                     "ntt_frac_of_hbm": round(ach / peak, 4),
                     "limbs_per_launch": 640, "algorithmic_bytes_per_launch": algo},
-        "roofline": {"kernel": "ntt16_fwd_kernel<16> (config 2: 16 polys x 40 primes, N=2^16)",
+        "roofline": {"kernel": "ntt16_fwd_kernel<16,13> (config 2: 16 polys x 40 primes, N=2^16)",
                      "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "peak_kind": f"{kind} burst copy",
                      "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": traffic},
     }
