@@ -535,7 +535,6 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
   if (!valid_ctx(ctx) || (!ops && n)) return fail(FIDES_EINVAL, "null argument");
   if (n == 0) return FIDES_OK;
   fgb::Context* c = ctx->c;
-  if (chunk == 0) chunk = n;
   for (uint32_t i = 0; i < n; i++) {
     const fides_host_op& o = ops[i];
     const bool binary = o.op == FIDES_OP_ADD || o.op == FIDES_OP_SUB || o.op == FIDES_OP_MULT;
@@ -557,8 +556,19 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
   };
   int rc = FIDES_OK;
   std::vector<fides_op> fo(n);
-  for (uint32_t k0 = 0; k0 < n && rc == FIDES_OK; k0 += chunk) {
-    const uint32_t k1 = std::min(n, k0 + chunk);
+  std::vector<uint32_t> bounds{0};  // chunk k = requests bounds[k] .. bounds[k+1]-1
+  if (chunk == 0 && n >= 16) {      // automatic: chunks of 8, the first and the last of 4 (shorter fill and drain)
+    bounds.push_back(4);
+    while (bounds.back() + 12 <= n) bounds.push_back(bounds.back() + 8);
+    if (n - bounds.back() > 4) bounds.push_back(n - 4);
+    bounds.push_back(n);
+  } else {
+    const uint32_t c = chunk ? chunk : n;
+    for (uint32_t k = c; k < n; k += c) bounds.push_back(k);
+    bounds.push_back(n);
+  }
+  for (size_t ci = 0; ci + 1 < bounds.size() && rc == FIDES_OK; ci++) {
+    const uint32_t k0 = bounds[ci], k1 = bounds[ci + 1];
     // copy in (input handles are registered now; their memory is ready once ev_in has passed)
     std::vector<uint32_t> inputs;
     for (uint32_t i = k0; i < k1 && rc == FIDES_OK; i++) {
