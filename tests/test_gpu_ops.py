@@ -223,6 +223,28 @@ def test_host_batch_pipelined_equals_oracle(env, chunk):
         assert m.towers == e.shape[1]
 
 
+def test_host_batch_automatic_chunks(env):
+    """chunk = 0 with 21 requests runs chunks of 4, 8, 5 and 4 (the automatic schedule): every output equals the
+    oracle's."""
+    import fideslib_gb300 as F
+    nq = env.nq
+    g1, k1 = env.rot_key(1)
+    ops, expect = [], []
+    for i in range(21):
+        t = 2 + i % (nq - 1)
+        ct = env.at(t)
+        out = np.zeros_like(ct)
+        if i % 2:
+            ops.append((F.OP_ROTATE, ct, None, 1, out, env.scale))
+            expect.append(env.orc.rotate(ct, g1, k1))
+        else:
+            ops.append((F.OP_ADD, ct, ct, 0, out, env.scale))
+            expect.append(env.orc.add(ct, ct))
+    env.gpu.eval_batch_host(ops, 0)
+    for (code, a, b, idx, out, _), e in zip(ops, expect):
+        assert np.array_equal(out, e), code
+
+
 def test_batched_rotations_full_ring_cfg3(engine_lib):
     """Config-3 shape at full size: N=2^16, 30 Q towers (60 + 29x50 bits), 10 special 60-bit primes, dnum=3.
     Four ciphertexts at levels 0, 13, 21, 28 rotated in one batch (two of them twice, sharing a ModUp):
