@@ -831,12 +831,11 @@ cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc,
         if (b.present[(J.g + g) * b.bs + k]) J.pmask |= 1ull << (g * 16 + k);
   }
   const size_t smem = sizeof(u64) * 2 * kDotWords * kT;
-  static bool attr_done = false;
-  if (!attr_done) {
-    const cudaError_t e = cudaFuncSetAttribute(ptdot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_done = true;
-  }
+  static std::atomic<unsigned long long> attr_done{0};
+  const cudaError_t ea = once_per_device(attr_done, [&] {
+    return cudaFuncSetAttribute(ptdot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  if (ea != cudaSuccess) return ea;
   ptdot_kernel<<<dim3(r.N / kT, (b.t + b.np) * b.njobs, 1), kT, smem, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();

@@ -4,11 +4,27 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "arith.cuh"
 
 namespace fgb {
 
 constexpr int kMaxJobs = 64;
+
+// Runs `set` (a kernel attribute such as its dynamic shared-memory limit, which applies per device) once per device
+// of the process; safe to call from several host threads.
+template <class F>
+inline cudaError_t once_per_device(std::atomic<unsigned long long>& done, F set) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  e = set();
+  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 // CRT tables resident on the device (built once per context, Context::build).
 struct CrtTables {

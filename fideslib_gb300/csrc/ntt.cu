@@ -22,6 +22,9 @@
 // two-wavefront minimum of 64-bit accesses.
 #include <cooperative_groups.h>
 
+#include <atomic>
+
+#include "kernels.cuh"
 #include "ntt.cuh"
 
 namespace cg = cooperative_groups;
@@ -498,14 +501,14 @@ template <int LOGN, int LOGE>
 cudaError_t launch16(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape16<LOGN, LOGE>;
   auto kern = inverse ? ntt16_inv_kernel<LOGN, LOGE> : ntt16_fwd_kernel<LOGN, LOGE>;
-  static bool attr_done[2] = {false, false};
+  static std::atomic<unsigned long long> attr_done[2];
   const size_t smem = sizeof(u64) * S::E;
-  if (!attr_done[inverse]) {
+  const cudaError_t ea = once_per_device(attr_done[inverse], [&] {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess && S::C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-    attr_done[inverse] = true;
-  }
+    return e;
+  });
+  if (ea != cudaSuccess) return ea;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(S::C, b.limb_begin[b.njobs], 1);
   cfg.blockDim = dim3(kThreads16, 1, 1);
@@ -528,13 +531,12 @@ template <int LOGN>
 cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape<LOGN>;
   auto kern = inverse ? ntt_inv_kernel<LOGN> : ntt_fwd_kernel<LOGN>;
-  static bool attr_done[2] = {false, false};
+  static std::atomic<unsigned long long> attr_done[2];
   const size_t smem = sizeof(u64) * S::E;
-  if (!attr_done[inverse]) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_done[inverse] = true;
-  }
+  const cudaError_t ea = once_per_device(attr_done[inverse], [&] {
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  if (ea != cudaSuccess) return ea;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(S::C, b.limb_begin[b.njobs], 1);
   cfg.blockDim = dim3(kThreads, 1, 1);
