@@ -146,6 +146,7 @@ Context* Context::create(int logN, int nq, int np, int dnum, const u64* moduli, 
     return nullptr;
   }
   Context* c = new Context();
+  cudaGetDevice(&c->device);
   c->logN = logN;
   c->N = 1 << logN;
   c->nq = nq;

@@ -68,6 +68,7 @@ class Context {
   static Context* create(int logN, int nq, int np, int dnum, const u64* moduli, const u64* roots, std::string* err);
 
   int N = 0, logN = 0, nq = 0, np = 0, dnum = 0, alpha = 0, ntow = 0;
+  int device = 0;  // the CUDA device current at creation; every call on the context runs on it
   std::vector<u64> mod, psi;
   cudaStream_t stream = nullptr;      // stream all work is ordered on
   cudaStream_t own_stream = nullptr;  // the context's own stream

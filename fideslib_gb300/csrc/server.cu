@@ -57,6 +57,7 @@ struct fides_server {
   fides_bootstrap_plan plan{};  // cheb_coeffs points into coeffs
   std::vector<double> coeffs;
   uint32_t N = 0, np = 0, nq = 0, alpha = 1;
+  int device = 0;  // current at fides_server_create: the context's device
   std::thread worker;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -86,6 +87,7 @@ struct fides_server {
 
   // Worker loop: admit -> launch (up to max_inflight batches queued) -> retire completed batches.
   void run() {
+    cudaSetDevice(device);  // a new thread starts on device 0; the context lives on the creator's device
     cudaStream_t stream = (cudaStream_t)fides_ctx_stream(ctx);
     std::deque<InFlight> inflight;
     size_t inflight_bytes = 0;
@@ -220,6 +222,7 @@ int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_se
   s->nq = shape.nq;
   s->np = shape.np;
   s->alpha = shape.alpha ? shape.alpha : 1;
+  cudaGetDevice(&s->device);
   s->worker = std::thread([s] { s->run(); });
   *out = s;
   return FIDES_OK;

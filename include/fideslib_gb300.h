@@ -69,7 +69,9 @@ const char* fides_version(void);
 int fides_find_primes(uint32_t bits, uint32_t count, uint64_t two_n, const uint64_t* exclude, uint32_t nexclude,
                       uint64_t* out);
 
-/* Context (LoadContext, api/CryptoContext.cpp:199-249). */
+/* Context (LoadContext, api/CryptoContext.cpp:199-249).  The context lives on the CUDA device current when it is
+ * created; make that device current in any other host thread that calls into it (fides_server_create records it
+ * for its worker thread). */
 int fides_ctx_create(const fides_params* params, fides_ctx** out);
 int fides_ctx_destroy(fides_ctx* ctx);
 /* The moduli and primitive 2N-th roots actually used (nq + np entries each). */
