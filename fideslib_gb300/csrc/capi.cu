@@ -340,11 +340,17 @@ int fides_ct_load_device(fides_ctx* ctx, const uint64_t* dev_data, const fides_c
 int fides_ct_meta_get(fides_ctx* ctx, uint32_t handle, fides_ct_meta* meta) {
   if (!valid_ctx(ctx) || !meta) return fail(FIDES_EINVAL, "null argument");
   fgb::DevCt* ct = find_ct(ctx, handle);
-  if (!ct) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+  bool ext = false;
+  if (!ct) {
+    auto it = ctx->c->ext_cts.find(handle);
+    if (it == ctx->c->ext_cts.end()) return fail(FIDES_EINVAL, "unknown ciphertext handle");
+    ct = &it->second;
+    ext = true;
+  }
   meta->towers = (uint32_t)ct->t;
   meta->noise_deg = (uint32_t)ct->noise_deg;
   meta->slots = (uint32_t)ct->slots;
-  meta->reserved = 0;
+  meta->reserved = ext ? (uint32_t)ctx->c->np : 0;
   meta->scale = ct->scale;
   return FIDES_OK;
 }

@@ -57,7 +57,7 @@ typedef struct {
   uint32_t towers;          /* active Q towers t */
   uint32_t noise_deg;       /* noise scale degree */
   uint32_t slots;
-  uint32_t reserved;
+  uint32_t reserved;        /* fides_ct_meta_get: the special rows of an extended-basis ciphertext (else 0) */
   double scale;             /* scaling factor */
 } fides_ct_meta;
 
