@@ -605,12 +605,14 @@ class BootstrapPlan(C.Structure):
                 ("lt_cts", C.c_uint32 * 4), ("stc_count", C.c_uint32), ("lt_stc", C.c_uint32 * 4),
                 ("sse", C.c_uint32), ("sse_to_sparse", C.c_uint32), ("sse_to_dense", C.c_uint32),
                 ("cheb_coeffs", C.POINTER(C.c_double)), ("cheb_n", C.c_uint32), ("double_angle", C.c_uint32),
-                ("cheb_lo", C.c_double), ("cheb_hi", C.c_double), ("const_scale", C.c_double)]
+                ("cheb_lo", C.c_double), ("cheb_hi", C.c_double), ("const_scale", C.c_double),
+                ("prescale", C.c_double)]
 
     @classmethod
     def make(cls, slots: int, raise_towers: int, lt_cts, lt_stc, coeffs: np.ndarray, double_angle: int,
-             lo: float, hi: float, const_scale: float, sse_keys=None) -> "BootstrapPlan":
-        """lt_cts / lt_stc: factor handles in application order; sse_keys: (to_sparse_id, to_dense_id) or None.
+             lo: float, hi: float, const_scale: float, sse_keys=None, prescale: float = 0.0) -> "BootstrapPlan":
+        """lt_cts / lt_stc: factor handles in application order; sse_keys: (to_sparse_id, to_dense_id) or None;
+        prescale: 0 for a prescaled input, else the factor of the input's adjustment multiply-and-rescale.
         Keeps a reference to the coefficient buffer for the plan's lifetime."""
         c = np.ascontiguousarray(np.array(coeffs, dtype=np.float64))
         p = cls()
@@ -625,6 +627,7 @@ class BootstrapPlan(C.Structure):
         p.cheb_coeffs = c.ctypes.data_as(C.POINTER(C.c_double))
         p.cheb_n, p.double_angle = len(c), double_angle
         p.cheb_lo, p.cheb_hi, p.const_scale = lo, hi, const_scale
+        p.prescale = prescale
         p._coeffs = c
         return p
 

@@ -8,6 +8,7 @@
 // diagonals are supplied by the caller through fides_lt_create_strided, the way FIDESlib receives its
 // bootstrap plaintexts from OpenFHE (RawCiphertext.cu AddBootstrapPrecomputation); only the homomorphic
 // evaluation runs here.  For n = slots and each input ciphertext:
+//   0. (prescale != 0) x = Rescale(x * round(prescale * q_top)), q_top the top prime of x
 //   1. (sse)  x = KeySwitch_{dense->sparse}(x dropped to one tower)
 //   2.        x = ModRaise(x) to raise_towers towers;  (sse) x = KeySwitch_{sparse->dense}(x)
 //   3.        x = x + rot_r(x) for r = n, 2n, ..., N/4        (trace onto the n-slot subring; n < N/2 only)
@@ -55,14 +56,26 @@ int bootstrap(fides_ctx* ctx, const V& in, const fides_bootstrap_plan* p, V& out
   uint64_t moduli[64];
   FGB_TRY(fides_ctx_moduli(ctx, moduli, nullptr));
   const size_t m = in.size();
+  Scope sc(ctx);
+  V x = in;
+  if (p->prescale != 0.0) {  // the reference's ModRaise adjustment (its `prescaled` = false)
+    std::vector<double> top(m);
+    for (size_t i = 0; i < m; i++) {
+      const uint32_t t = fgb::vec::towers_of(ctx, x[i]);
+      if (t < 2) return fgb::set_last_error(FIDES_EINVAL, "prescaling needs an input of at least two towers");
+      top[i] = (double)moduli[t - 1];
+    }
+    V y, z;
+    FGB_TRY(fgb::vec::mult_scalar_at(sc, x, p->prescale, top, y));
+    FGB_TRY(fgb::vec::rescale(sc, y, z));
+    x = z;
+  }
   std::vector<double> k_over_2pi(2 * m);
   for (size_t i = 0; i < m; i++) {
-    const double scale_in = fgb::vec::scale_of(ctx, in[i]);
+    const double scale_in = fgb::vec::scale_of(ctx, x[i]);
     if (!(scale_in > 0)) return fgb::set_last_error(FIDES_EINVAL, "unknown ciphertext handle");
     k_over_2pi[i] = k_over_2pi[m + i] = (double)moduli[0] / scale_in / (2.0 * M_PI);
   }
-  Scope sc(ctx);
-  V x = in;
   if (p->sse) {
     V low, sw;
     FGB_TRY(fgb::vec::drop_to(sc, x, std::vector<uint32_t>(m, 1), low));

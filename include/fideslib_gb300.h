@@ -310,6 +310,9 @@ typedef struct {
   uint32_t double_angle;
   double cheb_lo, cheb_hi;    /* approximation interval in slot values r */
   double const_scale;         /* scale for the constants of EvalMod */
+  double prescale;            /* 0: the input is prescaled (the reference's `prescaled`); else the input (>= 2
+                                 towers) is first multiplied by this factor, encoded at its top prime, and
+                                 rescaled (ModRaise's adjustment, src/CKKS/Bootstrap.cu:441-484) */
 } fides_bootstrap_plan;
 int fides_eval_bootstrap(fides_ctx* ctx, uint32_t ct, const fides_bootstrap_plan* plan, uint32_t* out);
 /* m bootstraps in flight together: every step batched over all m ciphertexts (equal results to m single calls;

@@ -78,9 +78,13 @@ class Setup:
         z = (rng.uniform(-1, 1, self.slots) + 1j * rng.uniform(-1, 1, self.slots)) * 0.5
         return z, self.orc.encrypt(seed, self.s, self.orc.encode(z, DELTA_M, 1))
 
-    def replay(self, ct):
+    def replay(self, ct, prescale=0.0):
         """The recipe of fideslib_gb300/csrc/bootstrap.cu on the oracle, op for op."""
         orc, sim = self.orc, Sim(self.orc, self.mods, self.rlk)
+        scale_in = DELTA_M
+        if prescale:
+            ct, scale_in = sim.rescale(sim.mult_scalar((ct, DELTA_M), prescale, float(self.mods[ct.shape[1] - 1])))
+        K = self.mods[0] / scale_in
         x = ct
         if self.sse:
             x = orc.key_switch(np.ascontiguousarray(x[:, :1]), self.sse[0])
@@ -91,7 +95,7 @@ class Setup:
         while r < N // 2:
             x = orc.add(x, orc.rotate(x, *self.keys[r]))
             r <<= 1
-        v = (x, DELTA_M)
+        v = (x, scale_in)
         for f in self.cts:
             v = sim.rescale((f.replay(orc, v[0], self.keys, N), v[1] * DELTA_PT))
         c = orc.rotate(v[0], *self.conj)
@@ -101,7 +105,7 @@ class Setup:
             y = sim.chebyshev(h, list(self.coeffs), self.lo, self.hi, DELTA_PT)
             for _ in range(R_DOUBLE):
                 y = sim.add_scalar(sim.mult_int(sim.rescale(sim.mult(y, y)), 2), -1.0)
-            modded.append(sim.rescale(sim.mult_scalar(y, self.K / (2 * np.pi), DELTA_PT)))
+            modded.append(sim.rescale(sim.mult_scalar(y, K / (2 * np.pi), DELTA_PT)))
         w = (orc.add(modded[0][0], orc.mult_monomial(modded[1][0], N // 2)), modded[0][1])
         for f in self.stc:
             w = sim.rescale((f.replay(orc, w[0], self.keys, N), w[1] * DELTA_PT))
@@ -132,6 +136,27 @@ def test_bootstrap_sparse_slots():
     z, ct = st.message(77)
     _, meta = check(st, z, ct, 1e-3)
     assert meta.towers >= 2
+
+
+def test_bootstrap_with_prescale():
+    """plan.prescale != 0 (the reference's ModRaise without `prescaled`): a two-tower input is multiplied by the
+    factor encoded at its top prime and rescaled first; the result is bit-exact against the replay and decrypts to
+    factor * message."""
+    st = Setup(slots=16, budget=(1, 1), sse=False, seed=0x5EED0006)
+    F, gpu, orc = st.F, st.gpu, st.orc
+    rng = np.random.default_rng(81)
+    z = (rng.uniform(-1, 1, st.slots) + 1j * rng.uniform(-1, 1, st.slots)) * 0.5
+    ct = orc.encrypt(81, st.s, orc.encode(z, DELTA_M, 2))
+    plan = F.BootstrapPlan.make(st.slots, NQ, list(st.plan.lt_cts[:st.plan.cts_count]),
+                                list(st.plan.lt_stc[:st.plan.stc_count]), st.coeffs, R_DOUBLE, st.lo, st.hi,
+                                DELTA_PT, prescale=0.5)
+    out = gpu.eval_bootstrap(gpu.load_ciphertext(ct, DELTA_M), plan)
+    got = gpu.store_ciphertext(out)
+    ref, ref_scale = st.replay(ct, prescale=0.5)
+    assert np.array_equal(got, ref)
+    err, bits = st.precision(got, gpu.meta(out).scale, 0.5 * z)
+    print(f"prescaled bootstrap: max slot error {err:.3e} ({bits:.1f} bits)")
+    assert err < 1e-3, err
 
 
 def test_bootstrap_full_slots_level_budget_sse_and_batch():
