@@ -1,12 +1,12 @@
 #!/usr/bin/env python
 """Benchmark of the CKKS hot path on one GB300 (or N independent replicas under torchrun).
 
-Headline workload (BASELINE config 3b): N = 2^16, Q = 30 towers (one 60-bit + 29 x 50-bit primes, all
+Headline workload (config 3b, batched hybrid key-switch rotations): N = 2^16, Q = 30 towers (one 60-bit + 29 x 50-bit primes, all
 = 1 mod 2^17), dnum = 3 with 10 special 60-bit primes; a batch of 64 ciphertexts at levels uniform in 1..29,
 each rotated once by an index from {+-2^k}; 32 rotation keys resident in HBM.  One step = the 64 rotations.
 `value` is HRotate ops/s with inputs resident in HBM; `e2e` is the same through the C ABI from pinned host
 buffers (fides_eval_batch_host: H2D of every input ciphertext, D2H of every result inside the timed region,
-pipelined in chunks of 8 requests across copy and compute streams).
+pipelined in chunks of 4, 8, ..., 8, 4 requests across copy and compute streams).
 
 Alongside: config 3a (one ciphertext, 32 hoisted rotations), config 4 (served request stream), config 5
 (eight full-slot bootstraps in flight) and config 2 (batched NTT -> INTT over 16 polynomials x 40 primes at
@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -114,7 +115,7 @@ class Clocks:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"fides_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)

@@ -34,7 +34,7 @@ def build() -> str:
 
 
 def build_ref() -> str | None:
-    """Compile the reference CPU NTT when the reference tree is present (not on the GPU machine)."""
+    """Compile the reference CPU NTT when the reference tree is present on this host."""
     r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(r.stdout + r.stderr)
