@@ -369,23 +369,24 @@ __global__ void __launch_bounds__(kT) ext_epilogue_kernel(const __grid_constant_
   }
 }
 
+// Element-wise kernels move two coefficients per thread (16-byte accesses); grid.x = N / (2 kT).
+__device__ __forceinline__ ulonglong2 ld2(const u64* p) { return *reinterpret_cast<const ulonglong2*>(p); }
+__device__ __forceinline__ void st2(u64* p, ulonglong2 v) { *reinterpret_cast<ulonglong2*>(p) = v; }
+
 __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ TensorBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const TensorJob& J = b.jobs[z];
   const int j = (int)blockIdx.y - b.row_begin[z];
-  const size_t o = (size_t)j * r.N + blockIdx.x * kT + threadIdx.x;
+  const size_t o = (size_t)j * r.N + ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
   const size_t P = (size_t)J.t * r.N;
   const PrimeConst& c = pc[j];
-  const u64 x0 = J.x[o], x1 = J.x[P + o], y0 = J.y[o], y1 = J.y[P + o];
-  J.d[o] = mul_mod(x0, y0, c);
-  J.d[P + o] = add_mod(mul_mod(x0, y1, c), mul_mod(x1, y0, c), c.p);
-  J.d[2 * P + o] = mul_mod(x1, y1, c);
+  const ulonglong2 x0 = ld2(J.x + o), x1 = ld2(J.x + P + o), y0 = ld2(J.y + o), y1 = ld2(J.y + P + o);
+  st2(J.d + o, make_ulonglong2(mul_mod(x0.x, y0.x, c), mul_mod(x0.y, y0.y, c)));
+  st2(J.d + P + o, make_ulonglong2(add_mod(mul_mod(x0.x, y1.x, c), mul_mod(x1.x, y0.x, c), c.p),
+                                   add_mod(mul_mod(x0.y, y1.y, c), mul_mod(x1.y, y0.y, c), c.p)));
+  st2(J.d + 2 * P + o, make_ulonglong2(mul_mod(x1.x, y1.x, c), mul_mod(x1.y, y1.y, c)));
 }
-
-// Element-wise kernels move two coefficients per thread (16-byte accesses); grid.x = N / (2 kT).
-__device__ __forceinline__ ulonglong2 ld2(const u64* p) { return *reinterpret_cast<const ulonglong2*>(p); }
-__device__ __forceinline__ void st2(u64* p, ulonglong2 v) { *reinterpret_cast<ulonglong2*>(p) = v; }
 
 __global__ void __launch_bounds__(kT) addsub_kernel(const __grid_constant__ AddBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
@@ -410,15 +411,14 @@ __global__ void __launch_bounds__(kT) rescale_switch_kernel(const __grid_constan
   const RescaleJob& J = b.jobs[z];
   const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
   const int poly = row >= t - 1 ? 1 : 0, i = row - poly * (t - 1);
-  const int n = blockIdx.x * kT + threadIdx.x;
+  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
   const PrimeConst& om = pc[t - 1];
   const PrimeConst& nm = pc[i];
   const u64 om_mod_nm = shoup(om.p, 1ull, nm.one_sh, nm.p);
-  const u64 diff = nm.p - om_mod_nm;
-  u64 v = J.top[(size_t)poly * r.N + n];
-  if (v > (om.p >> 1)) v += diff;
-  v = shoup(v, 1ull, nm.one_sh, nm.p);
-  J.tmp[((size_t)poly * (t - 1) + i) * r.N + n] = v;
+  const u64 diff = nm.p - om_mod_nm, half = om.p >> 1;
+  const ulonglong2 v = ld2(J.top + (size_t)poly * r.N + n);
+  auto sw = [&](u64 x) { return shoup(x > half ? x + diff : x, 1ull, nm.one_sh, nm.p); };
+  st2(J.tmp + ((size_t)poly * (t - 1) + i) * r.N + n, make_ulonglong2(sw(v.x), sw(v.y)));
 }
 
 __global__ void __launch_bounds__(kT) rescale_epilogue_kernel(const __grid_constant__ RescaleBatch b, Ring r,
@@ -427,14 +427,14 @@ __global__ void __launch_bounds__(kT) rescale_epilogue_kernel(const __grid_const
   const RescaleJob& J = b.jobs[z];
   const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
   const int poly = row >= t - 1 ? 1 : 0, i = row - poly * (t - 1);
-  const int n = blockIdx.x * kT + threadIdx.x;
+  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
   const u64 q = pc[i].p;
   const ulonglong2 w = c.rs_qinv[(size_t)(t - 1) * c.nq + i];
-  const u64 a = J.x[((size_t)poly * t + i) * r.N + n];
-  const u64 bb = J.tmp[((size_t)poly * (t - 1) + i) * r.N + n];
-  J.out[((size_t)poly * (t - 1) + i) * r.N + n] = shoup(sub_mod(a, bb, q), w.x, w.y, q);
+  const ulonglong2 a = ld2(J.x + ((size_t)poly * t + i) * r.N + n);
+  const ulonglong2 bb = ld2(J.tmp + ((size_t)poly * (t - 1) + i) * r.N + n);
+  st2(J.out + ((size_t)poly * (t - 1) + i) * r.N + n,
+      make_ulonglong2(shoup(sub_mod(a.x, bb.x, q), w.x, w.y, q), shoup(sub_mod(a.y, bb.y, q), w.x, w.y, q)));
 }
-
 
 __global__ void __launch_bounds__(kT) ptop_kernel(const __grid_constant__ PtBatch b, Ring r,
                                                   const PrimeConst* __restrict__ pc) {
@@ -750,7 +750,7 @@ cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const Pri
   if (b.njobs <= 0) return cudaSuccess;
   TensorBatch bb;
   const int rows = with_rows(b, bb, [](const TensorJob& j) { return j.t; });
-  dim3 grid(r.N / kT, rows, 1);
+  dim3 grid(r.N / (2 * kT), rows, 1);
   tensor_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
@@ -772,7 +772,7 @@ cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, 
   RescaleBatch bb;
   const int rows = with_rows(b, bb, [](const RescaleJob& j) { return 2 * (j.t - 1); });
   if (rows <= 0) return cudaSuccess;
-  dim3 grid(r.N / kT, rows, 1);
+  dim3 grid(r.N / (2 * kT), rows, 1);
   rescale_switch_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
@@ -784,7 +784,7 @@ cudaError_t launch_rescale_epilogue(const RescaleBatch& b, const Ring& r, const 
   RescaleBatch bb;
   const int rows = with_rows(b, bb, [](const RescaleJob& j) { return 2 * (j.t - 1); });
   if (rows <= 0) return cudaSuccess;
-  dim3 grid(r.N / kT, rows, 1);
+  dim3 grid(r.N / (2 * kT), rows, 1);
   rescale_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
