@@ -243,14 +243,33 @@ bool Context::build(const u64* roots, std::string* err) {
       inv[(size_t)i * N + k] = make_ulonglong2(b, shoup_of(b, p));
     }
   });
+  // The NTT kernels read the twiddles of their last four stages (s >= logN - 4, the 16-residue groups of pass C)
+  // from a transposed copy: entry m + G*nw + j (m = 2^s, nw = m / (N/16) twiddles per group G) is stored at
+  // m + j*(N/16) + G, so the lanes of a warp (consecutive groups) read consecutive entries.
+  std::vector<ulonglong2> fwd_t(fwd), inv_t(inv);
+  const int groups = N >> 4;
+  parallel_for(ntow, [&](int i) {
+    const size_t base = (size_t)i * N;
+    for (int s = logN - 4; s < logN; s++) {
+      const int m = 1 << s, nw = m / groups;
+      for (int G = 0; G < groups; G++)
+        for (int j = 0; j < nw; j++) {
+          fwd_t[base + m + (size_t)j * groups + G] = fwd[base + m + (size_t)G * nw + j];
+          inv_t[base + m + (size_t)j * groups + G] = inv[base + m + (size_t)G * nw + j];
+        }
+    }
+  });
+  ulonglong2* d_psi = (ulonglong2*)dmalloc(sizeof(ulonglong2) * fwd.size());
   ulonglong2* d_fwd = (ulonglong2*)dmalloc(sizeof(ulonglong2) * fwd.size());
   ulonglong2* d_inv = (ulonglong2*)dmalloc(sizeof(ulonglong2) * inv.size());
-  if (!d_fwd || !d_inv) {
+  if (!d_psi || !d_fwd || !d_inv) {
     *err = "device allocation failed";
     return false;
   }
-  cudaMemcpy(d_fwd, fwd.data(), sizeof(ulonglong2) * fwd.size(), cudaMemcpyHostToDevice);
-  cudaMemcpy(d_inv, inv.data(), sizeof(ulonglong2) * inv.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_psi, fwd.data(), sizeof(ulonglong2) * fwd.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_fwd, fwd_t.data(), sizeof(ulonglong2) * fwd.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_inv, inv_t.data(), sizeof(ulonglong2) * inv.size(), cudaMemcpyHostToDevice);
+  psi_brev = d_psi;
   tabs.pc = d_pc;
   tabs.tw_fwd = d_fwd;
   tabs.tw_inv = d_inv;
@@ -1011,7 +1030,7 @@ cudaError_t Context::mult_monomial(const u64* x, int t, unsigned k, u64* out, cu
   MonoBatch mb{};
   mb.jobs[0] = MonoJob{x, out, t, k & (2u * N - 1)};
   mb.njobs = 1;
-  return launch_monomial(mb, ring_, d_pc, tabs.tw_fwd, s);
+  return launch_monomial(mb, ring_, d_pc, psi_brev, s);
 }
 
 cudaError_t Context::mod_raise(const u64* x, int t_in, int T, u64* out, cudaStream_t s) {

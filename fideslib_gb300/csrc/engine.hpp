@@ -80,6 +80,7 @@ class Context {
   float ntt_tune_ms[kNttSizeClasses * (kNttFwdVariants + kNttInvVariants)] = {};  // tune_ntt timings
   CrtTables crt{};
   PrimeConst* d_pc = nullptr;
+  const ulonglong2* psi_brev = nullptr;  // [ntow][N] {psi^brev(i), shoup} in natural order (monomial products)
 
   // --- primitives on device memory ---
   cudaError_t ntt(const u64* src, u64* dst, int npolys, int limbs, int first_prime, long long poly_stride,

@@ -59,19 +59,29 @@ __device__ __forceinline__ void gs_bfly(u64& X, u64& Y, const ulonglong2& w, u64
 
 // Radix-2^LOGR stages over x[k] = a[G*2^(LOGS+LOGR) + k*2^LOGS + low] (low < 2^LOGS).  At the sub-stage on
 // bit kb of k the pair distance is 2^(LOGS+kb), the global stage is s = LOGN-1-(LOGS+kb) and the twiddle of
-// the pair whose lower member is k has table index 2^s + G*2^(LOGR-1-kb) + (k >> (kb+1)).
+// the pair whose lower member is k has table index 2^s + G*2^(LOGR-1-kb) + j, j = k >> (kb+1).  The last four
+// stages (LOGS = 0, LOGR = 4: one 16-residue group per thread, consecutive groups in a warp) read the transposed
+// copy of the table, index 2^s + j*(N/16) + G (DeviceTables), so a warp's loads are contiguous.
+template <int LOGR, int LOGS, int LOGN>
+__device__ __forceinline__ const ulonglong2* tw_entry(const ulonglong2* __restrict__ tw, int s, int kb, int G, int j) {
+  if constexpr (LOGS == 0) {
+    static_assert(LOGR == 4, "the transposed twiddle layout covers radix-16 groups");
+    return tw + (1 << s) + j * (1 << (LOGN - 4)) + G;
+  } else {
+    return tw + (1 << s) + G * (1 << (LOGR - 1 - kb)) + j;
+  }
+}
+
 template <int LOGR, int LOGS, int LOGN>
 __device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 negp,
                                           u64 p4) {
 #pragma unroll
   for (int kb = LOGR - 1; kb >= 0; kb--) {
     const int s = LOGN - 1 - (LOGS + kb);
-    const int nw = 1 << (LOGR - 1 - kb);
-    const ulonglong2* row = tw + (1 << s) + G * nw;
 #pragma unroll
     for (int k = 0; k < (1 << LOGR); k++) {
       if (k & (1 << kb)) continue;
-      const ulonglong2 w = __ldg(row + (k >> (kb + 1)));
+      const ulonglong2 w = __ldg(tw_entry<LOGR, LOGS, LOGN>(tw, s, kb, G, k >> (kb + 1)));
       if ((s & 1) == 0)
         ct_bfly<true>(x[k], x[k + (1 << kb)], w, negp, p4);
       else
@@ -86,12 +96,10 @@ __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulon
 #pragma unroll
   for (int kb = 0; kb < LOGR; kb++) {
     const int s = LOGN - 1 - (LOGS + kb);
-    const int nw = 1 << (LOGR - 1 - kb);
-    const ulonglong2* row = tw + (1 << s) + G * nw;
 #pragma unroll
     for (int k = 0; k < (1 << LOGR); k++) {
       if (k & (1 << kb)) continue;
-      const ulonglong2 w = __ldg(row + (k >> (kb + 1)));
+      const ulonglong2 w = __ldg(tw_entry<LOGR, LOGS, LOGN>(tw, s, kb, G, k >> (kb + 1)));
       gs_bfly(x[k], x[k + (1 << kb)], w, negp, p4);
     }
   }

@@ -32,8 +32,11 @@ struct NttBatch {
 
 struct DeviceTables {
   const PrimeConst* pc;      // [ntowers]
-  const ulonglong2* tw_fwd;  // [ntowers][N] {psi^brev(i), shoup}
-  const ulonglong2* tw_inv;  // [ntowers][N] {psi^-brev(i), shoup}
+  // [ntowers][N] {psi^brev(i), shoup} / {psi^-brev(i), shoup}, with the entries of the last four stages transposed:
+  // entry m + G*nw + j of stage s >= logN - 4 (m = 2^s, nw = m*16/N twiddles per 16-residue group G) is stored at
+  // m + j*(N/16) + G
+  const ulonglong2* tw_fwd;
+  const ulonglong2* tw_inv;
   int logN;
   // forward kernel for N >= 2^13 (0 = radix-16 with 8192 residues per CTA; 1 = radix-32/16; 2 = radix-16 with 4096
   // residues per CTA, twice the CTAs per limb), chosen by tune_ntt separately for launches of at most
