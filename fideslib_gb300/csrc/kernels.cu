@@ -185,20 +185,32 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
 // rows, tmax_g its largest tower count and m_g its job count, ordered (tower row, job) with the job fastest, so the
 // m_g blocks that read the same key values are scheduled back to back and a key shared by several ciphertexts (one
 // rotation of a lock-step batch, the relinearisation key of a batch of products) is read from HBM about once, the
-// other reads hitting L2.  A block whose tower lies above its job's level exits.  Every digit's value and both key
-// halves are loaded before any arithmetic; digits are split into 30-bit halves here and key values come split
-// (launch_key_split), accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max); MAXB bounds beta at
-// compile time.  Outputs are left in [0, 4p): the ModDown INTT takes them as they are and both epilogues reduce.
+// other reads hitting L2.  When jobs of different groups share their digits (row_outer, set by the launcher) the
+// rows are ordered (tower row, job) over the whole batch instead, (tmax + np) * njobs rows, so that both the digits
+// and the keys of a row are read about once.  A block whose tower lies above its job's level exits.  Every digit's
+// value and both key halves are loaded before any arithmetic; digits are split into 30-bit halves here and key
+// values come split (launch_key_split), accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max); MAXB
+// bounds beta at compile time.  Outputs are left in [0, 4p): the ModDown INTT takes them as they are and both
+// epilogues reduce.
 template <int MAXB>
 __global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
     ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c, const PrimeConst* __restrict__ pc,
                     int iters) {
-  const int G = find_job(b.row_begin, b.ngroups, (int)blockIdx.y);
-  const int m = b.grp_begin[G + 1] - b.grp_begin[G];
-  const int local = (int)blockIdx.y - b.row_begin[G];
-  const int rr = local / m;
-  const int tmax = (b.row_begin[G + 1] - b.row_begin[G]) / m - c.np;
-  const KsJob& J = b.jobs[b.grp_begin[G] + (local - rr * m)];
+  int q, rr, tmax;
+  if (b.row_outer) {  // block row y = rr * njobs + q
+    q = (int)blockIdx.y % b.njobs;
+    rr = (int)blockIdx.y / b.njobs;
+    tmax = b.jobs[q].t;
+    if (rr >= tmax + c.np) return;  // beyond this job's rows
+  } else {
+    const int G = find_job(b.row_begin, b.ngroups, (int)blockIdx.y);
+    const int m = b.grp_begin[G + 1] - b.grp_begin[G];
+    const int local = (int)blockIdx.y - b.row_begin[G];
+    rr = local / m;
+    tmax = (b.row_begin[G + 1] - b.row_begin[G]) / m - c.np;
+    q = b.grp_begin[G] + (local - rr * m);
+  }
+  const KsJob& J = b.jobs[q];
   const int t = J.t;
   const int tower = rr < tmax ? rr : c.nq + (rr - tmax);
   if (tower < c.nq && tower >= t) return;  // a Q tower above this job's level
@@ -677,6 +689,23 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
     bb.row_begin[++bb.ngroups] = rows;
   }
   bb.grp_begin[bb.ngroups] = k;
+  // Jobs of different key groups that read the same digits (the rotations of one hoisted ModUp: baby steps of a
+  // linear transform, RotateHoisted) would re-read those digits once per group when the groups run one after the
+  // other.  Then the blocks are ordered by tower row first, so every job's blocks of one row run together and the
+  // row's digits and key values are read from HBM about once, the other reads hitting L2.
+  bb.row_outer = 0;
+  for (int i = 0; i < bb.ngroups && !bb.row_outer; i++)
+    for (int x = bb.grp_begin[i]; x < bb.grp_begin[i + 1] && !bb.row_outer; x++)
+      for (int y = bb.grp_begin[i + 1]; y < k; y++)
+        if (bb.jobs[x].a == bb.jobs[y].a && bb.jobs[x].conv == bb.jobs[y].conv) {
+          bb.row_outer = 1;
+          break;
+        }
+  if (bb.row_outer) {
+    int tmax = 0;
+    for (int i = 0; i < k; i++) tmax = std::max(tmax, bb.jobs[i].t);
+    rows = (tmax + c.np) * k;
+  }
   const int iters = std::min(4, r.N / (2 * kT));  // N / 512 is a power of two >= 2
   dim3 grid(r.N / (2 * kT * iters), rows, 1);
   switch (c.dnum) {  // beta <= dnum: size the register arrays exactly (fewer registers, more resident warps)

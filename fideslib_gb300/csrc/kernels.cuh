@@ -72,6 +72,7 @@ struct KsBatch {
                                 // group for the key inner product)
   int ngroups;                  // key inner product: jobs grp_begin[g] .. grp_begin[g+1]-1 share one key
   int grp_begin[kMaxJobs + 1];
+  int row_outer;                // key inner product: block rows ordered (tower row, job) instead of (group, row, job)
   KsJob jobs[kMaxJobs];
 };
 
