@@ -6,7 +6,7 @@ Headline workload (config 3b, batched hybrid key-switch rotations): N = 2^16, Q 
 each rotated once by an index from {+-2^k}; 32 rotation keys resident in HBM.  One step = the 64 rotations.
 `value` is HRotate ops/s with inputs resident in HBM; `e2e` is the same through the C ABI from pinned host
 buffers (fides_eval_batch_host: H2D of every input ciphertext, D2H of every result inside the timed region,
-pipelined in chunks of 4, 8, ..., 8, 4 requests across copy and compute streams).
+pipelined in chunks of 4, 8, ..., 8, 4 requests across copy streams and two compute streams).
 
 Alongside: config 3a (one ciphertext, 32 hoisted rotations), config 4 (served request stream), config 5
 (eight full-slot bootstraps in flight) and config 2 (batched NTT -> INTT over 16 polynomials x 40 primes at
@@ -357,7 +357,7 @@ def run_ours(args, rank, world, dist):
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (keys 3.8 GiB, cts ~1 GiB)"},
         "e2e": {"value": round(64 * world / (e2e_ms / 1e3), 2), "unit": "HRotate ops/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                "path": "fides_eval_batch_host, pinned host buffers, chunks of 4, 8, ..., 8, 4"},
+                "path": "fides_eval_batch_host, pinned host buffers, chunks of 4, 8, ..., 8, 4 on two compute streams"},
         "gpu_launches": int(launches),
         "per_op": {"value": round(64 * world / (per_op_ms / 1e3), 2), "unit": "HRotate ops/s",
                    "ms_per_step": round(per_op_ms, 4), "batched_over_per_op": round(per_op_ms / ms, 3)},

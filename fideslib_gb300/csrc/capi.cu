@@ -533,10 +533,11 @@ static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
   return FIDES_OK;
 }
 
-// Pipelined batch from and to host memory: chunk k's inputs are copied in on one stream while chunk k-1 computes
-// on the context stream and chunk k-2's results are copied out on a third, so the copy engines run beside the
-// kernels.  Inputs and outputs must be pinned host memory for the copies to be asynchronous.  Device memory comes
-// from the stream-ordered pool, whose reuse across the three streams follows their event dependencies.
+// Pipelined batch from and to host memory: chunk k's inputs are copied in on one stream while earlier chunks compute
+// and chunk k-2's results are copied out on another, so the copy engines run beside the kernels.  Consecutive
+// chunks compute on two streams (the context stream and chunk_alt), so one chunk's launches fill the SMs that the
+// other's leave idle.  Inputs and outputs must be pinned host memory for the copies to be asynchronous.  Device
+// memory comes from the stream-ordered pool, whose reuse across the streams follows their event dependencies.
 int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32_t chunk) {
   if (!valid_ctx(ctx) || (!ops && n)) return fail(FIDES_EINVAL, "null argument");
   if (n == 0) return FIDES_OK;
@@ -552,7 +553,9 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
   }
   if (!c->copy_in) CK(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking), "copy stream");
   if (!c->copy_out) CK(cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking), "copy stream");
+  if (!c->chunk_alt) CK(cudaStreamCreateWithFlags(&c->chunk_alt, cudaStreamNonBlocking), "compute stream");
   const size_t limb = (size_t)c->N * sizeof(uint64_t);
+  cudaStream_t const main_stream = c->stream;
   std::vector<cudaEvent_t> events;
   auto event = [&]() {
     cudaEvent_t e;
@@ -573,8 +576,14 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
     for (uint32_t k = c; k < n; k += c) bounds.push_back(k);
     bounds.push_back(n);
   }
+  {  // the second compute stream starts after the work already queued on the context stream
+    cudaEvent_t ev0 = event();
+    cudaEventRecord(ev0, main_stream);
+    cudaStreamWaitEvent(c->chunk_alt, ev0, 0);
+  }
   for (size_t ci = 0; ci + 1 < bounds.size() && rc == FIDES_OK; ci++) {
     const uint32_t k0 = bounds[ci], k1 = bounds[ci + 1];
+    c->stream = (ci & 1) ? c->chunk_alt : main_stream;  // every call below orders its work on this chunk's stream
     // copy in (input handles are registered now; their memory is ready once ev_in has passed)
     std::vector<uint32_t> inputs;
     for (uint32_t i = k0; i < k1 && rc == FIDES_OK; i++) {
@@ -619,6 +628,12 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
       c->free_limbs(r.data, c->copy_out);
       c->cts.erase(it);
     }
+  }
+  c->stream = main_stream;
+  {  // later work on the context stream follows both compute streams
+    cudaEvent_t ev1 = event();
+    cudaEventRecord(ev1, c->chunk_alt);
+    cudaStreamWaitEvent(main_stream, ev1, 0);
   }
   const cudaError_t e1 = cudaStreamSynchronize(c->copy_out), e2 = cudaStreamSynchronize(c->stream);
   for (cudaEvent_t e : events) cudaEventDestroy(e);

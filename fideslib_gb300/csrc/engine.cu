@@ -133,6 +133,7 @@ Context::~Context() {
   for (cudaEvent_t e : side_ev)
     if (e) cudaEventDestroy(e);
   if (copy_out) cudaStreamDestroy(copy_out);
+  if (chunk_alt) cudaStreamDestroy(chunk_alt);
   if (stream) cudaStreamDestroy(stream);
 }
 

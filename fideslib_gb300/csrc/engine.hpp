@@ -73,6 +73,7 @@ class Context {
   cudaStream_t stream = nullptr;      // stream all work is ordered on
   cudaStream_t own_stream = nullptr;  // the context's own stream
   cudaStream_t copy_in = nullptr, copy_out = nullptr;  // copy streams of the pipelined host batch (lazily made)
+  cudaStream_t chunk_alt = nullptr;  // compute stream of the pipelined host batch's odd chunks (lazily made)
   cudaStream_t side = nullptr;                         // second stream of split key-switch batches (lazily made)
   cudaEvent_t side_ev[2] = {nullptr, nullptr};
 

@@ -341,8 +341,8 @@ int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n);
 /* The same from and to host memory, pipelined (no counterpart in the reference, whose API loads, evaluates and
  * stores one ciphertext per call, api/CryptoContext.cpp:270-289): requests run in chunks of `chunk` (0 = automatic:
  * chunks of 8 with a first and last chunk of 4, which shortens the pipeline's fill and drain; one chunk below 16
- * requests); chunk k's inputs are copied to the device while chunk k-1 computes and chunk k-2's results are copied
- * back, on separate streams.  a (and b for ADD / SUB / MULT) are host u64[2][towers][N] with `meta`; out receives
+ * requests); chunk k's inputs are copied to the device while earlier chunks compute and chunk k-2's results are
+ * copied back, on separate streams, and consecutive chunks compute on two streams that overlap on the device.  a (and b for ADD / SUB / MULT) are host u64[2][towers][N] with `meta`; out receives
  * u64[2][out towers][N] and out_meta its metadata.  Returns after every result is in host memory.  Use pinned
  * host buffers: pageable ones make the copies synchronous. */
 typedef struct {
