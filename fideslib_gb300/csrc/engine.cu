@@ -202,6 +202,11 @@ bool Context::build(const u64* roots, std::string* err) {
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
       uint64_t thr = ~0ull;
       cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      // Memory freed on one stream is reused on another only once the free has completed or an event orders the
+      // two: the pool may not make an allocating stream wait on another stream's pending work, which would chain
+      // the copy and compute streams of a pipelined host batch into one sequence.
+      int no = 0;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
     }
   }
 
