@@ -109,6 +109,7 @@ _SIGS = {
     "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "fides_ctx_set_mem_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fides_ctx_mem_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "fides_ctx_set_input_check": (C.c_int, [C.c_void_p, C.c_int]),
     "fides_pt_encode": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                   C.c_uint32, u32p]),
     "fides_pt_decode": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -239,6 +240,10 @@ class CryptoContext:
     def set_stream(self, stream: int | None):
         _check(lib().fides_ctx_set_stream(self._h, None if not stream else C.c_void_p(stream)))
 
+
+    def set_input_check(self, enable: bool = True):
+        """Opt-in check that loaded residues are below their primes (loads refuse others with FIDES_EINVAL)."""
+        _check(lib().fides_ctx_set_input_check(self._h, 1 if enable else 0))
 
     def ntt_host(self, data: np.ndarray, first_prime: int = 0, inverse: bool = False) -> np.ndarray:
         """data: u64[npolys][limbs][N] (host), transformed in place and returned."""

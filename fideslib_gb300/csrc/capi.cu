@@ -63,6 +63,15 @@ int check_ks_shape(fides_ctx* ctx) {
   return FIDES_OK;
 }
 
+// Opt-in validation of a freshly loaded object (fides_ctx_set_input_check): every residue below its prime.
+int check_loaded(fgb::Context* c, const fgb::u64* x, long long rows, int period, int tq, const char* what) {
+  if (!c->input_check) return FIDES_OK;
+  const int r = c->residues_out_of_range(x, rows, period, tq);
+  if (r < 0) return fail(FIDES_ECUDA, std::string(what) + ": residue check failed");
+  if (r > 0) return fail(FIDES_EINVAL, std::string(what) + " has a residue that is not below its tower's prime");
+  return FIDES_OK;
+}
+
 }  // namespace
 
 namespace fgb {
@@ -101,6 +110,12 @@ int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes) {
 int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes) {
   if (!valid_ctx(ctx) || !bytes) return fail(FIDES_EINVAL, "null argument");
   *bytes = ctx->c->mem_in_use;
+  return FIDES_OK;
+}
+
+int fides_ctx_set_input_check(fides_ctx* ctx, int enable) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  ctx->c->input_check = enable != 0;
   return FIDES_OK;
 }
 
@@ -254,6 +269,7 @@ int fides_ntt_batch_host(fides_ctx* ctx, uint64_t* data, uint32_t npolys, uint32
   return rc;
 }
 
+// A key refused by the input check is not loaded: its slot is freed and left null (the caller drops the entry).
 static int load_key(fides_ctx* ctx, const uint64_t* key, bool device, fgb::u64** slot) {
   fgb::Context* c = ctx->c;
   const size_t bytes = (size_t)2 * c->dnum * c->ntow * c->N * sizeof(uint64_t);
@@ -264,6 +280,11 @@ static int load_key(fides_ctx* ctx, const uint64_t* key, bool device, fgb::u64**
   }
   CK(cudaMemcpyAsync(*slot, key, bytes, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
      "key copy");
+  if (int rc = check_loaded(c, *slot, (long long)2 * c->dnum * c->ntow, c->ntow, c->ntow, "key")) {
+    cudaFree(*slot);
+    *slot = nullptr;
+    return rc;
+  }
   CK(fgb::launch_key_split(*slot, bytes / sizeof(uint64_t), c->stream), "key layout");
   CK(cudaStreamSynchronize(c->stream), "key copy");
   return FIDES_OK;
@@ -283,14 +304,18 @@ int fides_load_rotation_key(fides_ctx* ctx, uint32_t galois, const uint64_t* key
   if (!valid_ctx(ctx) || !key) return fail(FIDES_EINVAL, "null argument");
   if ((galois & 1) == 0 || galois >= 2u * ctx->c->N) return fail(FIDES_EINVAL, "Galois element must be odd and < 2N");
   fgb::u64*& slot = ctx->c->rot_keys[galois];
-  return load_key(ctx, key, false, &slot);
+  const int rc = load_key(ctx, key, false, &slot);
+  if (!slot) ctx->c->rot_keys.erase(galois);
+  return rc;
 }
 
 int fides_load_rotation_key_device(fides_ctx* ctx, uint32_t galois, const uint64_t* dev_key) {
   if (!valid_ctx(ctx) || !dev_key) return fail(FIDES_EINVAL, "null argument");
   if ((galois & 1) == 0 || galois >= 2u * ctx->c->N) return fail(FIDES_EINVAL, "Galois element must be odd and < 2N");
   fgb::u64*& slot = ctx->c->rot_keys[galois];
-  return load_key(ctx, dev_key, true, &slot);
+  const int rc = load_key(ctx, dev_key, true, &slot);
+  if (!slot) ctx->c->rot_keys.erase(galois);
+  return rc;
 }
 
 // Switch keys share the rotation-key table under tagged ids that no Galois element (< 2N <= 2^17) can take.
@@ -300,14 +325,18 @@ int fides_load_switch_key(fides_ctx* ctx, uint32_t key_id, const uint64_t* key) 
   if (!valid_ctx(ctx) || !key) return fail(FIDES_EINVAL, "null argument");
   if (key_id & kSwitchKeyTag) return fail(FIDES_EINVAL, "switch key id must be < 2^31");
   fgb::u64*& slot = ctx->c->rot_keys[kSwitchKeyTag | key_id];
-  return load_key(ctx, key, false, &slot);
+  const int rc = load_key(ctx, key, false, &slot);
+  if (!slot) ctx->c->rot_keys.erase(kSwitchKeyTag | key_id);
+  return rc;
 }
 
 int fides_load_switch_key_device(fides_ctx* ctx, uint32_t key_id, const uint64_t* dev_key) {
   if (!valid_ctx(ctx) || !dev_key) return fail(FIDES_EINVAL, "null argument");
   if (key_id & kSwitchKeyTag) return fail(FIDES_EINVAL, "switch key id must be < 2^31");
   fgb::u64*& slot = ctx->c->rot_keys[kSwitchKeyTag | key_id];
-  return load_key(ctx, dev_key, true, &slot);
+  const int rc = load_key(ctx, dev_key, true, &slot);
+  if (!slot) ctx->c->rot_keys.erase(kSwitchKeyTag | key_id);
+  return rc;
 }
 
 static int ct_load_impl(fides_ctx* ctx, const uint64_t* data, const fides_ct_meta* meta, uint32_t* handle,
@@ -325,6 +354,10 @@ static int ct_load_impl(fides_ctx* ctx, const uint64_t* data, const fides_ct_met
   CK(cudaMemcpyAsync(ct.data, data, (size_t)2 * ct.t * c->N * sizeof(uint64_t),
                      device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
      "ciphertext copy");
+  if (int rc = check_loaded(c, ct.data, 2 * ct.t, ct.t, ct.t, "ciphertext")) {
+    c->free_limbs(ct.data, c->stream);
+    return rc;
+  }
   *handle = register_ct(ctx, ct);
   return FIDES_OK;
 }
@@ -456,6 +489,8 @@ static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
     case FIDES_OP_KEY_SWITCH: {
       const bool ks = op.op == FIDES_OP_KEY_SWITCH;
       if (ks && ((uint32_t)op.index & kSwitchKeyTag)) return fail(FIDES_EINVAL, "switch key id must be < 2^31");
+      if (op.op == FIDES_OP_AUTOMORPHISM && (((uint32_t)op.index & 1) == 0 || (uint32_t)op.index >= 2u * c->N))
+        return fail(FIDES_EINVAL, "Galois element must be odd and < 2N");
       const uint32_t g = op.op == FIDES_OP_ROTATE ? fgb::Context::galois_for_index(c->N, op.index)
                          : ks                     ? kSwitchKeyTag | (uint32_t)op.index
                                                   : (uint32_t)op.index;
@@ -853,6 +888,10 @@ int fides_pt_load(fides_ctx* ctx, const uint64_t* data, uint32_t towers, double 
   if (!p.data) return fail(FIDES_ENOMEM, "plaintext allocation failed");
   CK(cudaMemcpyAsync(p.data, data, (size_t)towers * c->N * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream),
      "plaintext copy");
+  if (int rc = check_loaded(c, p.data, p.t, p.t, p.t, "plaintext")) {
+    c->free_limbs(p.data, c->stream);
+    return rc;
+  }
   const uint32_t h = c->next_handle++;
   c->pts[h] = p;
   *handle = h;
@@ -1293,6 +1332,10 @@ int fides_pt_load_ext(fides_ctx* ctx, const uint64_t* data, uint32_t towers, dou
   p.data = c->alloc_limbs(rows, c->stream);
   if (!p.data) return fail(FIDES_ENOMEM, "plaintext allocation failed");
   CK(cudaMemcpyAsync(p.data, data, rows * c->N * sizeof(uint64_t), cudaMemcpyDefault, c->stream), "plaintext copy");
+  if (int rc = check_loaded(c, p.data, (long long)rows, (int)rows, p.t, "plaintext")) {
+    c->free_limbs(p.data, c->stream);
+    return rc;
+  }
   const uint32_t h = c->next_handle++;
   c->pts[h] = p;
   *handle = h;

@@ -185,8 +185,8 @@ int encode_many(fgb::Context* c, const double* re, const double* im, int nv, uin
   for (size_t i = 0; i < host.size(); i++) host[i] = make_double2(re[i], im ? im[i] : 0.0);
   double2* a = nullptr;
   int* ovf = nullptr;
-  if (cudaMallocAsync(&a, host.size() * sizeof(double2), c->stream) != cudaSuccess ||
-      cudaMallocAsync(&ovf, sizeof(int), c->stream) != cudaSuccess)
+  if (cudaMallocFromPoolAsync(&a, host.size() * sizeof(double2), c->pool, c->stream) != cudaSuccess ||
+      cudaMallocFromPoolAsync(&ovf, sizeof(int), c->pool, c->stream) != cudaSuccess)
     return fgb::set_last_error(FIDES_ENOMEM, "encoding workspace allocation failed");
   cudaError_t e = cudaMemcpyAsync(a, host.data(), host.size() * sizeof(double2), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(ovf, 0, sizeof(int), c->stream);
@@ -265,7 +265,7 @@ int fides_pt_decode(fides_ctx* ctx, uint32_t pt, uint32_t slots, double* re, dou
   }
   u64* coeff = c->alloc_limbs(t, c->stream);
   double2* a = nullptr;
-  if (!coeff || cudaMallocAsync(&a, (size_t)n * sizeof(double2), c->stream) != cudaSuccess) {
+  if (!coeff || cudaMallocFromPoolAsync(&a, (size_t)n * sizeof(double2), c->pool, c->stream) != cudaSuccess) {
     c->free_limbs(coeff, c->stream);
     return fgb::set_last_error(FIDES_ENOMEM, "decoding workspace allocation failed");
   }

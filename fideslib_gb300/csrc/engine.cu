@@ -135,6 +135,8 @@ Context::~Context() {
   if (copy_out) cudaStreamDestroy(copy_out);
   if (chunk_alt) cudaStreamDestroy(chunk_alt);
   if (stream) cudaStreamDestroy(stream);
+  // Its allocations were freed above; the pool's cached memory goes back to the device with it.
+  if (pool) cudaMemPoolDestroy(pool);
 }
 
 Context* Context::create(int logN, int nq, int np, int dnum, const u64* moduli, const u64* roots, std::string* err) {
@@ -195,19 +197,26 @@ bool Context::build(const u64* roots, std::string* err) {
     return false;
   }
   stream = own_stream;
-  {  // keep freed stream-ordered allocations cached in the pool
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-      uint64_t thr = ~0ull;
-      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-      // Memory freed on one stream is reused on another only once the free has completed or an event orders the
-      // two: the pool may not make an allocating stream wait on another stream's pending work, which would chain
-      // the copy and compute streams of a pipelined host batch into one sequence.
-      int no = 0;
-      cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+  {  // the context's own stream-ordered pool on its device
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      *err = "cudaMemPoolCreate failed";
+      return false;
     }
+    // Freed allocations stay cached in the pool (the reference's pool keeps a release threshold at the maximum,
+    // src/CKKS/Context.cu:74-80).
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    // Memory freed on one stream is reused on another only once the free has completed or an event orders the
+    // two: the pool may not make an allocating stream wait on another stream's pending work, which would chain
+    // the copy and compute streams of a pipelined host batch into one sequence.
+    int no = 0;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
   }
 
   // per-prime constants
@@ -382,7 +391,7 @@ u64* Context::alloc_limbs(size_t nlimbs, cudaStream_t s) {
   std::lock_guard<std::mutex> lk(mem_mu_);
   if (mem_limit && mem_in_use + bytes > mem_limit) return nullptr;  // the caller reports FIDES_ENOMEM
   void* p = nullptr;
-  if (cudaMallocAsync(&p, bytes, s) != cudaSuccess) {
+  if (cudaMallocFromPoolAsync(&p, bytes, pool, s) != cudaSuccess) {
     cudaGetLastError();  // a failed allocation must not surface as a later launch error
     return nullptr;
   }
@@ -400,6 +409,20 @@ void Context::free_limbs(u64* p, cudaStream_t s) {
     mem_in_use -= it->second;
     mem_sizes_.erase(it);
   }
+}
+
+int Context::residues_out_of_range(const u64* x, long long rows, int period, int tq) {
+  if (!d_bad) {
+    d_bad = (int*)dmalloc(sizeof(int));
+    if (!d_bad) return -1;
+  }
+  int bad = 0;
+  if (cudaMemsetAsync(d_bad, 0, sizeof(int), stream) != cudaSuccess ||
+      launch_range_check(x, rows, logN, period, tq, nq, d_pc, d_bad, stream) != cudaSuccess ||
+      cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return -1;
+  return bad ? 1 : 0;
 }
 
 uint32_t Context::galois_inverse(uint32_t g) const {

@@ -173,7 +173,16 @@ class Context {
   std::unordered_map<uint32_t, DevLT> lts;
   u64* relin_key = nullptr;
 
-  // Stream-ordered pool allocations of ciphertexts and workspaces, counted against mem_limit (0 = none).
+  // Stream-ordered allocations of ciphertexts and workspaces from the context's own memory pool (created on its
+  // device at build time, so the device's default pool and every other user of it keep their settings), counted
+  // against mem_limit (0 = none).
+  cudaMemPool_t pool = nullptr;
+  // Opt-in validation of loaded residues (fides_ctx_set_input_check); d_bad is its device flag.
+  bool input_check = false;
+  int* d_bad = nullptr;
+  // 0 when every residue of x ([rows][N], row r = tower r % period, see launch_range_check) is below its prime,
+  // 1 when one is not, -1 on a CUDA error.  Synchronises the context stream.
+  int residues_out_of_range(const u64* x, long long rows, int period, int tq);
   u64* alloc_limbs(size_t nlimbs, cudaStream_t s);
   void free_limbs(u64* p, cudaStream_t s);
   size_t mem_limit = 0, mem_in_use = 0;

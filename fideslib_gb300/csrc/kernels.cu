@@ -723,6 +723,29 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
   return cudaGetLastError();
 }
 
+// Input validation (opt-in, fides_ctx_set_input_check): sets *bad when a residue is not below its prime.  Row r of
+// x holds tower j = r % period, whose prime is j for j < tq and nq + (j - tq) past it (the special rows of an
+// extended layout).
+__global__ void range_check_kernel(const u64* __restrict__ x, long long rows, int logN, int period, int tq, int nq,
+                                   const PrimeConst* __restrict__ pc, int* bad) {
+  const long long n = rows << logN;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)((i >> logN) % period);
+    if (x[i] >= pc[j < tq ? j : nq + (j - tq)].p) {
+      *bad = 1;
+      return;
+    }
+  }
+}
+
+cudaError_t launch_range_check(const u64* x, long long rows, int logN, int period, int tq, int nq,
+                               const PrimeConst* pc, int* bad, cudaStream_t s) {
+  if (rows <= 0) return cudaSuccess;
+  range_check_kernel<<<1024, kT, 0, s>>>(x, rows, logN, period, tq, nq, pc, bad);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_key_split(u64* key, size_t n, cudaStream_t s) {
   key_split_kernel<<<1024, kT, 0, s>>>(key, n);
   count_launch();

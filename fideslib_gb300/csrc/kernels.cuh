@@ -242,6 +242,10 @@ cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTa
                                     cudaStream_t s);
 cudaError_t launch_ext_epilogue(const KsBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
                                 cudaStream_t s);
+// Sets *bad (device int) when a residue of x ([rows][N]) is not below its prime: row r is tower j = r % period,
+// prime j for j < tq, else nq + (j - tq).
+cudaError_t launch_range_check(const u64* x, long long rows, int logN, int period, int tq, int nq,
+                               const PrimeConst* pc, int* bad, cudaStream_t s);
 // In place: every key residue k becomes (k mod 2^30) | (floor(k / 2^30) << 32), the form ks_inner_kernel reads.
 cudaError_t launch_key_split(u64* key, size_t n, cudaStream_t s);
 cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);

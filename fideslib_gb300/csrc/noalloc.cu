@@ -14,6 +14,8 @@
 //     it zeroed (every region is fully written before it is read), so it is never cleared;
 //   * calls whose GPU work overlaps (different streams, or different host threads) race on the array: order
 //     them on one stream;
+//   * the context's device must be the current device (FIDES_EINVAL otherwise): the array's address differs per
+//     device, and the context's stream and tables live on its own device;
 //   * the first call on a device looks up the array's device address with cudaGetSymbolAddress while that
 //     device is current; make that first call before any stream capture.
 #include <cuda_runtime.h>
@@ -41,11 +43,16 @@ __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocScratchBy
 std::mutex g_setup_mu;
 fgb::u64* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array for the current device (looked up once per device).
-int scratch_for_current_device(fgb::u64** out) {
+// Device address of the scratch array on the context's device `want`, which must be the current device: the
+// array's address is per device, and the context's stream and tables live on `want` (looked up once per device).
+int scratch_for_device(int want, fgb::u64** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fgb::set_last_error(FIDES_ENODEV, "no current CUDA device for the no-alloc scratch");
+  if (dev != want)
+    return fgb::set_last_error(FIDES_EINVAL,
+                               "the current CUDA device is not the context's device; make the context's device "
+                               "current before calling fides_eval_rotate_noalloc");
   std::lock_guard<std::mutex> lk(g_setup_mu);
   if (!g_scratch_ptr[dev]) {
     void* p = nullptr;
@@ -85,10 +92,12 @@ extern "C" int fides_eval_rotate_noalloc(fides_ctx* ctx, const uint64_t* dev_in,
   const size_t ct_bytes = 2 * (size_t)t * NN * sizeof(u64);
   if (overlaps(dev_in, ct_bytes, dev_out, ct_bytes))
     return fgb::set_last_error(FIDES_EINVAL, "output must not overlap the input");
+  if ((galois & 1) == 0 || galois >= 2u * (uint32_t)c->N)
+    return fgb::set_last_error(FIDES_EINVAL, "Galois element must be odd and < 2N");
   auto it = c->rot_keys.find(galois);
   if (it == c->rot_keys.end()) return fgb::set_last_error(FIDES_ENOKEY, "no rotation key for this Galois element");
   u64* ws = nullptr;
-  if (int rc = scratch_for_current_device(&ws)) return rc;
+  if (int rc = scratch_for_device(c->device, &ws)) return rc;
   cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
 
   const u64* a = (const u64*)dev_in + (size_t)t * NN;  // c1

@@ -102,6 +102,12 @@ int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms);
  * transforms are not counted).  fides_ctx_mem_in_use reports the bytes currently counted. */
 int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes);
 int fides_ctx_mem_in_use(fides_ctx* ctx, uint64_t* bytes);
+/* Opt-in validation of loaded residues (no counterpart in the reference, which copies them unchecked): while
+ * enabled, fides_ct_load*, fides_pt_load* and the key loaders check that every residue is below its tower's prime
+ * and refuse the object with FIDES_EINVAL otherwise (a refused key is unloaded, also one previously loaded under the
+ * same name).  The kernels' lazy-reduction bounds assume residues in [0, q); out-of-range input otherwise gives
+ * wrong results silently.  Costs one extra read of the object and a synchronisation per load. */
+int fides_ctx_set_input_check(fides_ctx* ctx, int enable);
 /* Overrides the autotuner's choices for every batch size (all variants give identical residues). */
 int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant, int32_t inv_variant);
 /* Ring and basis shape of a context. */
@@ -365,8 +371,9 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
  * so it rejects, with FIDES_EINVAL, rotations whose workspace (t + beta(t+np) + 2(t+np) + 2t limbs of 8N bytes)
  * exceeds 32 MiB, and it calls no cudaMalloc, cudaFree or other allocating routine.  All calls share that array
  * (it keeps the last call's contents; nothing needs it zeroed): calls whose GPU work overlaps race, so order
- * them on one stream.  The first call on a device looks up the array's address with that device current; make
- * it before any stream capture.  `stream` is a cudaStream_t (NULL = the context stream). */
+ * them on one stream.  The context's device must be the current device (FIDES_EINVAL otherwise).  The first call
+ * on a device looks up the array's address with that device current; make it before any stream capture.
+ * `stream` is a cudaStream_t (NULL = the context stream). */
 int fides_eval_rotate_noalloc(fides_ctx* ctx, const uint64_t* dev_in, uint32_t towers, uint32_t galois,
                               uint64_t* dev_out, void* stream);  /* dev_in, dev_out 16-byte aligned */
 

@@ -73,3 +73,37 @@ def test_server_reports_per_request_status(env):
             gpu.free(v)
         else:
             assert (kind, v) == ("err", F.FIDES_ENOMEM)
+
+
+def test_input_check_refuses_out_of_range_residues(env):
+    """With the opt-in input check on, a residue at or above its prime is refused at load time (FIDES_EINVAL) and
+    nothing is registered; in-range objects still load and evaluate to the oracle's result."""
+    F, gpu, orc = env["F"], env["gpu"], env["orc"]
+    gpu.set_input_check(True)
+    try:
+        base = gpu.mem_in_use()
+        bad = env["ct"].copy()
+        bad[1, 4, 17] = gpu.moduli[4]  # == q_4: out of range for tower 4 of c1
+        with pytest.raises(F.FidesError) as ei:
+            gpu.load_ciphertext(bad, 2.0 ** 40)
+        assert ei.value.code == F.FIDES_EINVAL
+        assert gpu.mem_in_use() == base
+        pt = np.zeros((6, N), dtype=np.uint64)
+        pt[5, 0] = np.uint64(2 ** 64 - 1)
+        with pytest.raises(F.FidesError) as ei:
+            gpu.load_plaintext(pt, 1.0)
+        assert ei.value.code == F.FIDES_EINVAL
+        g5 = orc.galois(5)
+        badkey = orc.rot_key(21, orc.secret(11), g5)
+        badkey[1, 2, 7, 9] = gpu.moduli[7]  # a special tower's prime in the b part of digit 2
+        with pytest.raises(F.FidesError) as ei:
+            gpu.load_rotation_key(g5, badkey)
+        assert ei.value.code == F.FIDES_EINVAL
+        h = gpu.load_ciphertext(env["ct"], 2.0 ** 40)
+        with pytest.raises(F.FidesError) as ei:  # the refused key was not registered
+            gpu.eval_rotate(h, 5)
+        assert ei.value.code == F.FIDES_ENOKEY
+        got = gpu.store_ciphertext(gpu.eval_rotate(h, 3))
+        assert np.array_equal(got, orc.rotate(env["ct"], env["g"], env["key"]))
+    finally:
+        gpu.set_input_check(False)

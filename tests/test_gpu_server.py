@@ -61,6 +61,6 @@ def test_served_results_equal_alone_results(engine_lib, max_batch, budget):
     srv.close()  # results stay in the context after the server stops
     for r, o, e in zip(reqs, outs, alone):
         assert np.array_equal(ctx.store_ciphertext(o), e), r
-    if max_batch == 64 and budget == 16 << 30:
-        assert st["mean_batch"] > 1
+    if budget == 16 << 30:  # a roomy budget: 48 requests submitted at once cannot all run one by one
+        assert st["mean_batch"] > 1 and st["batches"] < len(reqs), st
     ctx.close()

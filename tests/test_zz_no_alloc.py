@@ -17,9 +17,10 @@ import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def _noalloc(F, ctx, dev_in, towers, galois, dev_out):
+def _noalloc(F, ctx, dev_in, towers, galois, dev_out, stream=None):
     return F.lib().fides_eval_rotate_noalloc(ctx._h, ctypes.c_void_p(dev_in.data_ptr()), towers, galois,
-                                             ctypes.c_void_p(dev_out.data_ptr()), None)
+                                             ctypes.c_void_p(dev_out.data_ptr()),
+                                             None if stream is None else ctypes.c_void_p(stream))
 
 
 def test_noalloc_rotation_matches_allocating_entry_point(engine_lib):
@@ -44,12 +45,25 @@ def test_noalloc_rotation_matches_allocating_entry_point(engine_lib):
         dev_in = torch.from_numpy(ct.view(np.int64)).cuda()
         dev_out = torch.zeros_like(dev_in)
         torch.cuda.synchronize()
+        # The property the entry point exists for: the call allocates no device memory, neither from the
+        # context's pool (counted by fides_ctx_mem_in_use) nor through the caller's allocator.
+        pool_before, torch_before = ctx.mem_in_use(), torch.cuda.memory_allocated()
         rc = _noalloc(F, ctx, dev_in, t, g, dev_out)
         assert rc == F.FIDES_OK, F.lib().fides_last_error()
+        assert ctx.mem_in_use() == pool_before and torch.cuda.memory_allocated() == torch_before
         ctx.synchronize()
         got = dev_out.cpu().numpy().view(np.uint64)
         assert np.array_equal(got, expected), f"call {call}"
         assert np.array_equal(got, orc.rotate(ct, g, key)), f"call {call}"
+        # The same call ordered on a caller's stream instead of the context's.
+        side = torch.cuda.Stream()
+        dev_out2 = torch.zeros_like(dev_in)
+        torch.cuda.synchronize()
+        rc = _noalloc(F, ctx, dev_in, t, g, dev_out2, stream=side.cuda_stream)
+        assert rc == F.FIDES_OK, F.lib().fides_last_error()
+        side.synchronize()
+        assert ctx.mem_in_use() == pool_before
+        assert np.array_equal(dev_out2.cpu().numpy().view(np.uint64), expected), f"call {call} on a side stream"
     ctx.close()
 
 
