@@ -31,7 +31,9 @@ class FidesError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("log_n", C.c_uint32), ("nq", C.c_uint32), ("np", C.c_uint32), ("dnum", C.c_uint32),
-                ("moduli", u64p), ("roots", u64p), ("scaling_technique", C.c_int32)]
+                ("moduli", u64p), ("roots", u64p), ("scaling_technique", C.c_int32),
+                ("scaling_factor_real", C.POINTER(C.c_double)), ("scaling_factor_real_big", C.POINTER(C.c_double)),
+                ("mod_reduce_factor", C.POINTER(C.c_double)), ("default_scale", C.c_double)]
 
 
 class CtMeta(C.Structure):
@@ -48,6 +50,8 @@ _SIGS = {
     "fides_ctx_create": (C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "fides_ctx_destroy": (C.c_int, [C.c_void_p]),
     "fides_ctx_moduli": (C.c_int, [C.c_void_p, u64p, u64p]),
+    "fides_ctx_scaling": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fides_galois_element": (C.c_uint32, [C.c_void_p, C.c_int32]),
     "fides_synchronize": (C.c_int, [C.c_void_p]),
     "fides_ctx_stream": (C.c_void_p, [C.c_void_p]),
@@ -196,7 +200,10 @@ def _p(a: np.ndarray, t=u64p):
 class CryptoContext:
     """Device context: moduli, roots and all derived tables resident on the GPU (LoadContext)."""
 
-    def __init__(self, log_n: int, moduli, np_: int, dnum: int, roots=None, scaling_technique: int = FIXEDMANUAL):
+    def __init__(self, log_n: int, moduli, np_: int, dnum: int, roots=None, scaling_technique: int = FIXEDMANUAL,
+                 scaling_tables=None, default_scale: float = 0.0):
+        """scaling_tables: optional (scaling_factor_real, scaling_factor_real_big, mod_reduce_factor), nq doubles
+        each indexed by towers - 1 (RawParams' tables); None computes them for the technique."""
         moduli = np.ascontiguousarray(np.array(moduli, dtype=np.uint64))
         self.N = 1 << log_n
         self.log_n = log_n
@@ -205,7 +212,12 @@ class CryptoContext:
         self.dnum = dnum
         self.alpha = (self.nq + dnum - 1) // dnum
         r = None if roots is None else np.ascontiguousarray(np.array(roots, dtype=np.uint64))
-        prm = Params(log_n, self.nq, np_, dnum, _p(moduli), None if r is None else _p(r), scaling_technique)
+        dp = C.POINTER(C.c_double)
+        tabs = [None, None, None]
+        if scaling_tables is not None:
+            tabs = [np.ascontiguousarray(np.array(x, dtype=np.float64)) for x in scaling_tables]
+        prm = Params(log_n, self.nq, np_, dnum, _p(moduli), None if r is None else _p(r), scaling_technique,
+                     *[None if x is None else x.ctypes.data_as(dp) for x in tabs], default_scale)
         h = C.c_void_p()
         _check(lib().fides_ctx_create(C.byref(prm), C.byref(h)))
         self._h = h
@@ -225,6 +237,15 @@ class CryptoContext:
             self.close()
         except Exception:
             pass
+
+    def scaling(self):
+        """(technique, scaling_factor_real, scaling_factor_real_big, mod_reduce_factor) in use."""
+        t = C.c_int32()
+        sf, big, mrf = (np.zeros(self.nq) for _ in range(3))
+        dp = C.POINTER(C.c_double)
+        _check(lib().fides_ctx_scaling(self._h, C.byref(t), sf.ctypes.data_as(dp), big.ctypes.data_as(dp),
+                                       mrf.ctypes.data_as(dp)))
+        return t.value, sf, big, mrf
 
     # --- primitives ---
     def galois(self, index: int) -> int:

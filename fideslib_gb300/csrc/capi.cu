@@ -5,6 +5,7 @@
 #include <string>
 
 #include "../../include/fideslib_gb300.h"
+#include "autoscale.hpp"
 #include "engine.hpp"
 
 struct fides_ctx {
@@ -186,7 +187,24 @@ int fides_ctx_create(const fides_params* p, fides_ctx** out) {
   fgb::Context* c = fgb::Context::create((int)p->log_n, (int)p->nq, (int)p->np, (int)p->dnum, (const fgb::u64*)p->moduli,
                                                 (const fgb::u64*)p->roots, &err);
   if (!c) return fail(FIDES_EINVAL, err);
+  if (c->set_scaling(p->scaling_technique, p->scaling_factor_real, p->scaling_factor_real_big, p->mod_reduce_factor,
+                     p->default_scale, &err) != FIDES_OK) {
+    delete c;
+    return fail(FIDES_EINVAL, err);
+  }
   *out = new fides_ctx{c};
+  return FIDES_OK;
+}
+
+int fides_ctx_scaling(const fides_ctx* ctx, int32_t* technique, double* sf, double* big, double* mrf) {
+  if (!ctx || !ctx->c) return fail(FIDES_EINVAL, "null context");
+  const fgb::Context* c = ctx->c;
+  if (technique) *technique = c->technique;
+  for (int l = 0; l < c->nq; l++) {
+    if (sf) sf[l] = c->sf[l];
+    if (big) big[l] = c->big[l];
+    if (mrf) mrf[l] = c->mrf[l];
+  }
   return FIDES_OK;
 }
 
@@ -436,13 +454,16 @@ struct Pending {
   const fgb::u64* key = nullptr;
 };
 
-static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
+// Aligned operands (AutoScaler: the scaling technique's adjustments, or the FIXEDMANUAL tower cut) replace the
+// registered ones when given.
+static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd, const fgb::DevCt* Aov = nullptr,
+                   const fgb::DevCt* Bov = nullptr) {
   fgb::Context* c = ctx->c;
-  fgb::DevCt* A = find_ct(ctx, op.a);
+  const fgb::DevCt* A = Aov ? Aov : find_ct(ctx, op.a);
   if (!A) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(op.a));
-  fgb::DevCt* B = nullptr;
+  const fgb::DevCt* B = nullptr;
   if (op.op == FIDES_OP_ADD || op.op == FIDES_OP_SUB || op.op == FIDES_OP_MULT) {
-    B = find_ct(ctx, op.b);
+    B = Bov ? Bov : find_ct(ctx, op.b);
     if (!B) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(op.b));
     if (A->t != B->t) return fail(FIDES_EINVAL, "operands have different tower counts");
   }
@@ -491,9 +512,12 @@ static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
       if (ks && ((uint32_t)op.index & kSwitchKeyTag)) return fail(FIDES_EINVAL, "switch key id must be < 2^31");
       if (op.op == FIDES_OP_AUTOMORPHISM && (((uint32_t)op.index & 1) == 0 || (uint32_t)op.index >= 2u * c->N))
         return fail(FIDES_EINVAL, "Galois element must be odd and < 2N");
-      const uint32_t g = op.op == FIDES_OP_ROTATE ? fgb::Context::galois_for_index(c->N, op.index)
-                         : ks                     ? kSwitchKeyTag | (uint32_t)op.index
-                                                  : (uint32_t)op.index;
+      uint32_t g = op.op == FIDES_OP_ROTATE ? c->rotation_key_galois(op.index, A->slots)
+                   : ks                     ? kSwitchKeyTag | (uint32_t)op.index
+                                            : (uint32_t)op.index;
+      if (op.op == FIDES_OP_ROTATE && g == 0)
+        return fail(FIDES_ENOKEY, "no rotation key for index " + std::to_string(op.index) + " (Galois element " +
+                                      std::to_string(fgb::Context::galois_for_index(c->N, op.index)) + ")");
       auto it = c->rot_keys.find(g);
       if (it == c->rot_keys.end())
         return fail(FIDES_ENOKEY, ks ? "no switch key with id " + std::to_string(op.index)
@@ -518,8 +542,37 @@ static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd) {
 static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
   fgb::Context* c = ctx->c;
   std::vector<Pending> pd(n);
+  // Operand alignment first (its temporaries live until the batch's launches are queued, then are freed
+  // stream-ordered): binary ops whose operands differ in towers, or any operand under an automatic technique.
+  fgb::AutoScaler scaler(c, c->stream);
+  std::vector<fgb::DevCt> adj_a(n), adj_b(n);
+  std::vector<char> adjusted(n, 0);
   for (uint32_t i = 0; i < n; i++) {
-    int rc = prepare(ctx, ops[i], &pd[i]);
+    const int code = ops[i].op;
+    const bool binary = code == FIDES_OP_ADD || code == FIDES_OP_SUB || code == FIDES_OP_MULT;
+    const bool unary = code == FIDES_OP_SQUARE || code == FIDES_OP_MULT_PLAIN;
+    if (!binary && !(unary && c->technique != FIDES_FIXEDMANUAL)) continue;
+    const fgb::DevCt* A = find_ct(ctx, ops[i].a);
+    const fgb::DevCt* B = binary ? find_ct(ctx, ops[i].b) : nullptr;
+    if (!A || (binary && !B)) continue;  // prepare() reports the unknown handle
+    if (binary && c->technique == FIDES_FIXEDMANUAL && A->t == B->t) continue;
+    adj_a[i] = *A;
+    int rc = FIDES_OK;
+    if (binary) {
+      adj_b[i] = *B;
+      rc = scaler.prepare_binary(code, adj_a[i], adj_b[i]);
+    } else {
+      rc = scaler.prepare_unary(adj_a[i]);
+    }
+    if (rc) return rc;
+    adjusted[i] = 1;
+  }
+  for (uint32_t i = 0; i < n; i++) {
+    int rc = adjusted[i] ? prepare(ctx, ops[i], &pd[i], &adj_a[i], ops[i].op == FIDES_OP_SQUARE ||
+                                                                       ops[i].op == FIDES_OP_MULT_PLAIN
+                                                                   ? nullptr
+                                                                   : &adj_b[i])
+                         : prepare(ctx, ops[i], &pd[i]);
     if (rc) {
       for (uint32_t k = 0; k < i; k++) c->free_limbs(pd[k].out.data, c->stream);
       return rc;
@@ -747,9 +800,9 @@ int fides_eval_fast_rotation_precomputed(fides_ctx* ctx, uint32_t a, uint32_t pr
   if (!A || it == c->modups.end()) return fail(FIDES_EINVAL, "unknown ciphertext or precomputation handle");
   const fgb::DevModUp& M = it->second;
   if (M.t != A->t) return fail(FIDES_EINVAL, "precomputation was made at a different tower count");
-  const uint32_t g = fgb::Context::galois_for_index(c->N, index);
+  const uint32_t g = c->rotation_key_galois(index, A->slots);
   auto kt = c->rot_keys.find(g);
-  if (kt == c->rot_keys.end()) return fail(FIDES_ENOKEY, "no rotation key for Galois element " + std::to_string(g));
+  if (kt == c->rot_keys.end()) return fail(FIDES_ENOKEY, "no rotation key for index " + std::to_string(index));
   fgb::DevCt r;
   int rc = new_ct(ctx, A->t, *A, &r);
   if (rc) return rc;

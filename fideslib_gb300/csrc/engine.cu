@@ -438,9 +438,33 @@ uint32_t Context::galois_for_index(int N, int32_t index) {
   const int64_t half = N / 2;  // order of 5 modulo 2N
   int64_t r = index % half;
   if (r < 0) r += half;
-  u64 g = 1;
-  for (int64_t k = 0; k < r; k++) g = (g * 5) % M;
+  u64 g = 1, b = 5;
+  for (; r; r >>= 1, b = b * b % M)
+    if (r & 1) g = g * b % M;
   return (uint32_t)g;
+}
+
+uint32_t Context::rotation_key_galois(int32_t index, int slots) const {
+  const int64_t half = N / 2;
+  const uint32_t conj = (uint32_t)(2ull * N - 1);
+  if ((int64_t)index == (int64_t)conj) return rot_keys.count(conj) ? conj : 0;
+  const bool sparse = slots > 0 && slots < half;
+  int64_t idx = index;
+  if (sparse) {  // Ciphertext::normalyzeIndex: modulo slots, the upper half taken as negative rotations
+    idx %= slots;
+    if (idx < 0) idx += slots;
+    if (idx > slots / 2) idx += half - slots;
+  }
+  idx %= half;
+  if (idx < 0) idx += half;
+  uint32_t g = galois_for_index(N, (int32_t)idx);
+  if (rot_keys.count(g)) return g;
+  if (sparse)  // ContextData::GetRotationKey: a key of an index congruent modulo slots
+    for (int64_t i = 1; i < half / slots; i++) {
+      g = galois_for_index(N, (int32_t)((idx + i * slots) % half));
+      if (rot_keys.count(g)) return g;
+    }
+  return 0;
 }
 
 namespace {

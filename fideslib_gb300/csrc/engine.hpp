@@ -187,8 +187,26 @@ class Context {
   void free_limbs(u64* p, cudaStream_t s);
   size_t mem_limit = 0, mem_in_use = 0;
 
+  // Scaling technique (FIDES_FIXEDMANUAL .. FIDES_FLEXIBLEAUTOEXT) and its per-level tables, indexed by
+  // towers - 1 (RawParams::ScalingFactorReal / ScalingFactorRealBig / ModReduceFactor, RawCiphertext.cuh:50-86).
+  int technique = 0;
+  std::vector<double> sf, big, mrf;
+  // Sets the technique and its tables (null tables: computed as OpenFHE does for the technique); FIDES_OK or
+  // FIDES_EINVAL with *err set.
+  int set_scaling(int technique, const double* sf, const double* big, const double* mrf, double default_scale,
+                  std::string* err);
+  // Residues (towers 0..t-1) of the constant `operand` encoded at sf[t - 1] (ContextData::ElemForEvalMult).
+  void eval_mult_constants(int t, double operand, u64* out) const;
+
   uint32_t galois_inverse(uint32_t g) const;
   static uint32_t galois_for_index(int N, int32_t index);
+  // Galois element of the key a rotation by `index` of a ciphertext packing `slots` values uses, or 0 when no such
+  // key is loaded (Ciphertext::normalyzeIndex + ContextData::GetRotationKey(index, keyID, slots, actual_index),
+  // src/CKKS/Context.cu:591-619,1118-1125): with a sparse packing (0 < slots < N/2) the index is taken modulo slots
+  // (the upper half as negative rotations) and, when no key exists for it, the first loaded key of an index
+  // congruent to it modulo slots is used, as a rotation by any of them moves the packed values alike.  slots 0
+  // (unknown) or N/2: the index modulo N/2.
+  uint32_t rotation_key_galois(int32_t index, int slots) const;
 
  private:
   std::mutex mem_mu_;

@@ -49,7 +49,22 @@ typedef struct {
   uint32_t dnum;            /* key-switching digits; towers per digit alpha = ceil(nq / dnum) */
   const uint64_t* moduli;   /* nq + np primes */
   const uint64_t* roots;    /* nq + np primitive 2N-th roots (RawParams::root_of_unity); NULL = generated */
+  /* FIDES_FIXEDMANUAL: operands of an addition or multiplication at different tower counts are cut to the lower
+   * count, nothing else is adjusted.  FIDES_FIXEDAUTO / FIDES_FLEXIBLEAUTO / FIDES_FLEXIBLEAUTOEXT: before
+   * fides_eval_add / sub / mult / square (and their fides_eval_batch requests) the operands are rescaled, multiplied
+   * by scale-correcting constants and cut down to one level and scale exactly as Ciphertext::adjustForAddOrSub /
+   * adjustForMult do (src/CKKS/Ciphertext.cpp:1376-1518); a degree-2 operand of a square or of a plaintext
+   * product is rescaled first (Ciphertext::square, multPt).  Scalar ops encode at the scale the caller passes. */
   int32_t scaling_technique;
+  /* Per-level tables of RawParams (ScalingFactorReal, ScalingFactorRealBig, ModReduceFactor,
+   * RawCiphertext.cuh:50-86), nq entries each, indexed by towers - 1.  NULL = computed for the technique:
+   * FIXED*: every level default_scale (0 = 2^round(log2 q_{nq-1})); FLEXIBLEAUTO: sf[nq-1] = q_{nq-1},
+   * sf[l] = sf[l+1]^2 / q_{l+1}; FLEXIBLEAUTOEXT: sf[nq-1] = sf[nq-2] = q_{nq-2}, then the same recursion;
+   * big[l] = sf[l]^2 (FLEXIBLEAUTOEXT top level: sf[nq-1] sf[nq-2]); mod_reduce[l] = q_l. */
+  const double* scaling_factor_real;
+  const double* scaling_factor_real_big;
+  const double* mod_reduce_factor;
+  double default_scale;
 } fides_params;
 
 /* Ciphertext metadata (RawCipherText::Noise / NoiseLevel / slots, RawCiphertext.cuh:28-31). */
@@ -74,6 +89,9 @@ int fides_find_primes(uint32_t bits, uint32_t count, uint64_t two_n, const uint6
  * for its worker thread). */
 int fides_ctx_create(const fides_params* params, fides_ctx** out);
 int fides_ctx_destroy(fides_ctx* ctx);
+/* The scaling technique and its per-level tables in use (nq entries each, indexed by towers - 1; NULL skips). */
+int fides_ctx_scaling(const fides_ctx* ctx, int32_t* technique, double* scaling_factor_real,
+                      double* scaling_factor_real_big, double* mod_reduce_factor);
 /* The moduli and primitive 2N-th roots actually used (nq + np entries each). */
 int fides_ctx_moduli(const fides_ctx* ctx, uint64_t* moduli, uint64_t* roots);
 /* Galois element 5^index mod 2N (2N-1 for conjugation), FindAutomorphismIndex2nComplex semantics. */

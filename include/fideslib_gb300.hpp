@@ -40,6 +40,10 @@ struct Params {
   uint32_t dnum = 3;
   std::vector<uint64_t> roots;  // optional primitive 2N-th roots for q then p (OpenFHE root_of_unity)
   int32_t scaling_technique = FIDES_FIXEDMANUAL;
+  // RawParams' per-level tables (ScalingFactorReal, ScalingFactorRealBig, ModReduceFactor), indexed by towers - 1;
+  // empty = computed for the technique.
+  std::vector<double> scaling_factor_real, scaling_factor_real_big, mod_reduce_factor;
+  double default_scale = 0;
 };
 
 // The `count` largest primes < 2^bits with p == 1 mod 2N (for building synthetic parameter sets).
@@ -146,8 +150,11 @@ class CryptoContext {
   explicit CryptoContext(const Params& prm) {
     std::vector<uint64_t> mods(prm.q);
     mods.insert(mods.end(), prm.p.begin(), prm.p.end());
+    auto opt = [](const std::vector<double>& v) { return v.empty() ? nullptr : v.data(); };
     fides_params p{prm.log_n, (uint32_t)prm.q.size(), (uint32_t)prm.p.size(), prm.dnum, mods.data(),
-                   prm.roots.empty() ? nullptr : prm.roots.data(), prm.scaling_technique};
+                   prm.roots.empty() ? nullptr : prm.roots.data(), prm.scaling_technique,
+                   opt(prm.scaling_factor_real), opt(prm.scaling_factor_real_big), opt(prm.mod_reduce_factor),
+                   prm.default_scale};
     check(fides_ctx_create(&p, &ctx_));
     N_ = 1u << prm.log_n;
   }

@@ -37,7 +37,7 @@ def test_errors_without_gpu_are_status_codes(so):
     F.lib()
     import numpy as np
     m = np.array([1], dtype=np.uint64)
-    prm = F.Params(12, 1, 1, 1, m.ctypes.data_as(F.u64p), None, 0)
+    prm = F.Params(12, 1, 1, 1, m.ctypes.data_as(F.u64p), None, 0, None, None, None, 0.0)
     h = ctypes.c_void_p()
     rc = F.lib().fides_ctx_create(ctypes.byref(prm), ctypes.byref(h))
     assert rc in (F.FIDES_ENODEV, F.FIDES_EINVAL)

@@ -191,3 +191,29 @@ def test_rescale_matches_exact_division():
         exact = (b - top) // ql
         for j in range(2):
             assert int(rc[j][i]) == exact % mods[j]
+
+
+def test_scaling_tables_and_constants():
+    """The oracle's scaling tables keep FLEXIBLEAUTO's invariant (a product rescaled by q_l lands on the next
+    level's factor: sf[l-1] q_l = sf[l]^2), FIXED* tables are one power of two, and a constant is round(v sf)
+    reduced per tower (exact big-integer check, including the 2^k split past 2^125)."""
+    from oracle import autoscale as A
+    q = O.gen_primes(45, 6, 1 << 13)
+    sf, big, mrf = A.scaling_tables(q, A.FLEXIBLEAUTO)
+    assert sf[-1] == float(q[-1]) and mrf == [float(x) for x in q]
+    for lv in range(1, len(q)):
+        assert abs(sf[lv - 1] * q[lv] - sf[lv] ** 2) <= 1e-12 * sf[lv] ** 2
+        assert big[lv] == sf[lv] * sf[lv]
+    sfx, bigx, _ = A.scaling_tables(q, A.FLEXIBLEAUTOEXT)
+    assert sfx[-1] == sfx[-2] == float(q[-2]) and bigx[-1] == sfx[-1] * sfx[-2]
+    sff, _, _ = A.scaling_tables(q, A.FIXEDAUTO)
+    assert sff == [2.0 ** 45] * len(q)
+    for v in (1.0, -0.3, 12345.678, -2.0 ** 90):
+        k = A.eval_mult_constants(q, sf, 4, v)
+        x = v * sf[3]
+        if abs(x) < 2.0 ** 125:
+            exact = int(x + 0.5)
+            assert k == [exact % qi for qi in q[:4]]
+    big_v = 2.0 ** 100
+    k = A.eval_mult_constants(q, [2.0 ** 40] * 6, 2, big_v)  # 2^140: scaled by 2^15 and restored
+    assert k == [(2 ** 140) % qi for qi in q[:2]]
