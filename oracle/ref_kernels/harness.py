@@ -342,49 +342,66 @@ class RefKernels:
         first_prime + k, in place, through aux (same count): LimbPartition::ApplyNTT's two launches.  mode
         NTT_RESCALE: limbs are the kept towers, src[0] the top tower in coefficient form (rescale_prime its
         prime); NTT_MODDOWN: src[k] is the converted tower, limbs[k] the tower it is subtracted from."""
-        n, logN = len(limbs), self.logN
+        lp, ap = self.ptrs(limbs), self.ptrs(aux)
+        first_in = self.ptrs(src) if mode in (NTT_RESCALE, NTT_MODDOWN) else lp
+        out = self.ptrs(dst) if dst is not None else lp
+        self.ntt_launch(first_in, ap, out, len(limbs), first_prime, mode, rescale_prime, stream)
+        return (lp, ap, first_in, out)  # keep the pointer arrays alive until the launches have run
+
+    def ntt_launch(self, first_in, aux, out, n: int, first_prime: int, mode=NTT_NONE, rescale_prime=0, stream=0):
+        """The two NTT_ launches over prebuilt device pointer arrays (each of n limbs)."""
+        logN = self.logN
         if mode == NTT_RESCALE:  # LimbPartition::rescale's shapes (:597-633)
             b1, b2 = 1 << (logN // 2 - 1), 1 << ((logN + 1) // 2 - 1)
         else:
             b1, b2 = 1 << ((logN + 1) // 2 - 1), 1 << (logN // 2 - 1)
         s1, s2 = 8 * b1 * (2 * M + 2), 8 * b2 * (2 * M + 2)
-        lp, ap = self.ptrs(limbs), self.ptrs(aux)
-        first_in = self.ptrs(src) if mode in (NTT_RESCALE, NTT_MODDOWN) else lp
-        out = self.ptrs(dst) if dst is not None else lp
         self.launch(self.fn(self._ntt_name(False, mode)), (self.N // (b1 * M * 2), n), (b1, 1), s1,
-                    [("p", self.globals_ptr), ("p", first_in.data_ptr()), ("i", first_prime), ("p", ap.data_ptr()),
+                    [("p", self.globals_ptr), ("p", first_in.data_ptr()), ("i", first_prime), ("p", aux.data_ptr()),
                      ("p", 0), ("i", rescale_prime), ("p", 0), ("p", 0)], stream)
         self.launch(self.fn(self._ntt_name(True, mode)), (self.N // (b2 * M * 2), n), (b2, 1), s2,
-                    [("p", self.globals_ptr), ("p", ap.data_ptr()), ("i", first_prime), ("p", out.data_ptr()),
+                    [("p", self.globals_ptr), ("p", aux.data_ptr()), ("i", first_prime), ("p", out.data_ptr()),
                      ("p", 0), ("i", rescale_prime), ("p", 0), ("p", 0)], stream)
-        return (lp, ap, first_in, out)  # keep the pointer arrays alive until the launches have run
 
     def intt(self, limbs, first_prime: int, aux, stream=0, dst=None):
         """Inverse NTT (evaluation -> coefficient form, N^-1 included) of device limbs, LimbPartition::ApplyINTT."""
-        n, logN = len(limbs), self.logN
-        b1, b2 = 1 << (logN // 2 - 1), 1 << ((logN + 1) // 2 - 1)
-        s1, s2 = 8 * b1 * (2 * M + 2), 8 * b2 * (2 * M + 2)
         lp, ap = self.ptrs(limbs), self.ptrs(aux)
         out = self.ptrs(dst) if dst is not None else lp
+        self.intt_launch(lp, ap, out, len(limbs), first_prime, stream)
+        return (lp, ap, out)
+
+    def intt_launch(self, src, aux, out, n: int, first_prime: int, stream=0):
+        """The two INTT_ launches over prebuilt device pointer arrays (each of n limbs)."""
+        logN = self.logN
+        b1, b2 = 1 << (logN // 2 - 1), 1 << ((logN + 1) // 2 - 1)
+        s1, s2 = 8 * b1 * (2 * M + 2), 8 * b2 * (2 * M + 2)
         z = [("p", 0)] * 7
         self.launch(self.fn(self._intt_name(False)), (self.N // (b1 * M * 2), n), (b1, 1), s1,
-                    [("p", self.globals_ptr), ("p", lp.data_ptr()), ("i", first_prime), ("p", ap.data_ptr())] + z,
+                    [("p", self.globals_ptr), ("p", src.data_ptr()), ("i", first_prime), ("p", aux.data_ptr())] + z,
                     stream)
         self.launch(self.fn(self._intt_name(True)), (self.N // (b2 * M * 2), n), (b2, 1), s2,
-                    [("p", self.globals_ptr), ("p", ap.data_ptr()), ("i", first_prime), ("p", out.data_ptr())] + z,
+                    [("p", self.globals_ptr), ("p", aux.data_ptr()), ("i", first_prime), ("p", out.data_ptr())] + z,
                     stream)
-        return (lp, ap, out)
 
     def modup_conv(self, digit_in, t: int, d: int, out, stream=0):
         """DecompAndModUpConv for digit d of a ciphertext with t towers: digit_in = the digit's towers below t
         (coefficient form), out = one limb per target of the digit at t towers (the special primes, then the Q
         towers outside the digit below t), in that order."""
         assert len(digit_in) == sum(1 for i in self._digits()[0][d] if i < t)
+        assert len(out) == len(self.targets(t, d))
         ip, op = self.ptrs(digit_in), self.ptrs(out)
-        self.launch(self.fn("void FIDESlib::CKKS::DecompAndModUpConv<(FIDESlib::ALGO)3>(void**, int, void**, int, "
-                            "FIDESlib::Global::Globals const*)"), (self.N // 64, 1), (64, 2), 8 * len(digit_in) * 64,
-                    [("p", ip.data_ptr()), ("i", t), ("p", op.data_ptr()), ("i", d), ("p", self.globals_ptr)], stream)
+        self.modup_conv_launch(ip, op, len(digit_in), t, d, stream)
         return (ip, op)
+
+    def modup_conv_launch(self, ip, op, n_in: int, t: int, d: int, stream=0):
+        self.launch(self.fn("void FIDESlib::CKKS::DecompAndModUpConv<(FIDESlib::ALGO)3>(void**, int, void**, int, "
+                            "FIDESlib::Global::Globals const*)"), (self.N // 64, 1), (64, 2), 8 * n_in * 64,
+                    [("p", ip.data_ptr()), ("i", t), ("p", op.data_ptr()), ("i", d), ("p", self.globals_ptr)], stream)
+
+    def digit_base(self, d: int) -> int:
+        """first_prime of ntt / intt for the target list of digit d (the reference's DIGIT(d, 0))."""
+        return (self.lay["Constants.primeid_digit_to"] - self.lay["Constants.primeid_partition"]) // 4 + \
+            d * self.lay["MAXP"]
 
     def targets(self, t: int, d: int):
         return [j for j in self._digits()[1][d] if j < t or j >= self.L]
@@ -392,9 +409,13 @@ class RefKernels:
     def moddown_conv(self, special_in, out, stream=0):
         """ModDown2: special_in = the K special towers (coefficient form), out = len(out) Q towers 0.. (coefficient
         form) receiving the converted values."""
+        assert len(special_in) == self.K
         ip, op = self.ptrs(special_in), self.ptrs(out)
+        self.moddown_conv_launch(ip, op, len(out), stream)
+        return (ip, op)
+
+    def moddown_conv_launch(self, ip, op, n_out: int, stream=0):
         self.launch(self.fn("void FIDESlib::CKKS::ModDown2<(FIDESlib::ALGO)3>(void**, int, void**, int, "
                             "FIDESlib::Global::Globals const*)"), (self.N // 64, 1), (64, 2), 8 * self.K * 64,
-                    [("p", op.data_ptr()), ("i", len(out)), ("p", ip.data_ptr()), ("i", 0), ("p", self.globals_ptr)],
+                    [("p", op.data_ptr()), ("i", n_out), ("p", ip.data_ptr()), ("i", 0), ("p", self.globals_ptr)],
                     stream)
-        return (ip, op)
