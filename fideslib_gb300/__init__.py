@@ -140,6 +140,8 @@ _SIGS = {
     "fides_eval_double_angle_batch": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.c_uint32, u32p]),
     "fides_server_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "fides_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "fides_server_submit_to": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "fides_server_create_multi": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
     "fides_server_set_bootstrap_plan": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fides_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, u32p, C.POINTER(C.c_double)]),
     "fides_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
@@ -669,22 +671,26 @@ class ServerStats(C.Structure):
 
 
 class Server:
-    """Continuous-batching request server over one context (the C server's worker thread owns the context)."""
+    """Continuous-batching request server over one context, or over several (rings) with one admission queue and
+    one memory budget (the C server's worker thread owns the contexts)."""
 
-    def __init__(self, ctx: CryptoContext, max_batch: int = 64, max_inflight: int = 2, mem_budget: int = 16 << 30):
-        self.ctx = ctx
+    def __init__(self, ctx, max_batch: int = 64, max_inflight: int = 2, mem_budget: int = 16 << 30):
+        ctxs = list(ctx) if isinstance(ctx, (list, tuple)) else [ctx]
+        self.ctx = ctxs[0]
+        self.ctxs = ctxs
         cfg = ServerConfig(max_batch, max_inflight, mem_budget)
         h = C.c_void_p()
-        _check(lib().fides_server_create(ctx._h, C.byref(cfg), C.byref(h)))
+        arr = (C.c_void_p * len(ctxs))(*[c._h for c in ctxs])
+        _check(lib().fides_server_create_multi(arr, len(ctxs), C.byref(cfg), C.byref(h)))
         self._h = h
 
     def set_bootstrap_plan(self, plan: "BootstrapPlan"):
         _check(lib().fides_server_set_bootstrap_plan(self._h, C.byref(plan)))
 
-    def submit(self, code: int, a: int, b: int = 0, index: int = 0) -> int:
+    def submit(self, code: int, a: int, b: int = 0, index: int = 0, ring: int = 0) -> int:
         op = Op(code, a, b, index, 0)
         t = C.c_uint64()
-        _check(lib().fides_server_submit(self._h, C.byref(op), C.byref(t)))
+        _check(lib().fides_server_submit_to(self._h, ring, C.byref(op), C.byref(t)))
         return t.value
 
     def wait(self, ticket: int):

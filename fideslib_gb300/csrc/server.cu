@@ -1,12 +1,14 @@
-// Continuous-batching request server over one context (C ABI in include/fideslib_gb300.h).
+// Continuous-batching request server over one or several contexts (C ABI in include/fideslib_gb300.h).
 //
 // The reference has no serving layer (its API runs one op per call, api/CryptoContext.cpp); this is the
-// request loop the engine was shaped for.  Clients submit independent requests from any thread; one worker
-// thread owns the context.  Whenever the GPU can take more work, the worker admits every pending request that
-// fits the memory budget (output ciphertext + key-switch workspace, counted per request) up to max_batch, runs
-// them through fides_eval_batch (one launch per pipeline stage for all of them, at their own levels), and keeps
-// up to max_inflight batches queued on the stream, so requests that arrive while a batch runs are admitted into
-// the next one as soon as slots and memory free up.  Bootstrap requests (FIDES_OP_BOOTSTRAP, with the plan set
+// request loop the engine was shaped for.  Clients submit independent requests from any thread, each to one of
+// the server's rings (contexts: for example N = 2^15 and N = 2^16 side by side); one worker thread owns every
+// context.  Whenever the GPU can take more work, the worker admits, in arrival order and whatever their ring,
+// every pending request that fits the one memory budget (output ciphertext + key-switch workspace, counted per
+// request with its ring's shape) up to max_batch, runs each ring's share through fides_eval_batch on that
+// ring's stream (one launch per pipeline stage for all of them, at their own levels; the rings' batches overlap
+// on the device), and keeps up to max_inflight batches queued, so requests that arrive while a batch runs are
+// admitted into the next one as soon as slots and memory free up.  Bootstrap requests (FIDES_OP_BOOTSTRAP, with the plan set
 // by fides_server_set_bootstrap_plan) admitted together run as one fides_eval_bootstrap_batch.  Each request's
 // latency is stamped on the host from submit to the completion of its batch's CUDA event.
 #include <cuda_runtime.h>
@@ -36,6 +38,7 @@ double now_ms() {
 
 struct Req {
   fides_op op{};
+  uint32_t ring = 0;
   double t_submit = 0, t_done = 0;
   size_t footprint = 0;
   int state = 0;  // 0 pending, 1 running, 2 done
@@ -43,37 +46,43 @@ struct Req {
 };
 
 struct InFlight {
-  cudaEvent_t ev;
+  std::vector<cudaEvent_t> evs;  // one per ring that took part
   std::vector<uint64_t> tickets;
   size_t footprint;
+};
+
+struct Ring {
+  fides_ctx* ctx = nullptr;
+  uint32_t N = 0, np = 0, nq = 0, alpha = 1;
 };
 
 }  // namespace
 
 struct fides_server {
-  fides_ctx* ctx = nullptr;
+  std::vector<Ring> rings;
   fides_server_config cfg{};
   bool has_plan = false;
   fides_bootstrap_plan plan{};  // cheb_coeffs points into coeffs
   std::vector<double> coeffs;
-  uint32_t N = 0, np = 0, nq = 0, alpha = 1;
-  int device = 0;  // current at fides_server_create: the context's device
+  int device = 0;  // current at fides_server_create: the contexts' device
   std::thread worker;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<uint64_t> pending;
   std::unordered_map<uint64_t, Req> reqs;
-  std::vector<uint32_t> to_free;
+  std::vector<std::pair<uint32_t, uint32_t>> to_free;  // (ring, handle)
   std::vector<double> latencies;
   uint64_t next_ticket = 1, batches = 0, batched_ops = 0;
   double first_submit = -1, last_done = 0;
   bool stop = false;
   std::string error;
 
-  size_t footprint_of(const fides_op& op) {
+  size_t footprint_of(const Req& r) {
+    const fides_op& op = r.op;
+    const Ring& g = rings[r.ring];
     fides_ct_meta m{};
-    if (fides_ct_meta_get(ctx, op.a, &m) != FIDES_OK) return 0;
-    const size_t S = (size_t)8 * N, t = m.towers, beta = (t + alpha - 1) / alpha;
+    if (fides_ct_meta_get(g.ctx, op.a, &m) != FIDES_OK) return 0;
+    const size_t S = (size_t)8 * g.N, t = m.towers, np = g.np, beta = (t + g.alpha - 1) / g.alpha;
     size_t limbs = 2 * t;  // output
     if (op.op == FIDES_OP_ROTATE || op.op == FIDES_OP_AUTOMORPHISM || op.op == FIDES_OP_KEY_SWITCH ||
         op.op == FIDES_OP_MULT || op.op == FIDES_OP_SQUARE)
@@ -87,13 +96,12 @@ struct fides_server {
 
   // Worker loop: admit -> launch (up to max_inflight batches queued) -> retire completed batches.
   void run() {
-    cudaSetDevice(device);  // a new thread starts on device 0; the context lives on the creator's device
-    cudaStream_t stream = (cudaStream_t)fides_ctx_stream(ctx);
+    cudaSetDevice(device);  // a new thread starts on device 0; the contexts live on the creator's device
     std::deque<InFlight> inflight;
     size_t inflight_bytes = 0;
     for (;;) {
       std::vector<uint64_t> take;
-      std::vector<uint32_t> frees;
+      std::vector<std::pair<uint32_t, uint32_t>> frees;
       bool idle_wait = false;
       {
         std::unique_lock<std::mutex> lk(mu);
@@ -103,7 +111,7 @@ struct fides_server {
           size_t budget = inflight_bytes;
           while (!pending.empty() && take.size() < cfg.max_batch) {
             Req& r = reqs[pending.front()];
-            if (r.footprint == 0) r.footprint = footprint_of(r.op);  // context is only touched by this thread
+            if (r.footprint == 0) r.footprint = footprint_of(r);  // contexts are only touched by this thread
             const bool first = take.empty() && inflight.empty();
             if (!first && budget + r.footprint > cfg.mem_budget_bytes) break;
             budget += r.footprint;
@@ -116,50 +124,60 @@ struct fides_server {
         if (idle_wait) cv_work.wait(lk, [&] { return stop || !pending.empty() || !to_free.empty(); });
       }
       if (idle_wait) continue;
-      for (uint32_t h : frees) fides_ct_free(ctx, h);
+      for (auto& fr : frees) fides_ct_free(rings[fr.first].ctx, fr.second);
       if (!take.empty()) {
         std::vector<fides_op> ops(take.size());
+        std::vector<uint32_t> ring_of(take.size());
         size_t bytes = 0;
         {
           std::lock_guard<std::mutex> lk(mu);
           for (size_t i = 0; i < take.size(); i++) {
             ops[i] = reqs[take[i]].op;
+            ring_of[i] = reqs[take[i]].ring;
             bytes += reqs[take[i]].footprint;
           }
         }
-        // bootstrap requests go through fides_eval_bootstrap_batch (all of them in flight together), the rest
-        // through fides_eval_batch
-        std::vector<size_t> bi, oi;
-        for (size_t i = 0; i < ops.size(); i++) (ops[i].op == FIDES_OP_BOOTSTRAP ? bi : oi).push_back(i);
         std::vector<int> rcs(ops.size(), FIDES_OK);
-        if (!oi.empty()) {
-          std::vector<fides_op> sub(oi.size());
-          for (size_t k = 0; k < oi.size(); k++) sub[k] = ops[oi[k]];
-          const int rc = fides_eval_batch(ctx, sub.data(), (uint32_t)sub.size());
-          for (size_t k = 0; k < oi.size(); k++) {
-            if (rc != FIDES_OK && sub.size() > 1)  // one bad request must not fail its batch-mates
-              rcs[oi[k]] = fides_eval_batch(ctx, &sub[k], 1);
-            else
-              rcs[oi[k]] = rc;
-            ops[oi[k]].out = sub[k].out;
-          }
-        }
-        if (!bi.empty()) {
-          std::vector<uint32_t> in(bi.size()), outs(bi.size(), 0);
-          for (size_t k = 0; k < bi.size(); k++) in[k] = ops[bi[k]].a;
-          const int rc = has_plan ? fides_eval_bootstrap_batch(ctx, (uint32_t)in.size(), in.data(), &plan, outs.data())
-                                  : fgb::set_last_error(FIDES_EINVAL, "no bootstrap plan set on the server");
-          for (size_t k = 0; k < bi.size(); k++) {
-            if (rc != FIDES_OK && has_plan && bi.size() > 1)
-              rcs[bi[k]] = fides_eval_bootstrap(ctx, in[k], &plan, &outs[k]);
-            else
-              rcs[bi[k]] = rc;
-            ops[bi[k]].out = outs[k];
-          }
-        }
         InFlight f;
-        cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming);
-        cudaEventRecord(f.ev, stream);
+        for (uint32_t g = 0; g < rings.size(); g++) {
+          fides_ctx* ctx = rings[g].ctx;
+          // this ring's bootstrap requests go through fides_eval_bootstrap_batch (all of them in flight
+          // together; ring 0 holds the plan), the rest through fides_eval_batch
+          std::vector<size_t> bi, oi;
+          for (size_t i = 0; i < ops.size(); i++)
+            if (ring_of[i] == g) (ops[i].op == FIDES_OP_BOOTSTRAP ? bi : oi).push_back(i);
+          if (bi.empty() && oi.empty()) continue;
+          if (!oi.empty()) {
+            std::vector<fides_op> sub(oi.size());
+            for (size_t k = 0; k < oi.size(); k++) sub[k] = ops[oi[k]];
+            const int rc = fides_eval_batch(ctx, sub.data(), (uint32_t)sub.size());
+            for (size_t k = 0; k < oi.size(); k++) {
+              if (rc != FIDES_OK && sub.size() > 1)  // one bad request must not fail its batch-mates
+                rcs[oi[k]] = fides_eval_batch(ctx, &sub[k], 1);
+              else
+                rcs[oi[k]] = rc;
+              ops[oi[k]].out = sub[k].out;
+            }
+          }
+          if (!bi.empty()) {
+            std::vector<uint32_t> in(bi.size()), outs(bi.size(), 0);
+            for (size_t k = 0; k < bi.size(); k++) in[k] = ops[bi[k]].a;
+            const bool plan_ok = has_plan && g == 0;
+            const int rc = plan_ok ? fides_eval_bootstrap_batch(ctx, (uint32_t)in.size(), in.data(), &plan, outs.data())
+                                   : fgb::set_last_error(FIDES_EINVAL, "no bootstrap plan set for this ring");
+            for (size_t k = 0; k < bi.size(); k++) {
+              if (rc != FIDES_OK && plan_ok && bi.size() > 1)
+                rcs[bi[k]] = fides_eval_bootstrap(ctx, in[k], &plan, &outs[k]);
+              else
+                rcs[bi[k]] = rc;
+              ops[bi[k]].out = outs[k];
+            }
+          }
+          cudaEvent_t ev;
+          cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+          cudaEventRecord(ev, (cudaStream_t)fides_ctx_stream(ctx));
+          f.evs.push_back(ev);
+        }
         f.tickets = take;
         f.footprint = bytes;
         {
@@ -183,15 +201,19 @@ struct fides_server {
         std::lock_guard<std::mutex> lk(mu);
         full = inflight.size() >= cfg.max_inflight_batches || stop;
       }
-      if (!full && cudaEventQuery(inflight.front().ev) == cudaErrorNotReady) {
+      bool busy = false;
+      for (cudaEvent_t ev : inflight.front().evs) busy = busy || cudaEventQuery(ev) == cudaErrorNotReady;
+      if (!full && busy) {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait_for(lk, std::chrono::microseconds(20), [&] { return !pending.empty() || !to_free.empty(); });
         continue;
       }
       InFlight f = inflight.front();
       inflight.pop_front();
-      cudaEventSynchronize(f.ev);
-      cudaEventDestroy(f.ev);
+      for (cudaEvent_t ev : f.evs) {
+        cudaEventSynchronize(ev);
+        cudaEventDestroy(ev);
+      }
       const double t = now_ms();
       inflight_bytes -= f.footprint;
       std::lock_guard<std::mutex> lk(mu);
@@ -209,23 +231,35 @@ struct fides_server {
 
 extern "C" {
 
-int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_server** out) {
-  if (!ctx || !cfg || !out) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+int fides_server_create_multi(fides_ctx* const* ctxs, uint32_t n, const fides_server_config* cfg,
+                              fides_server** out) {
+  if (!ctxs || n == 0 || !cfg || !out) return fgb::set_last_error(FIDES_EINVAL, "null argument");
   if (cfg->max_batch < 1 || cfg->max_inflight_batches < 1 || cfg->mem_budget_bytes == 0)
     return fgb::set_last_error(FIDES_EINVAL, "max_batch, max_inflight_batches and mem_budget_bytes must be > 0");
   fides_server* s = new fides_server();
-  s->ctx = ctx;
+  for (uint32_t g = 0; g < n; g++) {
+    fides_ctx_shape shape{};
+    if (!ctxs[g] || fides_ctx_get_shape(ctxs[g], &shape) != FIDES_OK) {
+      delete s;
+      return fgb::set_last_error(FIDES_EINVAL, "null or invalid context");
+    }
+    for (uint32_t h = 0; h < g; h++)
+      if (ctxs[h] == ctxs[g]) {
+        delete s;
+        return fgb::set_last_error(FIDES_EINVAL, "a context may appear once");
+      }
+    s->rings.push_back(Ring{ctxs[g], shape.n, shape.np, shape.nq, shape.alpha ? shape.alpha : 1});
+  }
   s->cfg = *cfg;
-  fides_ctx_shape shape{};
-  fides_ctx_get_shape(ctx, &shape);
-  s->N = shape.n;
-  s->nq = shape.nq;
-  s->np = shape.np;
-  s->alpha = shape.alpha ? shape.alpha : 1;
   cudaGetDevice(&s->device);
   s->worker = std::thread([s] { s->run(); });
   *out = s;
   return FIDES_OK;
+}
+
+int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_server** out) {
+  if (!ctx) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+  return fides_server_create_multi(&ctx, 1, cfg, out);
 }
 
 int fides_server_set_bootstrap_plan(fides_server* s, const fides_bootstrap_plan* plan) {
@@ -239,11 +273,13 @@ int fides_server_set_bootstrap_plan(fides_server* s, const fides_bootstrap_plan*
   return FIDES_OK;
 }
 
-int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket) {
+int fides_server_submit_to(fides_server* s, uint32_t ring, const fides_op* op, uint64_t* ticket) {
   if (!s || !op || !ticket) return fgb::set_last_error(FIDES_EINVAL, "null argument");
+  if (ring >= s->rings.size()) return fgb::set_last_error(FIDES_EINVAL, "ring index out of range");
   Req r;
   r.op = *op;
   r.op.out = 0;
+  r.ring = ring;
   r.t_submit = now_ms();
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -255,6 +291,10 @@ int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket) {
   }
   s->cv_work.notify_one();
   return FIDES_OK;
+}
+
+int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket) {
+  return fides_server_submit_to(s, 0, op, ticket);
 }
 
 int fides_server_wait(fides_server* s, uint64_t ticket, uint32_t* out, double* latency_ms) {
@@ -275,7 +315,7 @@ int fides_server_release(fides_server* s, uint64_t ticket) {
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->reqs.find(ticket);
     if (it == s->reqs.end() || it->second.state != 2) return fgb::set_last_error(FIDES_EINVAL, "ticket not done");
-    if (it->second.op.out) s->to_free.push_back(it->second.op.out);
+    if (it->second.op.out) s->to_free.push_back({it->second.ring, it->second.op.out});
     s->reqs.erase(it);
   }
   s->cv_work.notify_one();

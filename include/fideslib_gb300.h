@@ -412,10 +412,19 @@ typedef struct {
   double p50_ms, p99_ms, mean_ms, max_ms, ops_per_s, mean_batch;
 } fides_server_stats;
 int fides_server_create(fides_ctx* ctx, const fides_server_config* cfg, fides_server** out);
+/* One server over n contexts (rings: e.g. N = 2^15 and N = 2^16 with their own keys), all created on the current
+ * device: one worker, one admission queue in arrival order and one memory budget across the rings; each admitted
+ * ring's requests run as one fides_eval_batch on that ring's stream, so the rings' batches overlap on the GPU.
+ * fides_server_create(ctx, ...) is the one-ring case.  Bootstrap requests go to ring 0 (the plan's ring). */
+int fides_server_create_multi(fides_ctx* const* ctxs, uint32_t n, const fides_server_config* cfg,
+                              fides_server** out);
 /* Bootstrap requests (FIDES_OP_BOOTSTRAP, operand a) use this plan (copied, with its coefficients); requests
  * admitted together run as one fides_eval_bootstrap_batch.  Set it before submitting. */
 int fides_server_set_bootstrap_plan(fides_server* s, const fides_bootstrap_plan* plan);
 int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket);
+/* Submits to ring `ring` (index into the contexts of fides_server_create_multi); the handles in `op` are that
+ * ring's.  fides_server_submit submits to ring 0. */
+int fides_server_submit_to(fides_server* s, uint32_t ring, const fides_op* op, uint64_t* ticket);
 /* Blocks until the request finished; returns its status and result handle. */
 int fides_server_wait(fides_server* s, uint64_t ticket, uint32_t* out, double* latency_ms);
 /* Frees the request's result ciphertext (done by the worker) and forgets the ticket. */
