@@ -29,6 +29,15 @@ class FidesError(RuntimeError):
         self.code = code
 
 
+class RawInfo(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("log_n", C.c_uint32), ("rows", C.c_uint32), ("polys", C.c_uint32),
+                ("noise_deg", C.c_uint32), ("slots", C.c_uint32), ("id", C.c_uint32), ("reserved", C.c_uint32),
+                ("scale", C.c_double)]
+
+
+RAW_CIPHERTEXT, RAW_PLAINTEXT, RAW_RELIN_KEY, RAW_ROTATION_KEY, RAW_SWITCH_KEY = 1, 2, 3, 4, 5
+
+
 class Params(C.Structure):
     _fields_ = [("log_n", C.c_uint32), ("nq", C.c_uint32), ("np", C.c_uint32), ("dnum", C.c_uint32),
                 ("moduli", u64p), ("roots", u64p), ("scaling_technique", C.c_int32),
@@ -114,6 +123,12 @@ _SIGS = {
     "fides_ctx_set_mem_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fides_ctx_mem_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_ctx_set_input_check": (C.c_int, [C.c_void_p, C.c_int]),
+    "fides_raw_write": (C.c_int, [C.c_char_p, C.c_void_p, u64p, u64p, u64p]),
+    "fides_raw_read_info": (C.c_int, [C.c_char_p, C.c_void_p]),
+    "fides_raw_read": (C.c_int, [C.c_char_p, C.c_void_p, u64p, u64p, u64p]),
+    "fides_ct_save": (C.c_int, [C.c_void_p, C.c_uint32, C.c_char_p]),
+    "fides_ct_load_file": (C.c_int, [C.c_void_p, C.c_char_p, u32p]),
+    "fides_key_load_file": (C.c_int, [C.c_void_p, C.c_char_p]),
     "fides_pt_encode": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32, C.c_double,
                                   C.c_uint32, u32p]),
     "fides_pt_decode": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -181,6 +196,28 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def raw_write(path: str, kind: int, data: np.ndarray, moduli, roots=None, noise_deg: int = 1, slots: int = 0,
+              ident: int = 0, scale: float = 0.0):
+    """data: u64[polys][rows][N] (host) to a raw residue file (fides_raw_write)."""
+    data = np.ascontiguousarray(data, dtype=np.uint64)
+    polys, rows, n = data.shape
+    info = RawInfo(kind, n.bit_length() - 1, rows, polys, noise_deg, slots, ident, 0, scale)
+    m = np.ascontiguousarray(np.array(moduli[:rows], dtype=np.uint64))
+    r = None if roots is None else np.ascontiguousarray(np.array(roots[:rows], dtype=np.uint64))
+    _check(lib().fides_raw_write(path.encode(), C.byref(info), _p(m), None if r is None else _p(r), _p(data)))
+
+
+def raw_read(path: str):
+    """(info, moduli, roots, data[polys][rows][N]) of a raw residue file (fides_raw_read)."""
+    info = RawInfo()
+    _check(lib().fides_raw_read_info(path.encode(), C.byref(info)))
+    m = np.zeros(info.rows, dtype=np.uint64)
+    r = np.zeros(info.rows, dtype=np.uint64)
+    d = np.zeros((info.polys, info.rows, 1 << info.log_n), dtype=np.uint64)
+    _check(lib().fides_raw_read(path.encode(), C.byref(info), _p(m), _p(r), _p(d)))
+    return info, m, r, d
 
 
 def declared_symbols() -> list[str]:
@@ -263,6 +300,17 @@ class CryptoContext:
     def set_stream(self, stream: int | None):
         _check(lib().fides_ctx_set_stream(self._h, None if not stream else C.c_void_p(stream)))
 
+
+    def save_ciphertext(self, h: int, path: str):
+        _check(lib().fides_ct_save(self._h, h, path.encode()))
+
+    def load_ciphertext_file(self, path: str) -> int:
+        h = C.c_uint32()
+        _check(lib().fides_ct_load_file(self._h, path.encode(), C.byref(h)))
+        return h.value
+
+    def load_key_file(self, path: str):
+        _check(lib().fides_key_load_file(self._h, path.encode()))
 
     def set_input_check(self, enable: bool = True):
         """Opt-in check that loaded residues are below their primes (loads refuse others with FIDES_EINVAL)."""

@@ -395,6 +395,42 @@ int fides_eval_batch_host(fides_ctx* ctx, fides_host_op* ops, uint32_t n, uint32
 int fides_eval_rotate_noalloc(fides_ctx* ctx, const uint64_t* dev_in, uint32_t towers, uint32_t galois,
                               uint64_t* dev_out, void* stream);  /* dev_in, dev_out 16-byte aligned */
 
+/* Raw residue files (no counterpart file format in the reference: it moves the same content between OpenFHE and
+ * the GPU in memory, as RawCipherText / RawPlainText / RawKeySwitchKey, src/CKKS/openfhe-interface/
+ * RawCiphertext.cuh:19-93).  This library's own little-endian format — NOT OpenFHE's cereal serialisation, whose
+ * schema is not in this tree: a 96-byte header (magic "FGBRAW01", the fields of fides_raw_info), the rows tower
+ * moduli, the rows primitive 2N-th roots the residues were transformed with (0 = not recorded), the residues
+ * u64[polys][rows][N] in evaluation form (bit-reversed, RawCipherText::sub_0 / sub_1 order), and an FNV-1a 64 hash
+ * of all preceding bytes.  A key holds polys = 2 dnum (the a vectors of every digit, then the b vectors) over all
+ * nq + np towers, the RawKeySwitchKey::r_key layout.  Readers refuse (FIDES_EINVAL) a bad magic or size, a hash
+ * mismatch, a residue at or above its modulus and, when loading into a context, other moduli, roots or ring. */
+enum { FIDES_RAW_CIPHERTEXT = 1, FIDES_RAW_PLAINTEXT = 2, FIDES_RAW_RELIN_KEY = 3, FIDES_RAW_ROTATION_KEY = 4,
+       FIDES_RAW_SWITCH_KEY = 5 };
+typedef struct {
+  uint32_t kind;       /* FIDES_RAW_* */
+  uint32_t log_n;
+  uint32_t rows;       /* towers per polynomial */
+  uint32_t polys;      /* 2 (ciphertext), 1 (plaintext), 2 dnum (key) */
+  uint32_t noise_deg;  /* RawCipherText::NoiseLevel */
+  uint32_t slots;
+  uint32_t id;         /* rotation key: Galois element; switch key: its id; else 0 */
+  uint32_t reserved;
+  double scale;        /* RawCipherText::Noise (scaling factor) */
+} fides_raw_info;
+/* Host buffers <-> file (no context, no device needed).  moduli and roots hold `rows` entries; roots may be NULL
+ * on write.  The file is written to path.tmp and renamed into place. */
+int fides_raw_write(const char* path, const fides_raw_info* info, const uint64_t* moduli, const uint64_t* roots,
+                    const uint64_t* data);
+int fides_raw_read_info(const char* path, fides_raw_info* info);
+/* Any of moduli / roots / data may be NULL (sizes from fides_raw_read_info). */
+int fides_raw_read(const char* path, fides_raw_info* info, uint64_t* moduli, uint64_t* roots, uint64_t* data);
+/* Context conveniences: a resident ciphertext to a file with its towers' moduli and roots, a file back into the
+ * context (its moduli and roots must be the context's), and a key file loaded as the relinearisation, rotation
+ * (under its Galois element) or switch key its kind names. */
+int fides_ct_save(fides_ctx* ctx, uint32_t handle, const char* path);
+int fides_ct_load_file(fides_ctx* ctx, const char* path, uint32_t* handle);
+int fides_key_load_file(fides_ctx* ctx, const char* path);
+
 /* Continuous-batching request server over one context (no counterpart in the reference, whose API runs one op
  * per call).  One worker thread owns the context: while a server runs, use the context only through it.
  * Clients on any thread submit independent requests (operands must be resident ciphertext handles); the worker

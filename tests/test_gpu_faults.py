@@ -107,3 +107,28 @@ def test_input_check_refuses_out_of_range_residues(env):
         assert np.array_equal(got, orc.rotate(env["ct"], env["g"], env["key"]))
     finally:
         gpu.set_input_check(False)
+
+
+def test_raw_files_through_a_context(env, tmp_path):
+    """A resident ciphertext saved and reloaded keeps its residues and metadata; a rotation key loaded from a raw
+    file rotates like the one loaded from memory; a file of another basis is refused."""
+    F, gpu, orc = env["F"], env["gpu"], env["orc"]
+    h = gpu.load_ciphertext(env["ct"], 2.0 ** 40, 1, 64)
+    p = str(tmp_path / "ct.fgb")
+    gpu.save_ciphertext(h, p)
+    h2 = gpu.load_ciphertext_file(p)
+    assert np.array_equal(gpu.store_ciphertext(h2), env["ct"])
+    m = gpu.meta(h2)
+    assert (m.towers, m.noise_deg, m.slots, m.scale) == (6, 1, 64, 2.0 ** 40)
+    g7 = orc.galois(7)
+    key = orc.rot_key(31, orc.secret(11), g7)
+    kp = str(tmp_path / "rot7.fgb")
+    F.raw_write(kp, F.RAW_ROTATION_KEY, key.reshape(-1, 8, N), gpu.moduli, gpu.roots, ident=g7)
+    gpu.load_key_file(kp)
+    got = gpu.store_ciphertext(gpu.eval_rotate(h2, 7))
+    assert np.array_equal(got, orc.rotate(env["ct"], g7, key))
+    other = O.make_moduli(LOGN, [59] + [45] * 5, [60] * 2)
+    F.raw_write(p, F.RAW_CIPHERTEXT, env["ct"], other)
+    with pytest.raises(F.FidesError) as ei:
+        gpu.load_ciphertext_file(p)
+    assert ei.value.code == F.FIDES_EINVAL
