@@ -50,6 +50,9 @@ def max_over_ranks(dist, value: float, device) -> float:
     return float(t.item())
 
 
+NTT_BUTTERFLIES_CFG2 = 640 * (N // 2) * LOGN  # one config-2 transform: 640 limbs of N/2 log2(N) butterflies
+
+
 def hrotate_bytes(t: int) -> int:
     """One HRotate at t towers on its own: ciphertext in and out plus its key (beta(t) digits of t + K towers)."""
     beta = (t + ALPHA - 1) // ALPHA
@@ -349,6 +352,7 @@ def run_ours(args, rank, world, dist):
 
     # config 2: batched NTT -> INTT, 16 polys x 40 primes, kernel roofline
     ntt = ntt_bench(args, dev, stream)
+    pipes = F.probe_pipes()  # the integer-pipe and butterfly ceilings the kernels are measured against
     peak, peak_kind = peaks()
     achieved = op_bytes / (ms / 1e3) / 1e9
     result = {
@@ -389,6 +393,8 @@ def run_ours(args, rank, world, dist):
         "hmult_cfg1": cfg1,
         "ntt_cfg2": ntt["summary"],
         "ntt_autotune_n16": ctx.ntt_tuning(),
+        "pipes": dict(pipes, ntt_fwd_butterflies_per_clk_sm=round(
+            NTT_BUTTERFLIES_CFG2 / (ntt["summary"]["ms_ntt"] * 1e-3) / pipes["sms"] / (pipes["clock_mhz"] * 1e6), 3)),
         "roofline": dict(ntt["roofline"], step={
             "what": "the headline step as a whole (cfg3b batch): algorithmic bytes (each distinct key once) / "
                     "ms_per_step; dominant kernel of the step: ntt16_fwd_kernel (forward NTTs of ModUp / ModDown)",
@@ -693,6 +699,48 @@ def profile_bootstrap():
     return {"profile_bootstrap": True, "launches_before_batch": l0, "launches_per_batch": F.kernel_launches() - l0}
 
 
+def profile_lt():
+    """A profiling case for the bootstrap's linear-transform kernels: the first CoeffsToSlots factor of the config-5
+    bootstrap (double-hoisted, diagonals encoded on the GPU at Q and P, 16 baby steps) applied to 8 ciphertexts at
+    25 towers (the bootstrap's 8 in flight), with random keys for that factor's rotations only (about 3 GB)."""
+    import numpy as np
+    import torch
+
+    import fideslib_gb300 as F
+    from fideslib_gb300 import bootplan as BP
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    nq, npr, dnum = 25, 5, 5
+    mods = gen_primes_host(60, 1, 2 * N)
+    mods += gen_primes_host(55, nq - 1, 2 * N, exclude=mods)
+    mods += gen_primes_host(60, npr, 2 * N, exclude=mods)
+    ctx = F.CryptoContext(LOGN, mods, npr, dnum)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0x5EED0005)
+    modt = torch.tensor(mods, dtype=torch.int64, device=dev)
+    n, delta = N // 2, 2.0 ** 55
+    M, stride, r = BP.factors(n, 3, True, scale=n / N)[0]
+    bs, gs, base, slots = BP.bsgs_layout(M, n, stride, r, bs=BP.ext_baby_steps(r))
+    present = [x is not None for x in slots]
+    diag = np.array([x if x is not None else np.zeros(n) for x in slots])
+    lt = ctx.lt_create_slots(bs, gs, diag, present, delta, nq, stride=stride, base=base, ext=True)
+    for idx in sorted(BP.rotation_indices(n, N, stride, bs, gs, base, slots)):
+        k = torch.randint(0, 1 << 62, (2, dnum, nq + npr, N), dtype=torch.int64, device=dev, generator=gen)
+        k %= modt.view(1, 1, -1, 1)
+        ctx.load_rotation_key_device(ctx.galois(idx), k.data_ptr())
+        del k
+    hs = []
+    for _ in range(8):
+        x = torch.randint(0, 1 << 62, (2, nq, N), dtype=torch.int64, device=dev, generator=gen) % modt[:nq].view(1, -1, 1)
+        hs.append(ctx.load_ciphertext_device(x.data_ptr(), nq, scale=delta))
+    torch.cuda.synchronize()
+    for _ in range(2):
+        for o in ctx.eval_linear_transform_batch(hs, lt):
+            ctx.free(o)
+    torch.cuda.synchronize()
+    return {"profile_lt": True, "bs": bs, "gs": gs, "ciphertexts": 8, "towers": nq}
+
+
 def boot_bench(args, dev):
     """Config 5: CKKS bootstrapping at N = 2^16 with 32768 full slots, level budget {3, 3} (CoeffsToSlots and
     SlotsToCoeffs each three factors of the special FFT, up to 63 diagonals per factor, encoded on the GPU at the
@@ -869,6 +917,9 @@ def main():
     ap.add_argument("--profile-bootstrap", action="store_true",
                     help="set up the config-5 bootstrap, run one batch of eight as warm-up and one more, print the "
                          "launch counts and exit (the command profiled for the bootstrap launch list)")
+    ap.add_argument("--profile-lt", action="store_true",
+                    help="run the config-5 CoeffsToSlots factor on 8 ciphertexts twice and exit (the command "
+                         "profiled for the linear-transform kernels)")
     ap.add_argument("--profile-step", action="store_true",
                     help="set up the headline workload, run --warmup batched steps and one more, print the launch "
                          "count and exit (the command profiled for the per-kernel launch list)")
@@ -876,6 +927,9 @@ def main():
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.profile_lt:
+        print(json.dumps(profile_lt()), flush=True)
+        return
     if args.profile_bootstrap:
         print(json.dumps(profile_bootstrap()), flush=True)
         return

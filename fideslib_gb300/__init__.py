@@ -38,6 +38,20 @@ class RawInfo(C.Structure):
 RAW_CIPHERTEXT, RAW_PLAINTEXT, RAW_RELIN_KEY, RAW_ROTATION_KEY, RAW_SWITCH_KEY = 1, 2, 3, 4, 5
 
 
+class ProbeResult(C.Structure):
+    _fields_ = [("sms", C.c_uint32), ("clock_mhz", C.c_double), ("imad32_per_clk_sm", C.c_double),
+                ("imad_wide_per_clk_sm", C.c_double), ("butterflies_per_clk_sm", C.c_double),
+                ("int8_mma_tops", C.c_double), ("launch_spacing_us", C.c_double)]
+
+
+def probe_pipes() -> dict:
+    """fides_probe_pipes: integer-pipe, butterfly, INT8 MMA and launch-spacing throughput of the current GPU."""
+    r = ProbeResult()
+    _check(lib().fides_probe_pipes(C.byref(r)))
+    return {k: (round(getattr(r, k), 3) if isinstance(getattr(r, k), float) else getattr(r, k))
+            for k, _ in ProbeResult._fields_}
+
+
 class Params(C.Structure):
     _fields_ = [("log_n", C.c_uint32), ("nq", C.c_uint32), ("np", C.c_uint32), ("dnum", C.c_uint32),
                 ("moduli", u64p), ("roots", u64p), ("scaling_technique", C.c_int32),
@@ -123,6 +137,7 @@ _SIGS = {
     "fides_ctx_set_mem_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fides_ctx_mem_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_ctx_set_input_check": (C.c_int, [C.c_void_p, C.c_int]),
+    "fides_probe_pipes": (C.c_int, [C.c_void_p]),
     "fides_raw_write": (C.c_int, [C.c_char_p, C.c_void_p, u64p, u64p, u64p]),
     "fides_raw_read_info": (C.c_int, [C.c_char_p, C.c_void_p]),
     "fides_raw_read": (C.c_int, [C.c_char_p, C.c_void_p, u64p, u64p, u64p]),

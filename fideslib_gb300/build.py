@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libfideslib_gb300.so"
 SOURCES = ["ntt.cu", "kernels.cu", "engine.cu", "capi.cu", "noalloc.cu", "server.cu", "poly_eval.cu", "bootstrap.cu",
-           "encode.cu", "autoscale.cu", "rawfile.cu"]
+           "encode.cu", "autoscale.cu", "rawfile.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-Wno-deprecated-gpu-targets"]

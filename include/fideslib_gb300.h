@@ -135,6 +135,19 @@ typedef struct {
 int fides_ctx_get_shape(const fides_ctx* ctx, fides_ctx_shape* shape);
 /* Number of engine kernels launched by this process so far (all contexts). */
 uint64_t fides_kernel_launches(void);
+/* Diagnostic (no counterpart in the reference): throughput of the units that bound the engine's kernels, measured
+ * on the current device with register-only kernels — 32-bit multiply-add and 32x32->64 multiply-add lanes per
+ * clock per SM, forward NTT butterflies (the engine's Shoup product and lazy reductions) per clock per SM, the
+ * legacy mma.sync INT8 tensor rate (tcgen05 has no INT8 form on sm_103a), and the spacing of back-to-back launches.
+ * Per-clock figures use the device's peak SM clock. */
+typedef struct {
+  uint32_t sms;
+  double clock_mhz;
+  double imad32_per_clk_sm, imad_wide_per_clk_sm, butterflies_per_clk_sm;
+  double int8_mma_tops;     /* tera int8 ops (2 per multiply-add) per second */
+  double launch_spacing_us; /* back-to-back empty launches (64 CTAs), GPU time per launch */
+} fides_probe_result;
+int fides_probe_pipes(fides_probe_result* r);
 
 /* Batched negacyclic NTT (inverse = 0: coefficient -> evaluation, bit-reversed) or INTT on `npolys`
  * polynomials of `limbs` towers each, tower j using prime first_prime + j.  Device memory, in place,
