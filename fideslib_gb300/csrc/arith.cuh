@@ -43,15 +43,19 @@ __device__ __forceinline__ u64 csub(u64 x, u64 m) { return x >= m ? x - m : x; }
 
 // y*w mod p in [0, 4p) for any y < 2^64: the quotient hi64(wsh*y) is estimated from the three high 32x32
 // partial products (dropping w0'*y0 and the low halves of the cross terms under-estimates it by at most 2),
-// and r = w*y + q*(2^64 - p) is formed with 64-bit multiply-accumulates (exact modulo 2^64; r < 4p).
+// and r = w*y + q*(2^64 - p) is formed exactly modulo 2^64 (r < 4p).  Every 64-bit partial sum is built from 32-bit
+// multiply-adds with a carry chain (mad.lo.cc / madc.hi) instead of 32x32->64 wide multiply-adds: on GB300 the wide
+// form issues at about a third of the 32-bit multiply-add rate, and this form ran the NTT butterfly 6.5% faster
+// (3.61 against 3.39 butterflies per clock per SM, identical results).
 __device__ __forceinline__ u64 shoup_lazy4(u64 y, u64 w, u64 wsh, u64 negp) {
   u64 r;
-  asm("{\n\t.reg .u32 y0,y1,s0,s1,w0,w1,n0,n1,t1,t2,q0,q1,r0,r1,c0,c1;\n\t.reg .u64 q,acc;\n\t"
+  asm("{\n\t.reg .u32 y0,y1,s0,s1,w0,w1,n0,n1,t1,t2,q0,q1,r0,r1,c0,c1;\n\t"
       "mov.b64 {y0,y1}, %1;\n\tmov.b64 {w0,w1}, %2;\n\tmov.b64 {s0,s1}, %3;\n\tmov.b64 {n0,n1}, %4;\n\t"
       "mul.hi.u32 t1, s1, y0;\n\tmul.hi.u32 t2, s0, y1;\n\t"
-      "add.cc.u32 c0, t1, t2;\n\taddc.u32 c1, 0, 0;\n\tmov.b64 acc, {c0,c1};\n\t"
-      "mad.wide.u32 q, s1, y1, acc;\n\tmov.b64 {q0,q1}, q;\n\t"
-      "mul.wide.u32 acc, w0, y0;\n\tmad.wide.u32 acc, q0, n0, acc;\n\tmov.b64 {r0,r1}, acc;\n\t"
+      "add.cc.u32 c0, t1, t2;\n\taddc.u32 c1, 0, 0;\n\t"
+      "mad.lo.cc.u32 q0, s1, y1, c0;\n\tmadc.hi.u32 q1, s1, y1, c1;\n\t"
+      "mul.lo.u32 r0, w0, y0;\n\tmul.hi.u32 r1, w0, y0;\n\t"
+      "mad.lo.cc.u32 r0, q0, n0, r0;\n\tmadc.hi.u32 r1, q0, n0, r1;\n\t"
       "mad.lo.u32 r1, w0, y1, r1;\n\tmad.lo.u32 r1, w1, y0, r1;\n\tmad.lo.u32 r1, q0, n1, r1;\n\t"
       "mad.lo.u32 r1, q1, n0, r1;\n\tmov.b64 %0, {r0,r1};\n\t}"
       : "=l"(r)
@@ -77,12 +81,12 @@ __device__ __forceinline__ u64 reduce128(u64 hi, u64 lo, const PrimeConst& c) {
 // three high partial products, remainder y + q * (2^64 - p)).
 __device__ __forceinline__ u64 reduce64_lazy4(u64 y, u64 one_sh, u64 negp) {
   u64 r;
-  asm("{\n\t.reg .u32 y0,y1,s0,s1,n0,n1,t1,t2,q0,q1,r0,r1,c0,c1;\n\t.reg .u64 q,acc;\n\t"
+  asm("{\n\t.reg .u32 y0,y1,s0,s1,n0,n1,t1,t2,q0,q1,r0,r1,c0,c1;\n\t"
       "mov.b64 {y0,y1}, %1;\n\tmov.b64 {s0,s1}, %2;\n\tmov.b64 {n0,n1}, %3;\n\t"
       "mul.hi.u32 t1, s1, y0;\n\tmul.hi.u32 t2, s0, y1;\n\t"
-      "add.cc.u32 c0, t1, t2;\n\taddc.u32 c1, 0, 0;\n\tmov.b64 acc, {c0,c1};\n\t"
-      "mad.wide.u32 q, s1, y1, acc;\n\tmov.b64 {q0,q1}, q;\n\t"
-      "mad.wide.u32 acc, q0, n0, %1;\n\tmov.b64 {r0,r1}, acc;\n\t"
+      "add.cc.u32 c0, t1, t2;\n\taddc.u32 c1, 0, 0;\n\t"
+      "mad.lo.cc.u32 q0, s1, y1, c0;\n\tmadc.hi.u32 q1, s1, y1, c1;\n\t"
+      "mad.lo.cc.u32 r0, q0, n0, y0;\n\tmadc.hi.u32 r1, q0, n0, y1;\n\t"
       "mad.lo.u32 r1, q0, n1, r1;\n\tmad.lo.u32 r1, q1, n0, r1;\n\tmov.b64 %0, {r0,r1};\n\t}"
       : "=l"(r)
       : "l"(y), "l"(one_sh), "l"(negp));
