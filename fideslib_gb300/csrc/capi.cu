@@ -539,7 +539,9 @@ static int prepare(fides_ctx* ctx, const fides_op& op, Pending* pd, const fgb::D
 
 // Runs a set of independent requests as one batch per op family: every ciphertext of a family goes through
 // each pipeline stage in a single launch.
-static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
+// align = false skips the operand alignment (the engine's own composites, which keep their operands at matching
+// levels and scales themselves).
+static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n, bool align = true) {
   fgb::Context* c = ctx->c;
   std::vector<Pending> pd(n);
   // Operand alignment first (its temporaries live until the batch's launches are queued, then are freed
@@ -551,7 +553,7 @@ static int run_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
     const int code = ops[i].op;
     const bool binary = code == FIDES_OP_ADD || code == FIDES_OP_SUB || code == FIDES_OP_MULT;
     const bool unary = code == FIDES_OP_SQUARE || code == FIDES_OP_MULT_PLAIN;
-    if (!binary && !(unary && c->technique != FIDES_FIXEDMANUAL)) continue;
+    if (!align || (!binary && !(unary && c->technique != FIDES_FIXEDMANUAL))) continue;
     const fgb::DevCt* A = find_ct(ctx, ops[i].a);
     const fgb::DevCt* B = binary ? find_ct(ctx, ops[i].b) : nullptr;
     if (!A || (binary && !B)) continue;  // prepare() reports the unknown handle
@@ -741,6 +743,19 @@ int fides_eval_batch(fides_ctx* ctx, fides_op* ops, uint32_t n) {
   if (!valid_ctx(ctx) || (n && !ops)) return fail(FIDES_EINVAL, "null argument");
   return run_batch(ctx, ops, n);
 }
+
+}  // extern "C"
+
+namespace fgb {
+// fides_eval_batch without the scaling technique's operand alignment: the bootstrap and polynomial-evaluation
+// composites track levels and scales exactly themselves, so their recipe is the same under every technique.
+int eval_batch_exact(fides_ctx* ctx, fides_op* ops, uint32_t n) {
+  if (!valid_ctx(ctx) || (n && !ops)) return fail(FIDES_EINVAL, "null argument");
+  return run_batch(ctx, ops, n, false);
+}
+}  // namespace fgb
+
+extern "C" {
 
 int fides_eval_add(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return one(ctx, FIDES_OP_ADD, a, b, 0, out); }
 int fides_eval_sub(fides_ctx* ctx, uint32_t a, uint32_t b, uint32_t* out) { return one(ctx, FIDES_OP_SUB, a, b, 0, out); }

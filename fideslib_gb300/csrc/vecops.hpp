@@ -53,11 +53,19 @@ inline double scale_of(fides_ctx* ctx, uint32_t h) {
   return m.scale;
 }
 
-// One batched op over a (and b, element-wise); outputs kept by the scope.
+}  // namespace fgb::vec
+namespace fgb {
+// fides_eval_batch without the scaling technique's operand alignment (capi.cu).
+int eval_batch_exact(fides_ctx* ctx, fides_op* ops, uint32_t n);
+}  // namespace fgb
+namespace fgb::vec {
+
+// One batched op over a (and b, element-wise); outputs kept by the scope.  The composites keep their operands at
+// matching levels and scales themselves, so the batch skips the scaling technique's alignment.
 inline int batch(Scope& sc, int32_t op, const V& a, const V* b, int32_t index, V& out) {
   std::vector<fides_op> ops(a.size());
   for (size_t i = 0; i < a.size(); i++) ops[i] = fides_op{op, a[i], b ? (*b)[i] : 0u, index, 0u};
-  FGB_TRY(fides_eval_batch(sc.ctx, ops.data(), (uint32_t)ops.size()));
+  FGB_TRY(eval_batch_exact(sc.ctx, ops.data(), (uint32_t)ops.size()));
   out.resize(a.size());
   for (size_t i = 0; i < a.size(); i++) out[i] = ops[i].out;
   sc.keep(out);

@@ -134,3 +134,22 @@ def test_sparse_slot_rotation_uses_a_congruent_key(base):
         ctx.eval_rotate(hf, 3)
     assert ei.value.code == F.FIDES_ENOKEY
     ctx.close()
+
+
+def test_composites_do_not_depend_on_the_technique(base):
+    """The engine's composites (here EvalMod's double-angle iterations and a Chebyshev series) keep their own exact
+    level and scale bookkeeping: under FLEXIBLEAUTO they return the residues they return under FIXEDMANUAL."""
+    import fideslib_gb300 as F
+    orc = base["orc"]
+    rng = np.random.default_rng(12)
+    z = rng.uniform(-1, 1, N // 2)
+    ct = orc.encrypt(90, base["s"], orc.encode(z, 2.0 ** 45, 8))
+    outs = []
+    for tech in (A.FIXEDMANUAL, A.FLEXIBLEAUTO):
+        ctx = _ctx(F, base, tech)
+        h = ctx.load_ciphertext(ct, 2.0 ** 45)
+        outs.append((ctx.store_ciphertext(ctx.eval_double_angle(h, 2)),
+                     ctx.store_ciphertext(ctx.eval_chebyshev(h, [0.1, -0.4, 0.25, 0.05, -0.02], -1.0, 1.0, 2.0 ** 45))))
+        ctx.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
