@@ -6,7 +6,11 @@ oracle/build_ref.sh) through the CUDA driver API and launches, with the referenc
     (src/CKKS/LimbPartition.cu:318-421), in plain, NTT_RESCALE (the rescale of LimbPartition::rescale,
     :575-652) and NTT_MODDOWN (the ModDown epilogue of LimbPartition::moddown, :1913-1985) modes;
   * DecompAndModUpConv (src/CKKS/Conv.cu:258-407), launched as LimbPartition::modup does (:766-772);
-  * ModDown2 (src/CKKS/Conv.cu:26-133), launched as LimbPartition::moddown does (:1948-1954).
+  * ModDown2 (src/CKKS/Conv.cu:26-133), launched as LimbPartition::moddown does (:1948-1954);
+  * fusedDotKSK_2_ (src/CKKS/ElemenwiseBatchKernels.cu:202-275), the key inner product, with the digit / key table
+    LimbPartition::dotKSKfused builds (src/CKKS/LimbPartitionMGPU.cu:404-446);
+  * binomialMult_ (src/CKKS/ElemenwiseBatchKernels.cu:1363-1395), the tensor product of a multiplication, launched
+    as LimbPartition::binomialMult does (src/CKKS/LimbPartition.cu:2600-2604).
 The constant block `FIDESlib::constants` and the table block `Global::Globals` are filled the way the
 reference's SetupConstants does (src/ConstantsGPU.cu:125-697), from the same primes and roots the engine uses and
 with OpenFHE's CRT tables (PartQlHatInvModq, PartQlHatModp, PHatInvModp, PHatModq, PInvModq,
@@ -419,3 +423,42 @@ class RefKernels:
                             "FIDESlib::Global::Globals const*)"), (self.N // 64, 1), (64, 2), 8 * self.K * 64,
                     [("p", op.data_ptr()), ("i", n_out), ("p", ip.data_ptr()), ("i", 0), ("p", self.globals_ptr)],
                     stream)
+
+    # --- key inner product and tensor product ------------------------------------------------------------------
+    def digit_list(self, d: int):
+        """Digit d's full target list (the special primes, then the Q towers outside the digit): DIGITlimb order."""
+        return self._digits()[1][d]
+
+    def ks_dot(self, c1, digit_limbs, key_a, key_b, t: int, out1, sout1, out2, sout2, stream=0):
+        """fusedDotKSK_2_ for a ciphertext with t towers.  c1: its t limbs (the own-digit towers are read from here);
+        digit_limbs[d]: digit d's ModUp output limbs in digit_list(d) order; key_a / key_b[d][j]: tower j of digit d
+        of the key halves (all nq + np towers).  out1 / out2 (t Q rows) and sout1 / sout2 (np special rows) receive
+        sum_d D_d a_d and sum_d D_d b_d."""
+        dec, _ = self._digits()
+        beta = (t + self.alpha - 1) // self.alpha
+        own = {j: d for d, ids in enumerate(dec) for j in ids}
+        tables = [None] * (6 * self.dnum)
+        for d in range(beta):
+            lst = self.digit_list(d)
+            tables[d] = self.ptrs(digit_limbs[d])
+            tables[self.dnum + d] = self.ptrs([key_a[d][j] for j in lst])
+            tables[2 * self.dnum + d] = self.ptrs([key_b[d][j] for j in lst])
+            tables[3 * self.dnum + d] = self.ptrs(c1)
+            tables[4 * self.dnum + d] = self.ptrs([key_a[own[j]][j] for j in range(self.L)])
+            tables[5 * self.dnum + d] = self.ptrs([key_b[own[j]][j] for j in range(self.L)])
+        dummy = tables[0]
+        tables = [x if x is not None else dummy for x in tables]
+        top = self.torch.tensor([x.data_ptr() for x in tables], dtype=self.torch.int64, device="cuda")
+        o1, s1, o2, s2 = self.ptrs(out1), self.ptrs(sout1), self.ptrs(out2), self.ptrs(sout2)
+        self.launch(self.fn("FIDESlib::CKKS::fusedDotKSK_2_(void**, void**, void**, void**, void***, int, int, int, int)"),
+                    (self.N // 128, self.K + t), (128, 1), 0,
+                    [("p", o1.data_ptr()), ("p", s1.data_ptr()), ("p", o2.data_ptr()), ("p", s2.data_ptr()),
+                     ("p", top.data_ptr()), ("i", beta), ("i", 0), ("i", self.K), ("i", 0)], stream)
+        return (tables, top, o1, s1, o2, s2)
+
+    def tensor(self, c0, c1, c2, d0, d1, stream=0):
+        """binomialMult_ over len(c0) Q towers from tower 0, in place: c0 <- c0 d0, c1 <- c0 d1 + c1 d0, c2 <- c1 d1."""
+        lists = [self.ptrs(x) for x in (c0, c1, c2, d0, d1)]
+        self.launch(self.fn("FIDESlib::CKKS::binomialMult_(int, void**, void**, void**, void**, void**)"), (self.N // 128, len(c0)),
+                    (128, 1), 0, [("i", 0)] + [("p", x.data_ptr()) for x in lists], stream)
+        return lists

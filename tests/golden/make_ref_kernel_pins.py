@@ -9,7 +9,10 @@ and dnum 3) it records, per case, a SHA-256 of the output residues and a few lea
   modup/t         INTT_ of each digit, DecompAndModUpConv, NTT_ of every converted tower (LimbPartition::modup),
                   laid out [digit][t + K][N] with the digit's own towers copied (the oracle's orc_modup layout);
   moddown/t       INTT_ of the K special rows, ModDown2, NTT_ in NTT_MODDOWN mode (LimbPartition::moddown);
-  rescale/t       INTT_ of the top tower, NTT_ in NTT_RESCALE mode (LimbPartition::rescale), on both polys.
+  rescale/t       INTT_ of the top tower, NTT_ in NTT_RESCALE mode (LimbPartition::rescale), on both polys;
+  ksinner/t       fusedDotKSK_2_ on seeded digits and a seeded key, laid out [b half, a half][t + K][N] (the oracle's
+                  orc_ks_inner order: sum_d D_d b_d, then sum_d D_d a_d);
+  tensor/t        binomialMult_ on two seeded t-tower ciphertexts: (c0 d0, c0 d1 + c1 d0, c1 d1).
 tests/test_ref_kernel_pins.py recomputes every case with the oracle on the same inputs and compares.
 """
 from __future__ import annotations
@@ -92,6 +95,7 @@ def run_reference(name: str, spec) -> dict:
     res["intt"] = digest(np.stack([host(t) for t in limbs]))
 
     alpha = (L + spec["dnum"] - 1) // spec["dnum"]
+    key = pin_key(mods, L, K, spec["dnum"])
     for t in spec["levels"]:
         # ModUp of a t-tower polynomial (evaluation form)
         a = splitmix_residues(100 + t, mods[:t])
@@ -145,8 +149,59 @@ def run_reference(name: str, spec) -> dict:
                 torch.cuda.synchronize()
                 outp.append(np.stack([host(r) for r in rows[:t - 1]]))
             res[f"rescale/{t}"] = digest(np.stack(outp))
+
+        # key inner product: digits in the oracle's layout, handed to the kernel as the reference's lists
+        c1, D = inner_inputs(t, mods, L, K, alpha)
+        dec_lists = R._digits()[0]
+        c1_dev = [dev(c1[j]) for j in range(t)]
+        key_a = [[dev(key[0, d, j]) for j in range(L + K)] for d in range(spec["dnum"])]
+        key_b = [[dev(key[1, d, j]) for j in range(L + K)] for d in range(spec["dnum"])]
+        zero = torch.zeros(N, dtype=torch.int64, device="cuda")
+        digit_limbs = []
+        for d in range(beta):
+            row = lambda j: j if j < L else t + (j - L)  # noqa: E731
+            digit_limbs.append([dev(D[d, row(j)]) if (j < t or j >= L) and j not in dec_lists[d] else zero
+                                for j in R.digit_list(d)])
+        outs = [[torch.empty(N, dtype=torch.int64, device="cuda") for _ in range(n)] for n in (t, K, t, K)]
+        keep.append(R.ks_dot(c1_dev, digit_limbs, key_a, key_b, t, *outs))
+        keep += [c1_dev, key_a, key_b, digit_limbs, outs]
+        torch.cuda.synchronize()
+        a_half = np.stack([host(x) for x in outs[0] + outs[1]])
+        b_half = np.stack([host(x) for x in outs[2] + outs[3]])
+        res[f"ksinner/{t}"] = digest(np.stack([b_half, a_half]))
+
+        # tensor product of two t-tower ciphertexts
+        x, y = tensor_inputs(t, mods)
+        c0, c1t, d0, d1 = ([dev(v[j]) for j in range(t)] for v in (x[0], x[1], y[0], y[1]))
+        c2 = [torch.empty(N, dtype=torch.int64, device="cuda") for _ in range(t)]
+        keep.append(R.tensor(c0, c1t, c2, d0, d1))
+        keep += [c0, c1t, c2, d0, d1]
+        torch.cuda.synchronize()
+        res[f"tensor/{t}"] = digest(np.stack([np.stack([host(r) for r in v]) for v in (c0, c1t, c2)]))
     torch.cuda.synchronize()
     return res
+
+
+def pin_key(mods, L, K, dnum):
+    """A seeded key of the real shape [2][dnum][L + K][N]."""
+    return splitmix_residues(500, list(mods) * (2 * dnum)).reshape(2, dnum, L + K, N)
+
+
+def inner_inputs(t, mods, L, K, alpha):
+    """c1 (t towers) and digits in the oracle's layout [beta][t + K][N] whose own-tower rows are c1's."""
+    beta = (t + alpha - 1) // alpha
+    c1 = splitmix_residues(600 + t, mods[:t])
+    D = np.stack([splitmix_residues(700 + 10 * t + d, list(mods[:t]) + list(mods[L:])) for d in range(beta)])
+    for d in range(beta):
+        for j in range(d * alpha, min((d + 1) * alpha, t)):
+            D[d, j] = c1[j]
+    return c1, D
+
+
+def tensor_inputs(t, mods):
+    x = splitmix_residues(800 + t, list(mods[:t]) * 2).reshape(2, t, N)
+    y = splitmix_residues(900 + t, list(mods[:t]) * 2).reshape(2, t, N)
+    return x, y
 
 
 def main():

@@ -1,10 +1,11 @@
 """The oracle against the reference's own GPU kernels (CPU test; fixtures from a GB300 run).
 
 tests/golden/ref_kernel_pins.json holds digests of what the reference's kernels — NTT_ / INTT_, DecompAndModUpConv,
-ModDown2 with the NTT_MODDOWN epilogue, the NTT_RESCALE rescale, compiled from its src/NTT.cu and src/CKKS/Conv.cu
-and launched as its LimbPartition launches them — return on seeded inputs (tests/golden/make_ref_kernel_pins.py).
-Here the oracle recomputes every case on the same inputs: orc_ntt_fwd / orc_ntt_inv, orc_modup, orc_moddown and
-orc_rescale must give the same residues, bit for bit.  The reference checks its Mult, Square and Rescale bit-exact
+ModDown2 with the NTT_MODDOWN epilogue, the NTT_RESCALE rescale, the key inner product fusedDotKSK_2_ and the tensor
+product binomialMult_, compiled from its src/NTT.cu, src/CKKS/Conv.cu and src/CKKS/ElemenwiseBatchKernels.cu and
+launched as its LimbPartition launches them — return on seeded inputs (tests/golden/make_ref_kernel_pins.py).
+Here the oracle recomputes every case on the same inputs: orc_ntt_fwd / orc_ntt_inv, orc_modup, orc_moddown,
+orc_rescale, orc_ks_inner and orc_tensor must give the same residues, bit for bit.  The reference checks its Mult, Square and Rescale bit-exact
 against OpenFHE (test/OpenFheInterfaceTests.cu), so these ops of the oracle — and through the GPU parity tests the
 engine's — are pinned to the reference's arithmetic, not only to this repository's restatement of it.
 """
@@ -15,7 +16,8 @@ import numpy as np
 import pytest
 
 import oracle as O
-from tests.golden.make_ref_kernel_pins import LOGN, N, PARAM_SETS, digest, splitmix_residues
+from tests.golden.make_ref_kernel_pins import (LOGN, N, PARAM_SETS, digest, inner_inputs, pin_key, splitmix_residues,
+                                               tensor_inputs)
 
 PINS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_kernel_pins.json")
 
@@ -52,3 +54,9 @@ def test_oracle_matches_reference_kernels(pins, name):
         if t >= 2:
             ct = splitmix_residues(400 + t, mods[:t] * 2).reshape(2, t, N)
             assert digest(orc.rescale(ct)) == got[f"rescale/{t}"], f"rescale at {t} towers"
+        if f"ksinner/{t}" in got:
+            key = pin_key(mods, L, K, spec["dnum"])
+            _, D = inner_inputs(t, mods, L, K, orc.alpha)
+            assert digest(orc.ks_inner(D, t, key)) == got[f"ksinner/{t}"], f"key inner product at {t} towers"
+            x, y = tensor_inputs(t, mods)
+            assert digest(orc.tensor(x, y)) == got[f"tensor/{t}"], f"tensor product at {t} towers"
