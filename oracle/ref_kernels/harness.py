@@ -8,7 +8,7 @@ oracle/build_ref.sh) through the CUDA driver API and launches, with the referenc
   * DecompAndModUpConv (src/CKKS/Conv.cu:258-407), launched as LimbPartition::modup does (:766-772);
   * ModDown2 (src/CKKS/Conv.cu:26-133), launched as LimbPartition::moddown does (:1948-1954);
   * fusedDotKSK_2_ (src/CKKS/ElemenwiseBatchKernels.cu:202-275), the key inner product, with the digit / key table
-    LimbPartition::dotKSKfused builds (src/CKKS/LimbPartitionMGPU.cu:404-446);
+    LimbPartition::dotKSKfusedMGPU builds (src/CKKS/LimbPartitionMGPU.cu:404-446);
   * binomialMult_ (src/CKKS/ElemenwiseBatchKernels.cu:1363-1395), the tensor product of a multiplication, launched
     as LimbPartition::binomialMult does (src/CKKS/LimbPartition.cu:2600-2604).
 The constant block `FIDESlib::constants` and the table block `Global::Globals` are filled the way the
