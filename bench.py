@@ -295,15 +295,19 @@ def run_ours(args, rank, world, dist):
     def e2e_step():  # pipelined: chunk k+1 copies in while chunk k computes and chunk k-1 copies out
         ctx.eval_batch_host(host_ops, chunk=E2E_CHUNK)
 
-    for _ in range(2):
+    for _ in range(3):
         e2e_step()
     torch.cuda.synchronize()
+    e2e_steps = max(1, args.steps)
+    e2e_each = []  # each call returns with its results in host memory (it synchronises its streams)
     t0 = time.perf_counter()
-    e2e_steps = max(1, args.steps // 2)
     for _ in range(e2e_steps):
+        t1 = time.perf_counter()
         e2e_step()
+        e2e_each.append((time.perf_counter() - t1) * 1e3)
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / e2e_steps, dev)
+    e2e_each.sort()
 
     # HMult + relinearisation + Rescale on the same 64 ragged-level ciphertexts (each squared against a second
     # ciphertext of its level), batched and per op
@@ -374,7 +378,10 @@ def run_ours(args, rank, world, dist):
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (keys 3.8 GiB, cts ~1 GiB)"},
         "e2e": {"value": round(64 * world / (e2e_ms / 1e3), 2), "unit": "HRotate ops/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                "path": "fides_eval_batch_host, pinned host buffers, chunks of 4, 8, ..., 8, 4 on two compute streams"},
+                "path": "fides_eval_batch_host, pinned host buffers, chunks of 4, 8, ..., 8, 4 on two compute streams",
+                "steps": e2e_steps, "ms_per_step": round(e2e_ms, 4),
+                "ms_per_step_min_median_max": [round(e2e_each[0], 3), round(e2e_each[len(e2e_each) // 2], 3),
+                                               round(e2e_each[-1], 3)]},
         "gpu_launches": int(launches),
         "per_op": {"value": round(64 * world / (per_op_ms / 1e3), 2), "unit": "HRotate ops/s",
                    "ms_per_step": round(per_op_ms, 4), "batched_over_per_op": round(per_op_ms / ms, 3)},

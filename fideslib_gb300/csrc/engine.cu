@@ -758,45 +758,35 @@ cudaError_t Context::mult_batch(const MultReq* reqs, int n, const u64* rlk, cuda
 cudaError_t Context::rescale_batch(const RescaleReq* reqs, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const size_t NN = (size_t)N;
-  size_t total = 0;
-  std::vector<size_t> off(n);
-  for (int i = 0; i < n; i++) {
+  for (int i = 0; i < n; i++)
     if (reqs[i].t < 2) return cudaErrorInvalidValue;
-    off[i] = total;
-    total += 2 + (size_t)2 * (reqs[i].t - 1);
-  }
-  u64* ws = alloc_limbs(total, s);
+  u64* ws = alloc_limbs((size_t)2 * n, s);  // the top tower of both polys, coefficient form
   if (!ws) return cudaErrorMemoryAllocation;
   cudaError_t err = cudaSuccess;
   uint8_t pm[64];
-  for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxJobs) {
-    RescaleBatch rb{};
-    for (int i = i0; i < n && rb.njobs < kMaxJobs; i++) {
-      u64* top = ws + off[i] * NN;
-      rb.jobs[rb.njobs++] = RescaleJob{reqs[i].x, top, top + 2 * NN, reqs[i].out, reqs[i].t};
-    }
+  for (int i0 = 0; i0 < n && err == cudaSuccess; i0 += kMaxNttJobs) {
+    const int i1 = std::min(n, i0 + kMaxNttJobs);
     {  // top towers of both polys to coefficient form (out of place)
       NttQueue q(tabs, true, s);
-      for (int b = 0; b < rb.njobs; b++) {
-        const RescaleJob& j = rb.jobs[b];
-        pm[0] = (uint8_t)(j.t - 1);
-        q.add(j.x + (size_t)(j.t - 1) * NN, const_cast<u64*>(j.top), (long long)j.t * N, N, 1, 2, pm);
+      for (int i = i0; i < i1; i++) {
+        pm[0] = (uint8_t)(reqs[i].t - 1);
+        q.add(reqs[i].x + (size_t)(reqs[i].t - 1) * NN, ws + (size_t)2 * i * NN, (long long)reqs[i].t * N, N, 1, 2,
+              pm);
       }
       q.flush();
       err = q.err;
     }
-    if (err == cudaSuccess) err = launch_rescale_switch(rb, ring_, nq, d_pc, s);
-    if (err == cudaSuccess) {
-      NttQueue q(tabs, false, s);
-      for (int b = 0; b < rb.njobs; b++) {
-        const RescaleJob& j = rb.jobs[b];
-        for (int k = 0; k < j.t - 1; k++) pm[k] = (uint8_t)k;
-        q.add(j.tmp, j.tmp, (long long)(j.t - 1) * N, (long long)(j.t - 1) * N, j.t - 1, 2, pm);
-      }
-      q.flush();
-      err = q.err;
+    if (err != cudaSuccess) break;
+    // the switch of the top tower into every q_i, the NTT and (x_i - .) q_l^-1 in one launch
+    NttBatch nb{};
+    NttEpi ep;
+    for (int i = i0; i < i1; i++) {
+      const int t = reqs[i].t;
+      for (int k = 0; k < t - 1; k++) pm[k] = (uint8_t)k;
+      ntt_add_job(nb, ws + (size_t)2 * i * NN, nullptr, N, 0, t - 1, 2, pm);
+      ep.jobs[i - i0] = NttEpiJob{reqs[i].x, reqs[i].out, crt.rs_qinv + (size_t)(t - 1) * nq, t, t - 1, t - 1};
     }
-    if (err == cudaSuccess) err = launch_rescale_epilogue(rb, ring_, crt, d_pc, s);
+    err = launch_ntt_epi(nb, ep, tabs, s);
   }
   free_limbs(ws, s);
   return err;

@@ -426,37 +426,6 @@ __global__ void __launch_bounds__(kT) addsub_kernel(const __grid_constant__ AddB
 }
 
 // OpenFHE NativeVector::SwitchModulus: values above om/2 are lifted to v - om before reduction mod nm.
-__global__ void __launch_bounds__(kT) rescale_switch_kernel(const __grid_constant__ RescaleBatch b, Ring r,
-                                                            const PrimeConst* __restrict__ pc) {
-  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
-  const RescaleJob& J = b.jobs[z];
-  const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
-  const int poly = row >= t - 1 ? 1 : 0, i = row - poly * (t - 1);
-  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
-  const PrimeConst& om = pc[t - 1];
-  const PrimeConst& nm = pc[i];
-  const u64 om_mod_nm = shoup(om.p, 1ull, nm.one_sh, nm.p);
-  const u64 diff = nm.p - om_mod_nm, half = om.p >> 1;
-  const ulonglong2 v = ld2(J.top + (size_t)poly * r.N + n);
-  auto sw = [&](u64 x) { return shoup(x > half ? x + diff : x, 1ull, nm.one_sh, nm.p); };
-  st2(J.tmp + ((size_t)poly * (t - 1) + i) * r.N + n, make_ulonglong2(sw(v.x), sw(v.y)));
-}
-
-__global__ void __launch_bounds__(kT) rescale_epilogue_kernel(const __grid_constant__ RescaleBatch b, Ring r,
-                                                              CrtTables c, const PrimeConst* __restrict__ pc) {
-  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
-  const RescaleJob& J = b.jobs[z];
-  const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
-  const int poly = row >= t - 1 ? 1 : 0, i = row - poly * (t - 1);
-  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
-  const u64 q = pc[i].p;
-  const ulonglong2 w = c.rs_qinv[(size_t)(t - 1) * c.nq + i];
-  const ulonglong2 a = ld2(J.x + ((size_t)poly * t + i) * r.N + n);
-  const ulonglong2 bb = ld2(J.tmp + ((size_t)poly * (t - 1) + i) * r.N + n);
-  st2(J.out + ((size_t)poly * (t - 1) + i) * r.N + n,
-      make_ulonglong2(shoup(sub_mod(a.x, bb.x, q), w.x, w.y, q), shoup(sub_mod(a.y, bb.y, q), w.x, w.y, q)));
-}
-
 __global__ void __launch_bounds__(kT) ptop_kernel(const __grid_constant__ PtBatch b, Ring r,
                                                   const PrimeConst* __restrict__ pc) {
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
@@ -823,30 +792,6 @@ cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeC
   const int rows = with_rows(b, bb, [](const AddJob& j) { return j.t; });
   dim3 grid(r.N / (2 * kT), rows, 1);
   addsub_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
-  count_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, const PrimeConst* pc,
-                                  cudaStream_t s) {
-  if (b.njobs <= 0) return cudaSuccess;
-  RescaleBatch bb;
-  const int rows = with_rows(b, bb, [](const RescaleJob& j) { return 2 * (j.t - 1); });
-  if (rows <= 0) return cudaSuccess;
-  dim3 grid(r.N / (2 * kT), rows, 1);
-  rescale_switch_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
-  count_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t launch_rescale_epilogue(const RescaleBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
-                                    cudaStream_t s) {
-  if (b.njobs <= 0) return cudaSuccess;
-  RescaleBatch bb;
-  const int rows = with_rows(b, bb, [](const RescaleJob& j) { return 2 * (j.t - 1); });
-  if (rows <= 0) return cudaSuccess;
-  dim3 grid(r.N / (2 * kT), rows, 1);
-  rescale_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }

@@ -103,20 +103,6 @@ struct AddBatch {
   AddJob jobs[kMaxJobs];
 };
 
-// Rescale of x [2][t][N]: top [2][N] holds INTT of the top towers, tmp [2][t-1][N] the switched copies.
-struct RescaleJob {
-  const u64* x;
-  const u64* top;
-  u64* tmp;
-  u64* out;
-  int t;
-};
-struct RescaleBatch {
-  int njobs;
-  int row_begin[kMaxJobs + 1];  // filled by each launcher: prefix sums of that kernel's rows per job
-  RescaleJob jobs[kMaxJobs];
-};
-
 // Plaintext op on [2][t][N]: mode 0 = multiply both polys by pt, 1 = c0 + pt, 2 = c0 - pt (c1 copied).
 struct PtJob {
   const u64* ct;
@@ -250,9 +236,5 @@ cudaError_t launch_range_check(const u64* x, long long rows, int logN, int perio
 cudaError_t launch_key_split(u64* key, size_t n, cudaStream_t s);
 cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeConst* pc, cudaStream_t s);
-cudaError_t launch_rescale_switch(const RescaleBatch& b, const Ring& r, int nq, const PrimeConst* pc,
-                                  cudaStream_t s);
-cudaError_t launch_rescale_epilogue(const RescaleBatch& b, const Ring& r, const CrtTables& c, const PrimeConst* pc,
-                                    cudaStream_t s);
 
 }  // namespace fgb

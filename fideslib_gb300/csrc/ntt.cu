@@ -110,6 +110,7 @@ struct LimbRef {
   u64* dst;
   int prime;
   bool valid;
+  int job, poly, row;
 };
 
 // Flattened limb blockIdx.y -> (job, limb of job); uniform over a cluster.
@@ -117,13 +118,15 @@ __device__ __forceinline__ LimbRef locate(const NttBatch& b, int N) {
   const int z = find_job(b.limb_begin, b.njobs, (int)blockIdx.y);
   const NttJob& J = b.jobs[z];
   const int q = (int)blockIdx.y - b.limb_begin[z];
-  LimbRef r{nullptr, nullptr, 0, false};
+  LimbRef r{nullptr, nullptr, 0, false, z, 0, 0};
   if (q < J.limbs * J.npolys) {
     const int poly = q / J.limbs, j = q - poly * J.limbs;
     r.src = J.src + poly * J.src_stride + (long long)j * N;
     r.dst = J.dst + poly * J.dst_stride + (long long)j * N;
     r.prime = J.prime_of[j];
     r.valid = true;
+    r.poly = poly;
+    r.row = j;
   }
   return r;
 }
@@ -138,9 +141,54 @@ struct Shape {
   static constexpr int LOGRA = LOGE - 8;  // pass A radix
 };
 
+// Input side of the fused rescale: the job's one row per poly (coefficients of prime switch_top) switched into
+// this limb's prime on load.
+struct SwitchIn {
+  u64 diff = 0, half = 0, one_sh = 0, p = 0;
+  __device__ __forceinline__ u64 operator()(u64 x) const { return shoup(x > half ? x + diff : x, 1ull, one_sh, p); }
+};
+
+__device__ __forceinline__ SwitchIn switch_in(const NttBatch& b, const DeviceTables& T, const NttEpi* e,
+                                              const LimbRef& L, const u64*& src) {
+  SwitchIn sw;
+  const u64 om = T.pc[e->jobs[L.job].switch_top].p;
+  src = b.jobs[L.job].src + L.poly * b.jobs[L.job].src_stride;
+  sw.p = T.pc[L.prime].p;
+  sw.one_sh = T.pc[L.prime].one_sh;
+  sw.diff = sw.p - shoup(om, 1ull, sw.one_sh, sw.p);
+  sw.half = om >> 1;
+  return sw;
+}
+
+// Starts pulling the rescale's x operands for residues n0 .. n0 + 15 (one 128-byte line) into L1 before the last
+// pass's butterflies, so their loads after it do not wait on HBM.
 template <int LOGN>
-__global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_constant__ NttBatch b,
-                                                           const __grid_constant__ DeviceTables T) {
+__device__ __forceinline__ void epi_prefetch(const NttEpi* e, const LimbRef& L, int n0) {
+  const NttEpiJob& E = e->jobs[L.job];
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(E.x + ((size_t)L.poly * E.x_ps + L.row) * (1 << LOGN) + n0));
+}
+
+// Output side of the fused rescale for a thread's 16 contiguous residues x (in [0, 16p)) at n0 .. n0 + 15.
+template <int LOGN>
+__device__ __forceinline__ void epi_store16(const NttEpi* e, const LimbRef& L, int n0, const u64 (&x)[16], u64 p) {
+  constexpr int N = 1 << LOGN;
+  const u64 p2 = 2 * p, p4 = 4 * p;
+  const NttEpiJob& E = e->jobs[L.job];
+  const ulonglong2 w = E.w[L.row];
+  const u64* xr = E.x + ((size_t)L.poly * E.x_ps + L.row) * N + n0;
+  ulonglong2* orow = reinterpret_cast<ulonglong2*>(E.out + ((size_t)L.poly * E.out_ps + L.row) * N + n0);
+#pragma unroll
+  for (int k = 0; k < 16; k += 2) {
+    const ulonglong2 xv = *reinterpret_cast<const ulonglong2*>(xr + k);
+    const u64 y0 = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
+    const u64 y1 = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
+    orow[k / 2] = make_ulonglong2(shoup(sub_mod(xv.x, y0, p), w.x, w.y, p), shoup(sub_mod(xv.y, y1, p), w.x, w.y, p));
+  }
+}
+
+// EPI: the fused rescale of NttEpi (null for the plain transform).
+template <int LOGN, bool EPI>
+__device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTables& T, const NttEpi* e) {
   using S = Shape<LOGN>;
   extern __shared__ __align__(16) u64 sm[];
   const int tid = threadIdx.x;
@@ -149,6 +197,9 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_const
   const u64 p = T.pc[L.prime].p, p2 = 2 * p, p4 = 4 * p, negp = T.pc[L.prime].negp;
   const ulonglong2* __restrict__ tw = T.tw_fwd + (size_t)L.prime * S::N;
   int h = 0;
+  const u64* src = L.src;
+  SwitchIn sw;
+  if constexpr (EPI) sw = switch_in(b, T, e, L, src);
 
   if constexpr (S::C > 1) {
     cg::cluster_group cl = cg::this_cluster();
@@ -164,7 +215,11 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_const
     for (int it = 0; it < IT; it++) {
       const int l = c * LPC + it * kThreads + tid;
 #pragma unroll
-      for (int hh = 0; hh < S::C; hh++) x[it][hh] = __ldg(L.src + hh * S::E + l);
+      for (int hh = 0; hh < S::C; hh++) x[it][hh] = __ldg(src + hh * S::E + l);
+      if constexpr (EPI) {
+#pragma unroll
+        for (int hh = 0; hh < S::C; hh++) x[it][hh] = sw(x[it][hh]);
+      }
     }
 #pragma unroll
     for (int it = 0; it < IT; it++) fwd_radix<S::LOGC, S::LOGE, LOGN>(x[it], 0, tw, negp, p4);
@@ -191,7 +246,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_const
       if constexpr (S::C > 1)
         x[k] = sm[swz(l)];
       else
-        x[k] = (l < S::E) ? __ldg(L.src + l) : 0ull;
+        x[k] = (l < S::E) ? (EPI ? sw(__ldg(src + l)) : __ldg(src + l)) : 0ull;
     }
     fwd_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4);
 #pragma unroll
@@ -216,16 +271,34 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_const
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
+    if constexpr (EPI) epi_prefetch<LOGN>(e, L, h * S::E + g * 16);
     fwd_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p4);
-    ulonglong2* out = reinterpret_cast<ulonglong2*>(L.dst + h * S::E + g * 16);
+    if constexpr (EPI) {
+      epi_store16<LOGN>(e, L, h * S::E + g * 16, x, p);
+    } else {
+      ulonglong2* out = reinterpret_cast<ulonglong2*>(L.dst + h * S::E + g * 16);
 #pragma unroll
-    for (int k = 0; k < 16; k += 2) {
-      ulonglong2 v;
-      v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
-      v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
-      out[k / 2] = v;
+      for (int k = 0; k < 16; k += 2) {
+        ulonglong2 v;
+        v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
+        v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
+        out[k / 2] = v;
+      }
     }
   }
+}
+
+template <int LOGN>
+__global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_constant__ NttBatch b,
+                                                           const __grid_constant__ DeviceTables T) {
+  ntt_fwd_body<LOGN, false>(b, T, nullptr);
+}
+
+template <int LOGN>
+__global__ void __launch_bounds__(kThreads, 2) ntt_fwd_epi_kernel(const __grid_constant__ NttBatch b,
+                                                               const __grid_constant__ DeviceTables T,
+                                                               const __grid_constant__ NttEpi e) {
+  ntt_fwd_body<LOGN, true>(b, T, &e);
 }
 
 template <int LOGN>
@@ -344,9 +417,9 @@ struct Shape16 {
   static constexpr int GROUPS = E / 16;                    // 16-residue groups per pass
 };
 
-template <int LOGN, int LOGE>
-__global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_constant__ NttBatch b,
-                                                                 const __grid_constant__ DeviceTables T) {
+// EPI: the fused rescale of NttEpi (null for the plain transform).
+template <int LOGN, int LOGE, bool EPI>
+__device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTables& T, const NttEpi* e) {
   using S = Shape16<LOGN, LOGE>;
   extern __shared__ __align__(16) u64 sm[];
   const int tid = threadIdx.x;
@@ -359,6 +432,9 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
     asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
     h = (int)cg::this_cluster().block_rank();
   }
+  const u64* src = L.src;
+  SwitchIn sw;
+  if constexpr (EPI) sw = switch_in(b, T, e, L, src);
   {  // phase X: residue k*4096 + col lives in CTA k >> LOCAL at (k & local mask) * 4096 + col
     constexpr int R = 1 << S::LOGX;
 #pragma unroll 1
@@ -366,7 +442,11 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
       const int col = h * S::COLS + q * kThreads16 + tid;
       u64 x[R];
 #pragma unroll
-      for (int k = 0; k < R; k++) x[k] = __ldg(L.src + k * 4096 + col);
+      for (int k = 0; k < R; k++) x[k] = __ldg(src + k * 4096 + col);
+      if constexpr (EPI) {
+#pragma unroll
+        for (int k = 0; k < R; k++) x[k] = sw(x[k]);
+      }
       fwd_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4);
       if constexpr (S::C > 1) {
         if (q == 0) asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
@@ -413,16 +493,35 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_c
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
+    if constexpr (EPI) epi_prefetch<LOGN>(e, L, h * S::E + g * 16);
     fwd_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p4);
-    ulonglong2* out = reinterpret_cast<ulonglong2*>(L.dst + h * S::E + g * 16);
+    if constexpr (EPI) {
+      epi_store16<LOGN>(e, L, h * S::E + g * 16, x, p);
+    } else {
+      ulonglong2* out = reinterpret_cast<ulonglong2*>(L.dst + h * S::E + g * 16);
 #pragma unroll
-    for (int k = 0; k < 16; k += 2) {
-      ulonglong2 v;
-      v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
-      v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
-      out[k / 2] = v;
+      for (int k = 0; k < 16; k += 2) {
+        ulonglong2 v;
+        v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
+        v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
+        out[k / 2] = v;
+      }
     }
   }
+}
+
+template <int LOGN, int LOGE>
+__global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_constant__ NttBatch b,
+                                                                 const __grid_constant__ DeviceTables T) {
+  ntt16_fwd_body<LOGN, LOGE, false>(b, T, nullptr);
+}
+
+// The forward transform with the fused rescale (NttEpi).
+template <int LOGN, int LOGE>
+__global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_epi_kernel(const __grid_constant__ NttBatch b,
+                                                                     const __grid_constant__ DeviceTables T,
+                                                                     const __grid_constant__ NttEpi e) {
+  ntt16_fwd_body<LOGN, LOGE, true>(b, T, &e);
 }
 
 // Inverse of the same shape (Gentleman–Sande, passes C^-1, B^-1, A^-1, then the cross-CTA phase X^-1 reading
@@ -535,6 +634,64 @@ cudaError_t launch16(const NttBatch& b, const DeviceTables& t, bool inverse, cud
   return cudaSuccess;
 }
 
+template <int LOGN, int LOGE>
+cudaError_t launch16_epi(const NttBatch& b, const NttEpi& e, const DeviceTables& t, cudaStream_t s) {
+  using S = Shape16<LOGN, LOGE>;
+  auto kern = ntt16_fwd_epi_kernel<LOGN, LOGE>;
+  static std::atomic<unsigned long long> attr_done;
+  const size_t smem = sizeof(u64) * S::E;
+  const cudaError_t ea = once_per_device(attr_done, [&] {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && S::C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+  });
+  if (ea != cudaSuccess) return ea;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(S::C, b.limb_begin[b.njobs], 1);
+  cfg.blockDim = dim3(kThreads16, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = S::C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaError_t err = cudaLaunchKernelEx(&cfg, kern, b, t, e);
+  if (err != cudaSuccess) return err;
+  count_launch();
+  return cudaSuccess;
+}
+
+template <int LOGN>
+cudaError_t launch_t_epi(const NttBatch& b, const NttEpi& e, const DeviceTables& t, cudaStream_t s) {
+  using S = Shape<LOGN>;
+  auto kern = ntt_fwd_epi_kernel<LOGN>;
+  static std::atomic<unsigned long long> attr_done;
+  const size_t smem = sizeof(u64) * S::E;
+  const cudaError_t ea = once_per_device(attr_done, [&] {
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  if (ea != cudaSuccess) return ea;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(S::C, b.limb_begin[b.njobs], 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = S::C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaError_t err = cudaLaunchKernelEx(&cfg, kern, b, t, e);
+  if (err != cudaSuccess) return err;
+  count_launch();
+  return cudaSuccess;
+}
+
 template <int LOGN>
 cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape<LOGN>;
@@ -600,6 +757,29 @@ cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, c
       return v == 1 ? launch_t<16>(b, t, false, s) : v == 0 ? launch16<16, 13>(b, t, false, s)
                                                            : launch16<16, 12>(b, t, false, s);
     default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_ntt_epi(const NttBatch& b, const NttEpi& e, const DeviceTables& t, cudaStream_t s) {
+  if (b.njobs <= 0 || b.limb_begin[b.njobs] <= 0) return cudaSuccess;
+  if (b.njobs > kMaxNttJobs || b.limb_begin[b.njobs] > 65535) return cudaErrorInvalidValue;
+  // the forward variant the autotuner picked for this batch size (as launch_ntt)
+  const long long work = (long long)b.limb_begin[b.njobs] << t.logN;
+  const int cls = work <= kTinyNttWork ? 0 : work <= kSmallNttWork ? 1 : 2;
+  const int v = cls == 0 ? t.fwd_variant_tiny : cls == 1 ? t.fwd_variant_small : t.fwd_variant;
+  switch (t.logN) {
+    case 10: return launch_t_epi<10>(b, e, t, s);
+    case 11: return launch_t_epi<11>(b, e, t, s);
+    case 12: return launch_t_epi<12>(b, e, t, s);
+    case 13: return v == 1 ? launch_t_epi<13>(b, e, t, s) : v == 2 ? launch16_epi<13, 12>(b, e, t, s)
+                                                                   : launch16_epi<13, 13>(b, e, t, s);
+    case 14: return v == 1 ? launch_t_epi<14>(b, e, t, s) : v == 2 ? launch16_epi<14, 12>(b, e, t, s)
+                                                                   : launch16_epi<14, 13>(b, e, t, s);
+    case 15: return v == 1 ? launch_t_epi<15>(b, e, t, s) : v == 2 ? launch16_epi<15, 12>(b, e, t, s)
+                                                                   : launch16_epi<15, 13>(b, e, t, s);
+    case 16: return v == 1 ? launch_t_epi<16>(b, e, t, s) : v == 2 ? launch16_epi<16, 12>(b, e, t, s)
+                                                                   : launch16_epi<16, 13>(b, e, t, s);
+    default: return cudaErrorNotSupported;
   }
 }
 

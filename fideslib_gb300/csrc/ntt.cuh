@@ -30,6 +30,26 @@ struct NttBatch {
   NttJob jobs[kMaxNttJobs];
 };
 
+// Rescale fused into the forward transform, as the reference's NTT_RESCALE fusion folds its epilogue into the NTT
+// (src/NTTfusions.cuh:214-235).  NTT job z reads one row per poly k (coefficients of prime switch_top, the INTT of
+// the dropped tower, at src + k * src_stride), switches each value into q_j on load with the centred rule
+// (x > q_top / 2: x + q_j - [q_top]_{q_j}), transforms it, and instead of storing the transform writes
+//   out[k * out_ps + j][n] = (x[k * x_ps + j][n] - NTT(switched row)[n]) * w[j]  mod q_j      (x in [0, q_j))
+// for limbs j < limbs of the job.  (A ModDown fused the same way measured slower on single operations and no faster
+// on batches than its separate epilogue kernel, so ModDown keeps that kernel.)
+struct NttEpiJob {
+  const u64* x;
+  u64* out;
+  const ulonglong2* w;  // [j] = {w_j, shoup(w_j)}
+  int x_ps;             // poly stride of x in limbs
+  int out_ps;           // poly stride of out in limbs
+  int switch_top;
+};
+
+struct NttEpi {
+  NttEpiJob jobs[kMaxNttJobs];
+};
+
 struct DeviceTables {
   const PrimeConst* pc;      // [ntowers]
   // [ntowers][N] {psi^brev(i), shoup} / {psi^-brev(i), shoup}, with the entries of the last four stages transposed:
@@ -56,6 +76,10 @@ constexpr long long kSmallNttWork = 128ll << 16;  // 128 limbs at N = 2^16
 
 // Forward (inverse=false: coefficient -> evaluation, bit-reversed) or inverse transform of every job.
 cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s);
+
+// Forward transform of every job with the fused rescale `e`, on the kernel variant launch_ntt would pick
+// (N = 2^10 .. 2^16).
+cudaError_t launch_ntt_epi(const NttBatch& b, const NttEpi& e, const DeviceTables& t, cudaStream_t s);
 
 // Autotuner: times every kernel variant of both directions on scratch batches of this ring (device memory from the
 // stream-ordered pool, synchronising `s`) of 8, 32 and 640 limbs' worth of residues at N = 2^16 (tiny, small,
