@@ -29,6 +29,8 @@ struct PrimeConst {
   u64 ninv;     // N^-1 mod p
   u64 ninv_sh;
   u64 negp;     // 2^64 - p
+  u64 w1ninv;   // psi^-brev(1) * N^-1 mod p: the inverse transform's last-stage twiddle with N^-1 folded in
+  u64 w1ninv_sh;
 };
 
 __device__ __forceinline__ u64 mulhi(u64 a, u64 b) { return __umul64hi(a, b); }

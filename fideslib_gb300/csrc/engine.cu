@@ -232,6 +232,8 @@ bool Context::build(const u64* roots, std::string* err) {
     c.ninv = hinv((u64)N, p);
     c.ninv_sh = shoup_of(c.ninv, p);
     c.negp = 0ull - p;
+    c.w1ninv = hmul(hpow(hinv(psi[i], p), (u64)N / 2, p), c.ninv, p);  // psi^-brev(1) = psi^-(N/2)
+    c.w1ninv_sh = shoup_of(c.w1ninv, p);
   }
   d_pc = (PrimeConst*)dmalloc(sizeof(PrimeConst) * ntow);
   if (!d_pc) {

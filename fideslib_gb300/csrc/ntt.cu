@@ -57,6 +57,17 @@ __device__ __forceinline__ void gs_bfly(u64& X, u64& Y, const ulonglong2& w, u64
   Y = shoup_lazy4(d, w.x, w.y, negp);
 }
 
+// The inverse's last stage (s = 0, one twiddle w1 = psi^-brev(1)) with N^-1 folded in: X, Y in [0, 4p) ->
+// (X + Y) N^-1, (X - Y + 4p) w1 N^-1, both in [0, 4p).  Saves the separate scaling of every output by N^-1.
+struct LastStage {
+  u64 ninv, ninv_sh, w1ninv, w1ninv_sh;
+};
+__device__ __forceinline__ void gs_bfly_last(u64& X, u64& Y, const LastStage& c, u64 negp, u64 p4) {
+  const u64 s = X + Y, d = X - Y + p4;
+  X = shoup_lazy4(s, c.ninv, c.ninv_sh, negp);
+  Y = shoup_lazy4(d, c.w1ninv, c.w1ninv_sh, negp);
+}
+
 // Radix-2^LOGR stages over x[k] = a[G*2^(LOGS+LOGR) + k*2^LOGS + low] (low < 2^LOGS).  At the sub-stage on
 // bit kb of k the pair distance is 2^(LOGS+kb), the global stage is s = LOGN-1-(LOGS+kb) and the twiddle of
 // the pair whose lower member is k has table index 2^s + G*2^(LOGR-1-kb) + j, j = k >> (kb+1).  The last four
@@ -90,17 +101,22 @@ __device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulon
   }
 }
 
+// last != null: these stages end the transform (their final stage is s = 0), which then applies N^-1 (LastStage).
 template <int LOGR, int LOGS, int LOGN>
 __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 negp,
-                                          u64 p4) {
+                                          u64 p4, const LastStage* last = nullptr) {
 #pragma unroll
   for (int kb = 0; kb < LOGR; kb++) {
     const int s = LOGN - 1 - (LOGS + kb);
 #pragma unroll
     for (int k = 0; k < (1 << LOGR); k++) {
       if (k & (1 << kb)) continue;
-      const ulonglong2 w = __ldg(tw_entry<LOGR, LOGS, LOGN>(tw, s, kb, G, k >> (kb + 1)));
-      gs_bfly(x[k], x[k + (1 << kb)], w, negp, p4);
+      if (s == 0 && last) {
+        gs_bfly_last(x[k], x[k + (1 << kb)], *last, negp, p4);
+      } else {
+        const ulonglong2 w = __ldg(tw_entry<LOGR, LOGS, LOGN>(tw, s, kb, G, k >> (kb + 1)));
+        gs_bfly(x[k], x[k + (1 << kb)], w, negp, p4);
+      }
     }
   }
 }
@@ -310,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
   const LimbRef L = locate(b, S::N);
   if (!L.valid) return;
   const PrimeConst& pc = T.pc[L.prime];
-  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp, ninv = pc.ninv, ninv_sh = pc.ninv_sh;
+  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp;
   const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
@@ -351,15 +367,17 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
       const int l = k * 256 + tid;
       x[k] = (l < S::E) ? sm[swz(l)] : 0ull;
     }
-    inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4);
-    if constexpr (S::C == 1) {
+    if constexpr (S::C == 1) {  // this pass ends the transform
+      const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
+      inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4, &last);
 #pragma unroll
       for (int k = 0; k < R; k++) {
         const int l = k * 256 + tid;
-        if (l < S::E) L.dst[l] = csub(csub(shoup_lazy4(x[k], ninv, ninv_sh, negp), p2), p);
+        if (l < S::E) L.dst[l] = csub(csub(x[k], p2), p);
       }
       return;
     } else {
+      inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4);
 #pragma unroll
       for (int k = 0; k < R; k++) sm[swz(k * 256 + tid)] = x[k];
     }
@@ -380,9 +398,10 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
         const u64* src = cl.map_shared_rank(sm, hh);
         x[hh] = src[swz(l)];
       }
-      inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, negp, p4);
+      const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
+      inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, negp, p4, &last);
 #pragma unroll
-      for (int hh = 0; hh < S::C; hh++) L.dst[hh * S::E + l] = csub(csub(shoup_lazy4(x[hh], ninv, ninv_sh, negp), p2), p);
+      for (int hh = 0; hh < S::C; hh++) L.dst[hh * S::E + l] = csub(csub(x[hh], p2), p);
     }
     cl.sync();  // peers may still be reading this CTA's shared memory
   }
@@ -535,7 +554,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
   const LimbRef L = locate(b, S::N);
   if (!L.valid) return;
   const PrimeConst& pc = T.pc[L.prime];
-  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp, ninv = pc.ninv, ninv_sh = pc.ninv_sh;
+  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp;
   const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
@@ -596,9 +615,10 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
 #pragma unroll
         for (int k = 0; k < R; k++) x[k] = sm[swz(k * 4096 + col)];
       }
-      inv_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4);
+      const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
+      inv_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4, &last);
 #pragma unroll
-      for (int k = 0; k < R; k++) L.dst[k * 4096 + col] = csub(csub(shoup_lazy4(x[k], ninv, ninv_sh, negp), p2), p);
+      for (int k = 0; k < R; k++) L.dst[k * 4096 + col] = csub(csub(x[k], p2), p);
     }
     if constexpr (S::C > 1) cg::this_cluster().sync();  // peers may still be reading this CTA's shared memory
   }
