@@ -36,6 +36,23 @@ constexpr int kThreads = 256;
 
 __device__ __forceinline__ int swz(int l) { return l ^ ((l >> 5) & 15); }
 
+// Distributed shared memory through 32-bit shared::cluster addresses: element `local` of this CTA's shared memory as
+// it appears in the cluster window at CTA `rank` (one register per address instead of a 64-bit generic pointer, which
+// keeps the cross-CTA phases of the radix-16 kernels free of register spills).
+__device__ __forceinline__ uint32_t peer_smem(const u64* local, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"((uint32_t)__cvta_generic_to_shared(local)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ u64 ld_peer(uint32_t addr) {
+  u64 v;
+  asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_peer(uint32_t addr, u64 v) {
+  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+
 // Forward (CT): x + wY, x - wY + 4p with wY from shoup_lazy4 in [0, 4p).  Values stay below 16p (< 2^64 for
 // p < 2^60): a stage with the correction maps X in [0, 16p) to x in [0, 8p) (X - 8p when X >= 8p) and outputs
 // [0, 12p); a stage without it takes X in [0, 12p) and outputs [0, 16p).  Stages alternate (correction on even global
@@ -244,10 +261,7 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
     for (int it = 0; it < IT; it++) {
       const int l = c * LPC + it * kThreads + tid;
 #pragma unroll
-      for (int hh = 0; hh < S::C; hh++) {
-        u64* dst = cl.map_shared_rank(sm, hh);
-        dst[swz(l)] = x[it][hh];
-      }
+      for (int hh = 0; hh < S::C; hh++) st_peer(peer_smem(sm + swz(l), hh), x[it][hh]);
     }
     cl.sync();
     h = c;
@@ -394,10 +408,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
       const int l = c * LPC + it * kThreads + tid;
       u64 x[S::C];
 #pragma unroll
-      for (int hh = 0; hh < S::C; hh++) {
-        const u64* src = cl.map_shared_rank(sm, hh);
-        x[hh] = src[swz(l)];
-      }
+      for (int hh = 0; hh < S::C; hh++) x[hh] = ld_peer(peer_smem(sm + swz(l), hh));
       const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
       inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, negp, p4, &last);
 #pragma unroll
@@ -469,12 +480,9 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
       fwd_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4);
       if constexpr (S::C > 1) {
         if (q == 0) asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
-        cg::cluster_group cl = cg::this_cluster();
 #pragma unroll
-        for (int k = 0; k < R; k++) {
-          u64* dst = cl.map_shared_rank(sm, k >> S::LOCAL);
-          dst[swz((k & ((1 << S::LOCAL) - 1)) * 4096 + col)] = x[k];
-        }
+        for (int k = 0; k < R; k++)
+          st_peer(peer_smem(sm + swz((k & ((1 << S::LOCAL) - 1)) * 4096 + col), k >> S::LOCAL), x[k]);
       } else {
 #pragma unroll
         for (int k = 0; k < R; k++) sm[swz(k * 4096 + col)] = x[k];
@@ -605,12 +613,9 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
       const int col = h * S::COLS + q * kThreads16 + tid;
       u64 x[R];
       if constexpr (S::C > 1) {
-        cg::cluster_group cl = cg::this_cluster();
 #pragma unroll
-        for (int k = 0; k < R; k++) {
-          const u64* src = cl.map_shared_rank(sm, k >> S::LOCAL);
-          x[k] = src[swz((k & ((1 << S::LOCAL) - 1)) * 4096 + col)];
-        }
+        for (int k = 0; k < R; k++)
+          x[k] = ld_peer(peer_smem(sm + swz((k & ((1 << S::LOCAL) - 1)) * 4096 + col), k >> S::LOCAL));
       } else {
 #pragma unroll
         for (int k = 0; k < R; k++) x[k] = sm[swz(k * 4096 + col)];
