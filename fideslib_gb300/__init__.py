@@ -123,6 +123,8 @@ _SIGS = {
     "fides_ext_store": (C.c_int, [C.c_void_p, C.c_uint32, u64p, C.c_void_p]),
     "fides_eval_many_to_one": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, u32p, u32p,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double), u32p]),
+    "fides_eval_linear_wsum": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), u32p]),
     "fides_level_reduce": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_mod_raise": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u32p]),
     "fides_lt_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, u64p, C.POINTER(C.c_uint8),
@@ -483,6 +485,19 @@ class CryptoContext:
         _check(lib().fides_eval_many_to_one(self._h, op, nb, stride, ptr(a_arr, u32), ptr(b_arr, u32),
                                             ptr(v_arr, f64), ptr(s_arr, f64), ptr(outs, u32)))
         return None if in_place else [int(x) for x in outs]
+
+    def eval_linear_wsum(self, terms, weights, scales) -> list[int]:
+        """Weighted sums in lock step (fides_eval_linear_wsum): terms[k][i] is term k of sum i, weights[k] its
+        weight, scales[k][i] the scale its weight is encoded at; returns one handle per sum."""
+        t = np.ascontiguousarray(np.array(terms, dtype=np.uint32))
+        n, m = t.shape
+        w = np.ascontiguousarray(np.array(weights, dtype=np.float64))
+        sc = np.ascontiguousarray(np.array(scales, dtype=np.float64).reshape(n, m))
+        outs = np.zeros(m, dtype=np.uint32)
+        f64 = C.POINTER(C.c_double)
+        _check(lib().fides_eval_linear_wsum(self._h, m, n, _p(t, u32p), w.ctypes.data_as(f64), sc.ctypes.data_as(f64),
+                                            _p(outs, u32p)))
+        return [int(x) for x in outs]
 
     # --- extended-basis ciphertexts (EvalFastRotationExt / KeySwitchDown) ---
     def eval_fast_rotation_ext(self, a: int, indices, add_first: bool = True, pre: int = 0) -> list[int]:

@@ -1116,6 +1116,82 @@ int fides_eval_many_to_one(fides_ctx* ctx, int32_t op, uint32_t nb, uint32_t str
   return FIDES_OK;
 }
 
+int fides_eval_linear_wsum(fides_ctx* ctx, uint32_t m, uint32_t n_terms, const uint32_t* cts, const double* weights,
+                           const double* scales, uint32_t* outs) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  if (m == 0) return FIDES_OK;
+  if (!cts || !weights || !scales || !outs) return fail(FIDES_EINVAL, "null argument");
+  if (n_terms < 1 || n_terms > 2 * fgb::kMaxWsumTerms) return fail(FIDES_EINVAL, "n_terms must be in [1, 16]");
+  fgb::Context* c = ctx->c;
+  const size_t total = (size_t)m * n_terms;
+  std::vector<const fgb::DevCt*> A(total);
+  for (size_t k = 0; k < total; k++) {
+    if (!(A[k] = find_ct(ctx, cts[k]))) return fail(FIDES_EINVAL, "unknown ciphertext handle " + std::to_string(cts[k]));
+    if (A[k]->noise_deg != 1) return fail(FIDES_EINVAL, "weighted-sum terms must have noise degree 1");
+  }
+  std::vector<fgb::DevCt> R(m);
+  for (uint32_t i = 0; i < m; i++) {
+    fgb::DevCt r = *A[i];
+    for (uint32_t k = 1; k < n_terms; k++) r.t = std::min(r.t, A[(size_t)k * m + i]->t);
+    r.scale = A[i]->scale * scales[i];
+    r.noise_deg = 2;
+    r.data = c->alloc_limbs((size_t)2 * r.t, c->stream);
+    if (!r.data) {
+      for (uint32_t q = 0; q < i; q++) c->free_limbs(R[q].data, c->stream);
+      return fail(FIDES_ENOMEM, "ciphertext allocation failed");
+    }
+    R[i] = r;
+  }
+  // Elements whose constant columns (scales[k*m + i] over k) agree share one launch's constant set; terms go
+  // in chunks of kMaxWsumTerms, later chunks accumulating into the output.
+  const fgb::Ring ring{c->N, c->logN};
+  auto same_set = [&](uint32_t x, uint32_t y) {
+    for (uint32_t k = 0; k < n_terms; k++)
+      if (scales[(size_t)k * m + x] != scales[(size_t)k * m + y]) return false;
+    return true;
+  };
+  cudaError_t e = cudaSuccess;
+  for (uint32_t k0 = 0; k0 < n_terms && e == cudaSuccess; k0 += fgb::kMaxWsumTerms) {
+    const uint32_t nk = std::min<uint32_t>(fgb::kMaxWsumTerms, n_terms - k0);
+    fgb::WsumBatch wb{};
+    auto flush = [&]() {
+      const cudaError_t x = wb.njobs ? fgb::launch_wsum(wb, ring, c->d_pc, c->stream) : cudaSuccess;
+      wb.njobs = 0;
+      return x;
+    };
+    uint32_t lead = 0;  // element whose constants the batch carries
+    for (uint32_t i = 0; i < m && e == cudaSuccess; i++) {
+      if (wb.njobs == fgb::kMaxJobs || (wb.njobs && !same_set(lead, i))) e = flush();
+      if (e != cudaSuccess) break;
+      if (wb.njobs == 0) {
+        lead = i;
+        wb.nterms = (int)nk;
+        wb.accumulate = k0 > 0;
+        for (uint32_t k = 0; k < nk; k++)
+          for (int j = 0; j < c->nq; j++) {
+            const uint64_t w = double_residue(weights[k0 + k] * scales[(size_t)(k0 + k) * m + i], c->mod[j]);
+            wb.set.mul[k][j] = w;
+            wb.set.mul_sh[k][j] = shoup_const(w, c->mod[j]);
+          }
+      }
+      fgb::WsumJob& J = wb.jobs[wb.njobs++];
+      for (uint32_t k = 0; k < nk; k++) {
+        J.term[k] = A[(size_t)(k0 + k) * m + i]->data;
+        J.term_t[k] = A[(size_t)(k0 + k) * m + i]->t;
+      }
+      J.out = R[i].data;
+      J.t = R[i].t;
+    }
+    if (e == cudaSuccess) e = flush();
+  }
+  if (e != cudaSuccess) {
+    for (uint32_t i = 0; i < m; i++) c->free_limbs(R[i].data, c->stream);
+    return cuda_fail(e, "weighted sum");
+  }
+  for (uint32_t i = 0; i < m; i++) outs[i] = register_ct(ctx, R[i]);
+  return FIDES_OK;
+}
+
 int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out) {
   if (!valid_ctx(ctx) || !out) return fail(FIDES_EINVAL, "null argument");
   fgb::Context* c = ctx->c;

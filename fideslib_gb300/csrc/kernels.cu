@@ -460,6 +460,32 @@ __global__ void __launch_bounds__(kT) scalar_kernel(const __grid_constant__ Scal
   st2(J.out + o1, make_ulonglong2(shoup(x1.x, w, wsh, q), shoup(x1.y, w, wsh, q)));
 }
 
+// grid (N/512, 2 t per job): two coefficients of one row per thread; every term's values are loaded before the
+// products, each product reduced (Shoup) and summed mod q.
+__global__ void __launch_bounds__(kT) wsum_kernel(const __grid_constant__ WsumBatch b, Ring r,
+                                                  const PrimeConst* __restrict__ pc) {
+  const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
+  const WsumJob& J = b.jobs[z];
+  const int row = (int)blockIdx.y - b.row_begin[z];
+  const int poly = row >= J.t ? 1 : 0, j = row - poly * J.t;
+  const size_t n = ((size_t)blockIdx.x * kT + threadIdx.x) * 2;
+  const u64 q = pc[j].p;
+  ulonglong2 x[kMaxWsumTerms];
+#pragma unroll
+  for (int k = 0; k < kMaxWsumTerms; k++)
+    if (k < b.nterms) x[k] = ld2(J.term[k] + ((size_t)poly * J.term_t[k] + j) * r.N + n);
+  u64* o = J.out + ((size_t)poly * J.t + j) * r.N + n;
+  ulonglong2 acc = b.accumulate ? ld2(o) : make_ulonglong2(0, 0);
+#pragma unroll
+  for (int k = 0; k < kMaxWsumTerms; k++)
+    if (k < b.nterms) {
+      const u64 w = b.set.mul[k][j], wsh = b.set.mul_sh[k][j];
+      acc.x = add_mod(acc.x, shoup(x[k].x, w, wsh, q), q);
+      acc.y = add_mod(acc.y, shoup(x[k].y, w, wsh, q), q);
+    }
+  st2(o, acc);
+}
+
 // grid rows per job: 2*t (poly-major).  X^k at point psi^(2 brev(i) + 1) is psi^e, e = (2 brev(i) + 1) k mod 2N;
 // psi^e = tw[brev(e)] for e < N and -tw[brev(e - N)] otherwise (psi^N = -1).
 __global__ void __launch_bounds__(kT) monomial_kernel(const __grid_constant__ MonoBatch b, Ring r,
@@ -810,6 +836,16 @@ cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst*
   ScalarBatch bb;
   const int rows = with_rows(b, bb, [](const ScalarJob& j) { return j.t; });
   scalar_kernel<<<dim3(r.N / (2 * kT), rows, 1), kT, 0, s>>>(bb, r, pc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wsum(const WsumBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s) {
+  if (b.njobs <= 0) return cudaSuccess;
+  if (b.nterms < 1 || b.nterms > kMaxWsumTerms) return cudaErrorInvalidValue;
+  WsumBatch bb;
+  const int rows = with_rows(b, bb, [](const WsumJob& j) { return 2 * j.t; });
+  wsum_kernel<<<dim3(r.N / (2 * kT), rows, 1), kT, 0, s>>>(bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }

@@ -138,6 +138,28 @@ struct ScalarBatch {
   ScalarSet sets[kMaxScalarSets];
 };
 
+// Weighted sums out = sum_k mul[k][j] * term_k over [2][t][N] (term k laid out [2][term_t[k]][N], rows j < t read),
+// one constant set shared by every job of the launch; accumulate != 0 adds the sum to what out holds.
+constexpr int kMaxWsumTerms = 8;
+struct WsumSet {
+  u64 mul[kMaxWsumTerms][64];
+  u64 mul_sh[kMaxWsumTerms][64];
+};
+struct WsumJob {
+  const u64* term[kMaxWsumTerms];
+  int term_t[kMaxWsumTerms];
+  u64* out;
+  int t;
+};
+struct WsumBatch {
+  int njobs;
+  int nterms;
+  int accumulate;
+  int row_begin[kMaxJobs + 1];
+  WsumJob jobs[kMaxJobs];
+  WsumSet set;
+};
+
 // Baby-step/giant-step inner sums: job (x, g, ng) writes, for the giant steps g .. g+ng-1,
 // out + k*out_stride ([2][rows][N]) = sum_{b<bs, present} rot[b] (.) pt[(g+k)*bs+b] with rot[0] = rot0 (the input
 // itself), rot[b] = rot_base + (b-1)*rot_stride ([2][rows][N] each) and pt[i] = pt_base + i*pt_stride.  One thread
@@ -213,6 +235,7 @@ struct MonoBatch {
 cudaError_t launch_ptop(const PtBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
+cudaError_t launch_wsum(const WsumBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_sum(const SumBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_raise_switch(const RaiseBatch& b, const Ring& r, const PrimeConst* pc, cudaStream_t s);
 cudaError_t launch_monomial(const MonoBatch& b, const Ring& r, const PrimeConst* pc, const ulonglong2* tw_fwd,

@@ -16,8 +16,8 @@
 //   p    = the coefficients (zero-padded to bs 2^m) split recursively by Chebyshev division at M = bs 2^(i-1)
 //          (node()); each part is evaluated at a target scale chosen so that every addition adds equal scales:
 //          a leaf sum_{k<bs} c_k T_k is Rescale(sum T_k * c_k) with c_k encoded at target * q_drop / scale(T_k)
-//          (terms dropped to their smallest tower count, summed in increasing k); the top-level target is the
-//          scale of T_1, so the result keeps the input's scale; the constant of the series is added last.
+//          (one weighted sum over the terms at their smallest tower count); the top-level target is the scale of
+//          T_1, so the result keeps the input's scale; the constant of the series is added last.
 // Non-scalar products for degree d: bs - 1 + (m - 1) + (2^m - 1) (16 for d = 47, against 46 for the full
 // T_1 .. T_d ladder).  Exact scale matching is what OpenFHE's FLEXIBLEAUTO mode does; without it sums of
 // terms whose scales differ by the primes' distance from the nominal scale carry that relative error, which the
@@ -149,32 +149,30 @@ struct Part {
   double c = 0.0;
 };
 
-// sum_{k<bs} c_k T_k at scale `target`: Rescale(sum_{k>=1, c_k != 0} T_k * c_k), term k's constant encoded at
-// target * q_drop / scale(T_k) (q_drop = the prime the rescale removes), terms dropped to their smallest tower
-// count and summed in increasing k; c_0 kept aside.
+// sum_{k<bs} c_k T_k at scale `target`: Rescale(sum T_k * c_k over k >= 1, c_k != 0), term k's constant encoded at
+// target * q_drop / scale(T_k) (q_drop = the prime the rescale removes), the terms read at their smallest tower
+// count and summed by one weighted-sum launch (the reference evaluates the same leaf with evalLinearWSumMutable,
+// src/CKKS/ApproxModEval.cu:213); c_0 kept aside.
 int leaf(Poly& P, const double* c, int bs, const std::vector<double>& target, Part& out) {
   const Towers tl = leaf_towers(P, c, bs);
-  V acc;
+  std::vector<V> terms;
+  std::vector<double> w;
+  std::vector<std::vector<double>> f;
   for (int k = 1; k < bs; k++) {
     if (c[k] == 0.0) continue;
-    std::vector<uint32_t> t(tl.size());
-    for (size_t e = 0; e < t.size(); e++) t[e] = (uint32_t)(tl[e] + 1);
-    V X, term;
-    FGB_TRY(fgb::vec::drop_to(P.sc, P.T[k], t, X));
-    const std::vector<double> sk = fgb::vec::scales(P.ctx, X);
-    std::vector<double> f(sk.size());
-    for (size_t e = 0; e < f.size(); e++) f[e] = target[e] * P.q[tl[e]] / sk[e];
-    FGB_TRY(fgb::vec::mult_scalar_at(P.sc, X, c[k], f, term));
-    if (acc.empty()) {
-      acc = term;
-    } else {
-      V s2;
-      FGB_TRY(fgb::vec::add(P.sc, acc, term, s2));
-      acc = s2;
-    }
+    const std::vector<double> sk = fgb::vec::scales(P.ctx, P.T[k]);
+    std::vector<double> fk(sk.size());
+    for (size_t e = 0; e < fk.size(); e++) fk[e] = target[e] * P.q[tl[e]] / sk[e];
+    terms.push_back(P.T[k]);
+    w.push_back(c[k]);
+    f.push_back(std::move(fk));
   }
   out.ct.clear();
-  if (!acc.empty()) FGB_TRY(fgb::vec::rescale(P.sc, acc, out.ct));
+  if (!terms.empty()) {
+    V acc;
+    FGB_TRY(fgb::vec::wsum(P.sc, terms, w, f, acc));
+    FGB_TRY(fgb::vec::rescale(P.sc, acc, out.ct));
+  }
   out.c = c[0];
   return FIDES_OK;
 }

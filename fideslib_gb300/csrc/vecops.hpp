@@ -149,6 +149,25 @@ inline int drop_to(Scope& sc, const V& a, const std::vector<uint32_t>& t, V& out
   return FIDES_OK;
 }
 
+// out[i] = sum_k round(w[k] * scale[k][i]) * terms[k][i] on the smallest tower count of element i's terms, one
+// weighted-sum launch per 64 elements (fides_eval_linear_wsum); the result has the scale of terms[0][i] times
+// scale[0][i] and noise degree 2.
+inline int wsum(Scope& sc, const std::vector<V>& terms, const std::vector<double>& w,
+                const std::vector<std::vector<double>>& scale, V& out) {
+  const size_t n = terms.size(), m = terms[0].size();
+  std::vector<uint32_t> cts(n * m);
+  std::vector<double> s(n * m);
+  for (size_t k = 0; k < n; k++)
+    for (size_t i = 0; i < m; i++) {
+      cts[k * m + i] = terms[k][i];
+      s[k * m + i] = scale[k][i];
+    }
+  out.assign(m, 0);
+  FGB_TRY(fides_eval_linear_wsum(sc.ctx, (uint32_t)m, (uint32_t)n, cts.data(), w.data(), s.data(), out.data()));
+  sc.keep(out);
+  return FIDES_OK;
+}
+
 inline std::vector<double> scales(fides_ctx* ctx, const V& a) {
   std::vector<double> s(a.size());
   for (size_t i = 0; i < a.size(); i++) s[i] = scale_of(ctx, a[i]);

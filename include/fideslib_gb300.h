@@ -249,6 +249,14 @@ int fides_eval_add_scalar(fides_ctx* ctx, uint32_t a, double v, uint32_t* out);
 enum { FIDES_OP_MULT_SCALAR = 13, FIDES_OP_ADD_SCALAR = 14, FIDES_OP_MULT_INT = 15 };
 int fides_eval_many_to_one(fides_ctx* ctx, int32_t op, uint32_t nb, uint32_t stride, const uint32_t* a,
                            const uint32_t* b, const double* values, const double* scales, uint32_t* outs);
+/* Weighted sum of ciphertexts, m sums in lock step (Ciphertext::evalLinearWSumMutable, src/CKKS/Ciphertext.cpp:
+ * 1171-1212, as the reference's Chebyshev evaluation uses it, src/CKKS/ApproxModEval.cu:213,255,328): for i < m,
+ *   outs[i] = sum_{k < n_terms} round(weights[k] * scales[k*m + i]) * cts[k*m + i]
+ * on the smallest tower count among element i's terms, in one launch per 64 sums (one kernel pass reading each term
+ * once).  Every term must have noise degree 1; the result has noise degree 2 and the scale of its first term times
+ * scales[i] (the caller chooses the scales so that all terms land on that scale).  n_terms <= 16. */
+int fides_eval_linear_wsum(fides_ctx* ctx, uint32_t m, uint32_t n_terms, const uint32_t* cts, const double* weights,
+                           const double* scales, uint32_t* outs);
 /* Keeps the first `towers` towers (LevelReduce / SetLevel, api/CryptoContext.hpp:184). */
 int fides_level_reduce(fides_ctx* ctx, uint32_t a, uint32_t towers, uint32_t* out);
 /* ModRaise (src/CKKS/Bootstrap.cu:393-...): tower 0 of `a`, lifted (centred) to `towers` towers. */

@@ -182,3 +182,33 @@ def test_plaintext_requests_through_the_server(env):
     srv.close()
     for o, d in zip(outs, direct):
         assert np.array_equal(gpu.store_ciphertext(o), d)
+
+
+@pytest.mark.parametrize("m,n_terms,shared", [(1, 1, True), (5, 7, True), (70, 3, True), (6, 11, False)])
+def test_linear_wsum(env, m, n_terms, shared):
+    """Weighted sums in lock step (fides_eval_linear_wsum, the reference's evalLinearWSumMutable): each sum equals
+    the oracle's scalar products of its terms (constants round(w_k * scale_ki)) added up, on the smallest tower
+    count of its terms.  70 sums split the launch by job count, 11 terms into two launches (the second
+    accumulating), per-sum constant columns into one launch per column."""
+    gpu, orc = env.gpu, env.orc
+    towers = [[int(env.rng.integers(2, NQ + 1)) for _ in range(m)] for _ in range(n_terms)]
+    terms = [env.cts(row) for row in towers]
+    weights = list(env.rng.uniform(-2, 2, n_terms))
+    if shared:
+        col = [2.0 ** int(e) for e in env.rng.integers(10, 40, n_terms)]
+        scales = [[col[k]] * m for k in range(n_terms)]
+    else:
+        scales = [[2.0 ** int(e) for e in env.rng.integers(10, 40, m)] for _ in range(n_terms)]
+    outs = gpu.eval_linear_wsum([[h for h in terms[k][1]] for k in range(n_terms)], weights, scales)
+    for i, o in enumerate(outs):
+        t = min(towers[k][i] for k in range(n_terms))
+        mods = env.mods[:t]
+        acc = None
+        for k in range(n_terms):
+            a = np.ascontiguousarray(terms[k][0][i][:, :t])
+            p = orc.scalar_op(a, [double_residue(weights[k] * scales[k][i], q) for q in mods], [0] * t)
+            acc = p if acc is None else orc.add(acc, p)
+        assert np.array_equal(gpu.store_ciphertext(o), acc), (m, n_terms, i)
+        meta = gpu.meta(o)
+        assert (meta.towers, meta.noise_deg) == (t, 2)
+        assert meta.scale == SCALE * scales[0][i]
