@@ -193,14 +193,6 @@ __device__ __forceinline__ SwitchIn switch_in(const NttBatch& b, const DeviceTab
   return sw;
 }
 
-// Starts pulling the rescale's x operands for residues n0 .. n0 + 15 (one 128-byte line) into L1 before the last
-// pass's butterflies, so their loads after it do not wait on HBM.
-template <int LOGN>
-__device__ __forceinline__ void epi_prefetch(const NttEpi* e, const LimbRef& L, int n0) {
-  const NttEpiJob& E = e->jobs[L.job];
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(E.x + ((size_t)L.poly * E.x_ps + L.row) * (1 << LOGN) + n0));
-}
-
 // Output side of the fused rescale for a thread's 16 contiguous residues x (in [0, 16p)) at n0 .. n0 + 15.
 template <int LOGN>
 __device__ __forceinline__ void epi_store16(const NttEpi* e, const LimbRef& L, int n0, const u64 (&x)[16], u64 p) {
@@ -301,7 +293,6 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
-    if constexpr (EPI) epi_prefetch<LOGN>(e, L, h * S::E + g * 16);
     fwd_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p4);
     if constexpr (EPI) {
       epi_store16<LOGN>(e, L, h * S::E + g * 16, x, p);
@@ -520,7 +511,6 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
-    if constexpr (EPI) epi_prefetch<LOGN>(e, L, h * S::E + g * 16);
     fwd_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p4);
     if constexpr (EPI) {
       epi_store16<LOGN>(e, L, h * S::E + g * 16, x, p);
