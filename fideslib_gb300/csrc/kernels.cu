@@ -227,34 +227,41 @@ __global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
   const size_t N = r.N;
   const int beta = (t + c.alpha - 1) / c.alpha;
   const size_t khalf = (size_t)c.dnum * c.ntow * N, kstep = (size_t)c.ntow * N;
+  // Digit d's row j is the input's own tower (row j of a) inside the digit, else row jj of its converted block.
+  // For three digits (three CTAs per SM, 80 registers) the rows are kept as 32-bit indices (negative: row -1-r of
+  // a) and turned into pointers per iteration, so no 64-bit pointers stay live across the products: that instance
+  // then has no register spills (68 bytes of spill stores with the pointers held).  The other instances spill less
+  // with the pointers worked out once, so they keep that form (ptxas -v).
+  constexpr bool kRowIndex = MAXB == 3;
   const u64* src[MAXB];
-  const u64* key = J.key + (size_t)tower * N;
+  int srow[MAXB];
 #pragma unroll
   for (int d = 0; d < MAXB; d++) {
     if (d >= beta) break;
     const int start = d * c.alpha;
     const int s = min(c.alpha, t - start);
-    if (j >= start && j < start + s) {
-      src[d] = J.a + (size_t)j * N;
-    } else {
-      const int jj = j < start ? j : j - s;
-      src[d] = J.conv + ((size_t)d * ext + jj) * N;
-    }
+    srow[d] = (j >= start && j < start + s) ? -1 - j : d * ext + (j < start ? j : j - s);
+    if constexpr (!kRowIndex) src[d] = srow[d] < 0 ? J.a + (size_t)j * N : J.conv + (size_t)srow[d] * N;
   }
-  u64* out0 = J.inner + (size_t)j * N;
-  u64* out1 = J.inner + ((size_t)ext + j) * N;
   const PrimeConst& P = pc[tower];
   const u64 p4 = 4 * P.p;
+  const u64* key0 = J.key + (size_t)tower * N;
 #pragma unroll 1
   for (int it = 0; it < iters; it++) {
     const int n = (((int)blockIdx.x * iters + it) * kT + (int)threadIdx.x) * 2;
     ulonglong2 D[MAXB], KA[MAXB], KB[MAXB];
+    const u64* key = key0 + n;
 #pragma unroll
     for (int d = 0; d < MAXB; d++) {
       if (d >= beta) break;
-      D[d] = *reinterpret_cast<const ulonglong2*>(src[d] + n);
-      KA[d] = *reinterpret_cast<const ulonglong2*>(key + d * kstep + n);
-      KB[d] = *reinterpret_cast<const ulonglong2*>(key + d * kstep + khalf + n);
+      const u64* sp;
+      if constexpr (kRowIndex)
+        sp = srow[d] < 0 ? J.a + (size_t)(-1 - srow[d]) * N : J.conv + (size_t)srow[d] * N;
+      else
+        sp = src[d];
+      D[d] = *reinterpret_cast<const ulonglong2*>(sp + n);
+      KA[d] = *reinterpret_cast<const ulonglong2*>(key + d * kstep);
+      KB[d] = *reinterpret_cast<const ulonglong2*>(key + d * kstep + khalf);
     }
     u64 v0[2], v1[2];
 #pragma unroll
@@ -274,8 +281,8 @@ __global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
       v0[e] = csub(reduce128_lazy8(h0, l0, P), p4);
       v1[e] = csub(reduce128_lazy8(h1, l1, P), p4);
     }
-    *reinterpret_cast<ulonglong2*>(out0 + n) = make_ulonglong2(v0[0], v0[1]);
-    *reinterpret_cast<ulonglong2*>(out1 + n) = make_ulonglong2(v1[0], v1[1]);
+    *reinterpret_cast<ulonglong2*>(J.inner + (size_t)j * N + n) = make_ulonglong2(v0[0], v0[1]);
+    *reinterpret_cast<ulonglong2*>(J.inner + ((size_t)ext + j) * N + n) = make_ulonglong2(v1[0], v1[1]);
   }
 }
 
