@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 NQ, NP, DNUM = 6, 3, 2
 
 
-@pytest.mark.parametrize("logN", [12, 13, 14, 15, 16])
+@pytest.mark.parametrize("logN", [10, 11, 12, 13, 14, 15, 16])
 def test_fused_rescale_every_variant(engine_lib, logN):
     import fideslib_gb300 as F
     N = 1 << logN
