@@ -18,8 +18,11 @@
 // Butterflies are Harvey-lazy with a cheaper quotient estimate (shoup_lazy4, products in [0, 4p)): forward
 // values live in [0, 16p) (the compare-and-subtract on every other stage), inverse in [0, 4p); outputs are reduced
 // to [0, p).  Needs p < 2^60.  Shared memory is
-// XOR-swizzled (word l stored at l ^ ((l >> 5) & 15)) so every pass reads and writes with at most the
-// two-wavefront minimum of 64-bit accesses.
+// XOR-swizzled on bits 1..3 (word l stored at l ^ (((l >> 4) & 7) << 1)): the passes that hold 16 residues at a
+// stride (X, A, B) access 64-bit words of distinct banks in every half-warp, and the last pass, whose thread holds
+// 16 contiguous residues, moves them as eight 16-byte pairs (the swizzle keeps pairs adjacent and aligned) with
+// distinct banks in every quarter-warp.  Against a swizzle on bits 0..3 with 64-bit accesses in the last pass this
+// took the 640-limb forward from 0.457 to 0.445 ms and the inverse from 0.543 to 0.534 ms.
 #include <cooperative_groups.h>
 
 #include <atomic>
@@ -34,7 +37,7 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ int swz(int l) { return l ^ ((l >> 5) & 15); }
+__device__ __forceinline__ int swz(int l) { return l ^ (((l >> 4) & 7) << 1); }
 
 // Distributed shared memory through 32-bit shared::cluster addresses: element `local` of this CTA's shared memory as
 // it appears in the cluster window at CTA `rank` (one register per address instead of a 64-bit generic pointer, which
@@ -292,7 +295,11 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
   for (int g = tid; g < S::E / 16; g += kThreads) {  // pass C
     u64 x[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
+    for (int k = 0; k < 16; k += 2) {
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(sm + swz(g * 16 + k));
+      x[k] = v.x;
+      x[k + 1] = v.y;
+    }
     fwd_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p4);
     if constexpr (EPI) {
       epi_store16<LOGN>(e, L, h * S::E + g * 16, x, p);
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
     }
     inv_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p4);
 #pragma unroll
-    for (int k = 0; k < 16; k++) sm[swz(g * 16 + k)] = x[k];
+    for (int k = 0; k < 16; k += 2) *reinterpret_cast<ulonglong2*>(sm + swz(g * 16 + k)) = make_ulonglong2(x[k], x[k + 1]);
   }
   __syncthreads();
 
@@ -510,7 +517,11 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
   for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass C
     u64 x[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) x[k] = sm[swz(g * 16 + k)];
+    for (int k = 0; k < 16; k += 2) {
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(sm + swz(g * 16 + k));
+      x[k] = v.x;
+      x[k + 1] = v.y;
+    }
     fwd_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p4);
     if constexpr (EPI) {
       epi_store16<LOGN>(e, L, h * S::E + g * 16, x, p);
@@ -568,7 +579,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
     }
     inv_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p4);
 #pragma unroll
-    for (int k = 0; k < 16; k++) sm[swz(g * 16 + k)] = x[k];
+    for (int k = 0; k < 16; k += 2) *reinterpret_cast<ulonglong2*>(sm + swz(g * 16 + k)) = make_ulonglong2(x[k], x[k + 1]);
   }
   __syncthreads();
 #pragma unroll 1
