@@ -47,6 +47,34 @@ __device__ __forceinline__ void acc4_mac(Acc4& A, uint32_t yl, uint32_t yh, uint
   mac64(A.a3, yh, ch);
 }
 
+// Three-product (Karatsuba) form of the same sum: y*c = yl*cl + (ys*cs - yl*cl - yh*ch) * 2^30 + yh*ch * 2^60 with
+// ys = yl + yh and cs = cl + ch (31 bits each).  am accumulates ys*cs modulo 2^64; the middle sum it stands for,
+// sum (yl*ch + yh*cl), is below 2^64 while an accumulator holds at most kAcc3Terms terms (16 cross products
+// < 2^60), so am - a0 - a3 taken modulo 2^64 is exact.  One multiply-add pair fewer per term than Acc4 (three
+// instead of four 32x32 products, whose high halves issue at half rate), for two more additions per term.
+constexpr int kAcc3Terms = 8;
+struct Acc3 {
+  u64 a0, am, a3;  // lo*lo, (lo+hi)*(lo+hi) mod 2^64, hi*hi
+};
+__device__ __forceinline__ void acc3_mac(Acc3& A, uint32_t yl, uint32_t yh, uint32_t ys, uint32_t cl, uint32_t ch) {
+  mac64(A.a0, yl, cl);
+  mac64(A.am, ys, cl + ch);
+  mac64(A.a3, yh, ch);
+}
+// (hi, lo) += a0 + (am - a0 - a3) * 2^30 + a3 * 2^60
+__device__ __forceinline__ void acc3_fold(const Acc3& A, u64& hi, u64& lo) {
+  const u64 m = A.am - A.a0 - A.a3;
+  u64 l = lo + A.a0;
+  hi += (l < lo);
+  lo = l;
+  l = lo + (m << 30);
+  hi += (m >> 34) + (l < lo);
+  lo = l;
+  l = lo + (A.a3 << 60);
+  hi += (A.a3 >> 4) + (l < lo);
+  lo = l;
+}
+
 // (hi, lo) += a0 + (a1 + a2) * 2^30 + a3 * 2^60
 __device__ __forceinline__ void acc4_fold(const Acc4& A, u64& hi, u64& lo) {
   const u64 m = A.a1 + A.a2;
@@ -198,9 +226,9 @@ __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ 
 // rows are ordered (tower row, job) over the whole batch instead, (tmax + np) * njobs rows, so that both the digits
 // and the keys of a row are read about once.  A block whose tower lies above its job's level exits.  Every digit's
 // value and both key halves are loaded before any arithmetic; digits are split into 30-bit halves here and key
-// values come split (launch_key_split), accumulated in one Acc4 per half-key (at most 8 digits, 16 terms max); MAXB
-// bounds beta at compile time.  Outputs are left in [0, 4p): the ModDown INTT takes them as they are and both
-// epilogues reduce.
+// values come split (launch_key_split), accumulated in one accumulator per half-key (Acc3 for four or more
+// digits, Acc4 below: at most 8 terms); MAXB bounds beta at compile time.  Outputs are left in [0, 4p): the
+// ModDown INTT takes them as they are and both epilogues reduce.
 template <int MAXB>
 __global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
     ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c, const PrimeConst* __restrict__ pc,
@@ -233,6 +261,12 @@ __global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
   // then has no register spills (68 bytes of spill stores with the pointers held).  The other instances spill less
   // with the pointers worked out once, so they keep that form (ptxas -v).
   constexpr bool kRowIndex = MAXB == 3;
+  // Four or more digits (the bootstrap's dnum 5, whose inner products are bound by their multiply-add stream)
+  // accumulate in the three-product form.  Three digits (dnum 3, three CTAs per SM at 80 registers) keep the
+  // four-product form: there the three-product form's extra live sums spill (68 bytes, ptxas -v), and with fewer
+  // digits the inner product is bound by its key reads; one or two digits keep it too.
+  constexpr bool kKaratsuba = MAXB >= 4;
+  static_assert(MAXB <= kAcc3Terms, "one accumulator chunk per half-key");
   const u64* src[MAXB];
   int srow[MAXB];
 #pragma unroll
@@ -266,18 +300,32 @@ __global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
     u64 v0[2], v1[2];
 #pragma unroll
     for (int e = 0; e < 2; e++) {
-      Acc4 A0{0, 0, 0, 0}, A1{0, 0, 0, 0};
-#pragma unroll
-      for (int d = 0; d < MAXB; d++) {
-        if (d >= beta) break;
-        const u64 Dv = e ? D[d].y : D[d].x, ka = e ? KA[d].y : KA[d].x, kb = e ? KB[d].y : KB[d].x;
-        const uint32_t dl = (uint32_t)(Dv & kMask30), dh = (uint32_t)(Dv >> 30);
-        acc4_mac(A0, dl, dh, (uint32_t)kb, (uint32_t)(kb >> 32));
-        acc4_mac(A1, dl, dh, (uint32_t)ka, (uint32_t)(ka >> 32));
-      }
       u64 h0 = 0, l0 = 0, h1 = 0, l1 = 0;
-      acc4_fold(A0, h0, l0);
-      acc4_fold(A1, h1, l1);
+      if constexpr (kKaratsuba) {
+        Acc3 A0{0, 0, 0}, A1{0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < MAXB; d++) {
+          if (d >= beta) break;
+          const u64 Dv = e ? D[d].y : D[d].x, ka = e ? KA[d].y : KA[d].x, kb = e ? KB[d].y : KB[d].x;
+          const uint32_t dl = (uint32_t)(Dv & kMask30), dh = (uint32_t)(Dv >> 30);
+          acc3_mac(A0, dl, dh, dl + dh, (uint32_t)kb, (uint32_t)(kb >> 32));
+          acc3_mac(A1, dl, dh, dl + dh, (uint32_t)ka, (uint32_t)(ka >> 32));
+        }
+        acc3_fold(A0, h0, l0);
+        acc3_fold(A1, h1, l1);
+      } else {
+        Acc4 A0{0, 0, 0, 0}, A1{0, 0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < MAXB; d++) {
+          if (d >= beta) break;
+          const u64 Dv = e ? D[d].y : D[d].x, ka = e ? KA[d].y : KA[d].x, kb = e ? KB[d].y : KB[d].x;
+          const uint32_t dl = (uint32_t)(Dv & kMask30), dh = (uint32_t)(Dv >> 30);
+          acc4_mac(A0, dl, dh, (uint32_t)kb, (uint32_t)(kb >> 32));
+          acc4_mac(A1, dl, dh, (uint32_t)ka, (uint32_t)(ka >> 32));
+        }
+        acc4_fold(A0, h0, l0);
+        acc4_fold(A1, h1, l1);
+      }
       v0[e] = csub(reduce128_lazy8(h0, l0, P), p4);
       v1[e] = csub(reduce128_lazy8(h1, l1, P), p4);
     }
