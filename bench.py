@@ -298,8 +298,9 @@ def run_ours(args, rank, world, dist):
     for _ in range(3):
         e2e_step()
     torch.cuda.synchronize()
-    # at least 20 host-to-host steps (0.2 s): a single step delayed by the shared host weighs less on the mean
-    e2e_steps = max(20, args.steps)
+    # at least 50 host-to-host steps (0.5 s): a single step delayed by the shared host (steps of 45-80 ms against
+    # a median of 10 ms were seen on some boxes) weighs less on the mean
+    e2e_steps = max(50, args.steps)
     e2e_each = []  # each call returns with its results in host memory (it synchronises its streams)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):

@@ -78,6 +78,13 @@ int check_loaded(fgb::Context* c, const fgb::u64* x, long long rows, int period,
 namespace fgb {
 // Lets other translation units of the library report through fides_last_error().
 int set_last_error(int code, const char* msg) { return fail(code, msg); }
+// For the request server: makes `s` the stream that later calls on ctx order their work on and returns the
+// previous one, without synchronising it (fides_ctx_set_stream does); the caller orders the two streams itself.
+cudaStream_t swap_ctx_stream(fides_ctx* ctx, cudaStream_t s) {
+  cudaStream_t old = ctx->c->stream;
+  ctx->c->stream = s;
+  return old;
+}
 }  // namespace fgb
 
 extern "C" {

@@ -6,9 +6,11 @@
 // context.  Whenever the GPU can take more work, the worker admits, in arrival order and whatever their ring,
 // every pending request that fits the one memory budget (output ciphertext + key-switch workspace, counted per
 // request with its ring's shape) up to max_batch, runs each ring's share through fides_eval_batch on that
-// ring's stream (one launch per pipeline stage for all of them, at their own levels; the rings' batches overlap
-// on the device), and keeps up to max_inflight batches queued, so requests that arrive while a batch runs are
-// admitted into the next one as soon as slots and memory free up.  Bootstrap requests (FIDES_OP_BOOTSTRAP, with the plan set
+// ring (one launch per pipeline stage for all of them, at their own levels; the rings' batches overlap on the
+// device), and keeps up to max_inflight batches in flight, each on a stream of its own (a lane), so requests that
+// arrive while a batch runs are admitted into the next one as soon as a lane and memory free up and run beside
+// it on the GPU instead of queueing behind it.  A released result is freed once every batch that was in flight at
+// its release has completed (a batch may still read it), and completed batches retire in any order.  Bootstrap requests (FIDES_OP_BOOTSTRAP, with the plan set
 // by fides_server_set_bootstrap_plan) admitted together run as one fides_eval_bootstrap_batch.  Each request's
 // latency is stamped on the host from submit to the completion of its batch's CUDA event.
 #include <cuda_runtime.h>
@@ -27,6 +29,7 @@
 
 namespace fgb {
 int set_last_error(int code, const char* msg);
+cudaStream_t swap_ctx_stream(fides_ctx* ctx, cudaStream_t s);
 }
 
 namespace {
@@ -49,11 +52,19 @@ struct InFlight {
   std::vector<cudaEvent_t> evs;  // one per ring that took part
   std::vector<uint64_t> tickets;
   size_t footprint;
+  uint64_t id;  // launch order
+  uint32_t lane;
 };
 
 struct Ring {
   fides_ctx* ctx = nullptr;
   uint32_t N = 0, np = 0, nq = 0, alpha = 1;
+  std::vector<cudaStream_t> lanes;  // one stream per in-flight batch (made by the worker)
+};
+
+struct DeferredFree {
+  uint32_t ring, handle;
+  uint64_t after;  // freed once every batch with an id up to this one has completed
 };
 
 }  // namespace
@@ -97,15 +108,42 @@ struct fides_server {
   // Worker loop: admit -> launch (up to max_inflight batches queued) -> retire completed batches.
   void run() {
     cudaSetDevice(device);  // a new thread starts on device 0; the contexts live on the creator's device
+    // Batches run on the server's own lanes.  Work the caller queued on a context before the server started
+    // (loads of resident ciphertexts and keys) completes first; while the server runs, its worker is the only
+    // thread that touches the contexts.
+    for (Ring& g : rings) {
+      cudaStreamSynchronize((cudaStream_t)fides_ctx_stream(g.ctx));
+      g.lanes.assign(cfg.max_inflight_batches, nullptr);
+      for (auto& l : g.lanes) cudaStreamCreateWithFlags(&l, cudaStreamNonBlocking);
+    }
     std::deque<InFlight> inflight;
+    std::vector<DeferredFree> deferred;
+    uint64_t launched = 0;
     size_t inflight_bytes = 0;
+    // A result is freed (stream-ordered on its context's own stream, which carries no batches) once no batch that
+    // could read it is still in flight.
+    auto flush_frees = [&] {
+      uint64_t oldest = UINT64_MAX;
+      for (const InFlight& f : inflight) oldest = std::min(oldest, f.id);
+      size_t k = 0;
+      for (const DeferredFree& d : deferred) {
+        if (d.after < oldest)
+          fides_ct_free(rings[d.ring].ctx, d.handle);
+        else
+          deferred[k++] = d;
+      }
+      deferred.resize(k);
+    };
     for (;;) {
       std::vector<uint64_t> take;
       std::vector<std::pair<uint32_t, uint32_t>> frees;
       bool idle_wait = false;
       {
         std::unique_lock<std::mutex> lk(mu);
-        if (stop && pending.empty() && inflight.empty() && to_free.empty()) break;
+        if (stop && pending.empty() && inflight.empty() && to_free.empty()) {
+          for (const DeferredFree& d : deferred) fides_ct_free(rings[d.ring].ctx, d.handle);
+          break;
+        }
         frees.swap(to_free);
         if (!pending.empty() && inflight.size() < cfg.max_inflight_batches) {
           size_t budget = inflight_bytes;
@@ -124,7 +162,8 @@ struct fides_server {
         if (idle_wait) cv_work.wait(lk, [&] { return stop || !pending.empty() || !to_free.empty(); });
       }
       if (idle_wait) continue;
-      for (auto& fr : frees) fides_ct_free(rings[fr.first].ctx, fr.second);
+      for (auto& fr : frees) deferred.push_back(DeferredFree{fr.first, fr.second, launched});
+      flush_frees();
       if (!take.empty()) {
         std::vector<fides_op> ops(take.size());
         std::vector<uint32_t> ring_of(take.size());
@@ -139,6 +178,12 @@ struct fides_server {
         }
         std::vector<int> rcs(ops.size(), FIDES_OK);
         InFlight f;
+        f.id = ++launched;
+        f.lane = 0;  // the first lane no batch in flight uses (one exists: fewer than max_inflight are in flight)
+        for (bool used = true; used; f.lane += used ? 1 : 0) {
+          used = false;
+          for (const InFlight& o : inflight) used = used || o.lane == f.lane;
+        }
         for (uint32_t g = 0; g < rings.size(); g++) {
           fides_ctx* ctx = rings[g].ctx;
           // this ring's bootstrap requests go through fides_eval_bootstrap_batch (all of them in flight
@@ -147,6 +192,8 @@ struct fides_server {
           for (size_t i = 0; i < ops.size(); i++)
             if (ring_of[i] == g) (ops[i].op == FIDES_OP_BOOTSTRAP ? bi : oi).push_back(i);
           if (bi.empty() && oi.empty()) continue;
+          cudaStream_t const lane = rings[g].lanes[f.lane];
+          cudaStream_t const home = fgb::swap_ctx_stream(ctx, lane);  // every call below orders its work on the lane
           if (!oi.empty()) {
             std::vector<fides_op> sub(oi.size());
             for (size_t k = 0; k < oi.size(); k++) sub[k] = ops[oi[k]];
@@ -175,8 +222,9 @@ struct fides_server {
           }
           cudaEvent_t ev;
           cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-          cudaEventRecord(ev, (cudaStream_t)fides_ctx_stream(ctx));
+          cudaEventRecord(ev, lane);
           f.evs.push_back(ev);
+          fgb::swap_ctx_stream(ctx, home);
         }
         f.tickets = take;
         f.footprint = bytes;
@@ -195,27 +243,34 @@ struct fides_server {
         continue;
       }
       if (inflight.empty()) continue;
-      // Retire the oldest batch.  While it runs, keep admitting new arrivals if a slot is free.
+      // Retire a completed batch (the lanes run concurrently, so any of them may finish first).  While all run,
+      // keep admitting new arrivals if a lane is free; with every lane busy, wait for the oldest batch.
       bool full;
       {
         std::lock_guard<std::mutex> lk(mu);
         full = inflight.size() >= cfg.max_inflight_batches || stop;
       }
-      bool busy = false;
-      for (cudaEvent_t ev : inflight.front().evs) busy = busy || cudaEventQuery(ev) == cudaErrorNotReady;
-      if (!full && busy) {
+      size_t done = inflight.size();
+      for (size_t i = 0; i < inflight.size() && done == inflight.size(); i++) {
+        bool busy = false;
+        for (cudaEvent_t ev : inflight[i].evs) busy = busy || cudaEventQuery(ev) == cudaErrorNotReady;
+        if (!busy) done = i;
+      }
+      if (done == inflight.size() && !full) {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait_for(lk, std::chrono::microseconds(20), [&] { return !pending.empty() || !to_free.empty(); });
         continue;
       }
-      InFlight f = inflight.front();
-      inflight.pop_front();
+      if (done == inflight.size()) done = 0;
+      InFlight f = inflight[done];
+      inflight.erase(inflight.begin() + (long)done);
       for (cudaEvent_t ev : f.evs) {
         cudaEventSynchronize(ev);
         cudaEventDestroy(ev);
       }
       const double t = now_ms();
       inflight_bytes -= f.footprint;
+      flush_frees();  // results released while this batch ran may be free now
       std::lock_guard<std::mutex> lk(mu);
       for (uint64_t tk : f.tickets) {
         Req& r = reqs[tk];
@@ -226,6 +281,9 @@ struct fides_server {
       last_done = t;
       cv_done.notify_all();
     }
+    for (Ring& g : rings)
+      for (cudaStream_t l : g.lanes)
+        if (l) cudaStreamDestroy(l);
   }
 };
 
