@@ -465,7 +465,72 @@ struct Shape16 {
   static constexpr int COLS = 4096 / C;                    // phase-X columns per CTA
   static constexpr int GX = COLS / kThreads16;             // phase-X groups per thread
   static constexpr int GROUPS = E / 16;                    // 16-residue groups per pass
+  static constexpr int NA = E / 4096;                      // pass-A groups (G values) per CTA
+  static constexpr int NB = E / 256;                       // pass-B groups per CTA
+  static constexpr int TWS = 15 * (NA + NB);               // twiddles of passes A and B staged in shared memory
+  static constexpr size_t SMEM = sizeof(u64) * E + sizeof(ulonglong2) * TWS;
 };
+
+// Twiddles of the middle passes in shared memory.  A CTA's pass A (LOGS = 8) and pass B (LOGS = 4) use the
+// groups G0 + gl, gl < n (n = NA or NB, G0 = h * n), whose stage-kb twiddles are the contiguous table entries
+// 2^s + G0 * 2^(3-kb) + [0, n * 2^(3-kb)).  They are copied once per CTA (cp.async, 16 bytes each, during phase X or
+// pass C^-1) into blocks: pass A's four stage blocks (kb = 3 .. 0, n * 2^(3-kb) entries each) then pass B's, so
+// stage kb's block starts at n * (2^(3-kb) - 1) within its pass and entry gl * 2^(3-kb) + j is twiddle j of group
+// gl.  Without the copy these loads went to L2 whenever the last pass's streaming twiddles had evicted them from
+// L1.
+template <int LOGN, int LOGE>
+__device__ __forceinline__ void stage_mid_twiddles(ulonglong2* tws, const ulonglong2* __restrict__ tw, int h) {
+  using S = Shape16<LOGN, LOGE>;
+  for (int e = threadIdx.x; e < S::TWS; e += kThreads16) {
+    const bool passA = e < 15 * S::NA;
+    const int n = passA ? S::NA : S::NB, logs = passA ? 8 : 4;
+    int local = passA ? e : e - 15 * S::NA, kb = 3;
+    while (local >= (n << (3 - kb))) {
+      local -= n << (3 - kb);
+      kb--;
+    }
+    const int st = LOGN - 1 - (logs + kb);
+    const ulonglong2* src = tw + (1 << st) + (h * n << (3 - kb)) + local;
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(tws + e);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void wait_staged() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// fwd_radix / inv_radix for a radix-16 pass whose twiddles are staged (stage_mid_twiddles): tws is the pass's
+// first block, n its group count, gl the local group.
+template <int LOGS, int LOGN>
+__device__ __forceinline__ void fwd_radix16_staged(u64 (&x)[16], int gl, const ulonglong2* tws, int n, u64 negp,
+                                                   u64 p4) {
+#pragma unroll
+  for (int kb = 3; kb >= 0; kb--) {
+    const int s = LOGN - 1 - (LOGS + kb);
+    const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      if (k & (1 << kb)) continue;
+      const ulonglong2 w = blk[k >> (kb + 1)];
+      if ((s & 1) == 0)
+        ct_bfly<true>(x[k], x[k + (1 << kb)], w, negp, p4);
+      else
+        ct_bfly<false>(x[k], x[k + (1 << kb)], w, negp, p4);
+    }
+  }
+}
+template <int LOGS, int LOGN>
+__device__ __forceinline__ void inv_radix16_staged(u64 (&x)[16], int gl, const ulonglong2* tws, int n, u64 negp,
+                                                   u64 p4) {
+#pragma unroll
+  for (int kb = 0; kb < 4; kb++) {
+    const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      if (k & (1 << kb)) continue;
+      gs_bfly(x[k], x[k + (1 << kb)], blk[k >> (kb + 1)], negp, p4);
+    }
+  }
+}
 
 // EPI: the fused rescale of NttEpi (null for the plain transform).
 template <int LOGN, int LOGE, bool EPI>
@@ -482,6 +547,8 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
     asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
     h = (int)cg::this_cluster().block_rank();
   }
+  ulonglong2* const tws = reinterpret_cast<ulonglong2*>(sm + S::E);
+  stage_mid_twiddles<LOGN, LOGE>(tws, tw, h);
   const u64* src = L.src;
   SwitchIn sw;
   if constexpr (EPI) sw = switch_in(b, T, e, L, src);
@@ -508,6 +575,7 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
         for (int k = 0; k < R; k++) sm[swz(k * 4096 + col)] = x[k];
       }
     }
+    wait_staged();
     if constexpr (S::C > 1)
       cg::this_cluster().sync();
     else
@@ -519,7 +587,7 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(hi * 4096 + k * 256 + low)];
-    fwd_radix<4, 8, LOGN>(x, h * (S::E / 4096) + hi, tw, negp, p4);
+    fwd_radix16_staged<8, LOGN>(x, hi, tws, S::NA, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(hi * 4096 + k * 256 + low)] = x[k];
   }
@@ -530,7 +598,7 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    fwd_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
+    fwd_radix16_staged<4, LOGN>(x, high, tws + 15 * S::NA, S::NB, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -589,6 +657,8 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
   const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
+  ulonglong2* const tws = reinterpret_cast<ulonglong2*>(sm + S::E);
+  stage_mid_twiddles<LOGN, LOGE>(tws, tw, h);
 #pragma unroll 1
   for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass C^-1
     u64 x[16];
@@ -603,6 +673,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
 #pragma unroll
     for (int k = 0; k < 16; k += 2) *reinterpret_cast<ulonglong2*>(sm + swz(g * 16 + k)) = make_ulonglong2(x[k], x[k + 1]);
   }
+  wait_staged();
   __syncthreads();
 #pragma unroll 1
   for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass B^-1
@@ -610,7 +681,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    inv_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
+    inv_radix16_staged<4, LOGN>(x, high, tws + 15 * S::NA, S::NB, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -621,7 +692,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(hi * 4096 + k * 256 + low)];
-    inv_radix<4, 8, LOGN>(x, h * (S::E / 4096) + hi, tw, negp, p4);
+    inv_radix16_staged<8, LOGN>(x, hi, tws, S::NA, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(hi * 4096 + k * 256 + low)] = x[k];
   }
@@ -657,7 +728,7 @@ cudaError_t launch16(const NttBatch& b, const DeviceTables& t, bool inverse, cud
   using S = Shape16<LOGN, LOGE>;
   auto kern = inverse ? ntt16_inv_kernel<LOGN, LOGE> : ntt16_fwd_kernel<LOGN, LOGE>;
   static std::atomic<unsigned long long> attr_done[2];
-  const size_t smem = sizeof(u64) * S::E;
+  const size_t smem = S::SMEM;
   const cudaError_t ea = once_per_device(attr_done[inverse], [&] {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess && S::C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -687,7 +758,7 @@ cudaError_t launch16_epi(const NttBatch& b, const NttEpi& e, const DeviceTables&
   using S = Shape16<LOGN, LOGE>;
   auto kern = ntt16_fwd_epi_kernel<LOGN, LOGE>;
   static std::atomic<unsigned long long> attr_done;
-  const size_t smem = sizeof(u64) * S::E;
+  const size_t smem = S::SMEM;
   const cudaError_t ea = once_per_device(attr_done, [&] {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess && S::C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
