@@ -197,7 +197,71 @@ struct Shape {
   static constexpr int LOGC = LOGN - LOGE;
   static constexpr int C = 1 << LOGC;
   static constexpr int LOGRA = LOGE - 8;  // pass A radix
+  static constexpr int NB = E / 256;      // pass-B groups per CTA (their twiddles are staged in shared memory)
+  static constexpr size_t SMEM = sizeof(u64) * E + sizeof(ulonglong2) * 15 * NB;
 };
+
+// Twiddles of the middle passes in shared memory (NA = 0 for the radix-32/16 kernels, whose radix-32 pass A has
+// one group per CTA and reads its 31 twiddles through L1).  A CTA's pass A (LOGS = 8) and pass B (LOGS = 4) use the
+// groups G0 + gl, gl < n (n = NA or NB, G0 = h * n), whose stage-kb twiddles are the contiguous table entries
+// 2^s + G0 * 2^(3-kb) + [0, n * 2^(3-kb)).  They are copied once per CTA (cp.async, 16 bytes each, during phase X or
+// pass C^-1) into blocks: pass A's four stage blocks (kb = 3 .. 0, n * 2^(3-kb) entries each) then pass B's, so
+// stage kb's block starts at n * (2^(3-kb) - 1) within its pass and entry gl * 2^(3-kb) + j is twiddle j of group
+// gl.  Without the copy these loads went to L2 whenever the last pass's streaming twiddles had evicted them from
+// L1.
+template <int LOGN, int NA, int NB>
+__device__ __forceinline__ void stage_mid_twiddles(ulonglong2* tws, const ulonglong2* __restrict__ tw, int h) {
+  for (int e = threadIdx.x; e < 15 * (NA + NB); e += (int)blockDim.x) {
+    const bool passA = e < 15 * NA;
+    const int n = passA ? NA : NB, logs = passA ? 8 : 4;
+    int local = passA ? e : e - 15 * NA, kb = 3;
+    while (local >= (n << (3 - kb))) {
+      local -= n << (3 - kb);
+      kb--;
+    }
+    const int st = LOGN - 1 - (logs + kb);
+    const ulonglong2* src = tw + (1 << st) + (h * n << (3 - kb)) + local;
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(tws + e);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void wait_staged() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// fwd_radix / inv_radix for a radix-16 pass whose twiddles are staged (stage_mid_twiddles): tws is the pass's
+// first block, n its group count, gl the local group.
+template <int LOGS, int LOGN>
+__device__ __forceinline__ void fwd_radix16_staged(u64 (&x)[16], int gl, const ulonglong2* tws, int n, u64 negp,
+                                                   u64 p4) {
+#pragma unroll
+  for (int kb = 3; kb >= 0; kb--) {
+    const int s = LOGN - 1 - (LOGS + kb);
+    const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      if (k & (1 << kb)) continue;
+      const ulonglong2 w = blk[k >> (kb + 1)];
+      if ((s & 1) == 0)
+        ct_bfly<true>(x[k], x[k + (1 << kb)], w, negp, p4);
+      else
+        ct_bfly<false>(x[k], x[k + (1 << kb)], w, negp, p4);
+    }
+  }
+}
+template <int LOGS, int LOGN>
+__device__ __forceinline__ void inv_radix16_staged(u64 (&x)[16], int gl, const ulonglong2* tws, int n, u64 negp,
+                                                   u64 p4) {
+#pragma unroll
+  for (int kb = 0; kb < 4; kb++) {
+    const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      if (k & (1 << kb)) continue;
+      gs_bfly(x[k], x[k + (1 << kb)], blk[k >> (kb + 1)], negp, p4);
+    }
+  }
+}
+
 
 // Input side of the fused rescale: the job's one row per poly (coefficients of prime switch_top) switched into
 // this limb's prime on load.
@@ -247,13 +311,16 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
   const u64 p = T.pc[L.prime].p, p2 = 2 * p, p4 = 4 * p, negp = T.pc[L.prime].negp;
   const ulonglong2* __restrict__ tw = T.tw_fwd + (size_t)L.prime * S::N;
   int h = 0;
+  if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
+  ulonglong2* const tws = reinterpret_cast<ulonglong2*>(sm + S::E);
+  stage_mid_twiddles<LOGN, 0, S::NB>(tws, tw, h);
   const u64* src = L.src;
   SwitchIn sw;
   if constexpr (EPI) sw = switch_in(b, T, e, L, src);
 
   if constexpr (S::C > 1) {
     cg::cluster_group cl = cg::this_cluster();
-    const int c = (int)cl.block_rank();
+    const int c = h;
     // "every CTA of the cluster is running" is all the first barrier has to establish (no data is exchanged
     // yet), so it is a relaxed arrive here and a wait just before the distributed-shared-memory stores,
     // overlapping the barrier with the loads and the first butterflies.
@@ -281,7 +348,6 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
       for (int hh = 0; hh < S::C; hh++) st_peer(peer_smem(sm + swz(l), hh), x[it][hh]);
     }
     cl.sync();
-    h = c;
   }
 
   {  // pass A
@@ -299,6 +365,7 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
 #pragma unroll
     for (int k = 0; k < R; k++) sm[swz(k * 256 + tid)] = x[k];
   }
+  wait_staged();
   __syncthreads();
 
 #pragma unroll 1
@@ -307,7 +374,7 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    fwd_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
+    fwd_radix16_staged<4, LOGN>(x, high, tws, S::NB, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -364,6 +431,8 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
   const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
+  ulonglong2* const tws = reinterpret_cast<ulonglong2*>(sm + S::E);
+  stage_mid_twiddles<LOGN, 0, S::NB>(tws, tw, h);
 
 #pragma unroll 1
   for (int g = tid; g < S::E / 16; g += kThreads) {  // pass C^-1
@@ -379,6 +448,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
 #pragma unroll
     for (int k = 0; k < 16; k += 2) *reinterpret_cast<ulonglong2*>(sm + swz(g * 16 + k)) = make_ulonglong2(x[k], x[k + 1]);
   }
+  wait_staged();
   __syncthreads();
 
 #pragma unroll 1
@@ -387,7 +457,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    inv_radix<4, 4, LOGN>(x, h * (S::E / 256) + high, tw, negp, p4);
+    inv_radix16_staged<4, LOGN>(x, high, tws, S::NB, negp, p4);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -471,67 +541,6 @@ struct Shape16 {
   static constexpr size_t SMEM = sizeof(u64) * E + sizeof(ulonglong2) * TWS;
 };
 
-// Twiddles of the middle passes in shared memory.  A CTA's pass A (LOGS = 8) and pass B (LOGS = 4) use the
-// groups G0 + gl, gl < n (n = NA or NB, G0 = h * n), whose stage-kb twiddles are the contiguous table entries
-// 2^s + G0 * 2^(3-kb) + [0, n * 2^(3-kb)).  They are copied once per CTA (cp.async, 16 bytes each, during phase X or
-// pass C^-1) into blocks: pass A's four stage blocks (kb = 3 .. 0, n * 2^(3-kb) entries each) then pass B's, so
-// stage kb's block starts at n * (2^(3-kb) - 1) within its pass and entry gl * 2^(3-kb) + j is twiddle j of group
-// gl.  Without the copy these loads went to L2 whenever the last pass's streaming twiddles had evicted them from
-// L1.
-template <int LOGN, int LOGE>
-__device__ __forceinline__ void stage_mid_twiddles(ulonglong2* tws, const ulonglong2* __restrict__ tw, int h) {
-  using S = Shape16<LOGN, LOGE>;
-  for (int e = threadIdx.x; e < S::TWS; e += kThreads16) {
-    const bool passA = e < 15 * S::NA;
-    const int n = passA ? S::NA : S::NB, logs = passA ? 8 : 4;
-    int local = passA ? e : e - 15 * S::NA, kb = 3;
-    while (local >= (n << (3 - kb))) {
-      local -= n << (3 - kb);
-      kb--;
-    }
-    const int st = LOGN - 1 - (logs + kb);
-    const ulonglong2* src = tw + (1 << st) + (h * n << (3 - kb)) + local;
-    const unsigned dst = (unsigned)__cvta_generic_to_shared(tws + e);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void wait_staged() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// fwd_radix / inv_radix for a radix-16 pass whose twiddles are staged (stage_mid_twiddles): tws is the pass's
-// first block, n its group count, gl the local group.
-template <int LOGS, int LOGN>
-__device__ __forceinline__ void fwd_radix16_staged(u64 (&x)[16], int gl, const ulonglong2* tws, int n, u64 negp,
-                                                   u64 p4) {
-#pragma unroll
-  for (int kb = 3; kb >= 0; kb--) {
-    const int s = LOGN - 1 - (LOGS + kb);
-    const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
-#pragma unroll
-    for (int k = 0; k < 16; k++) {
-      if (k & (1 << kb)) continue;
-      const ulonglong2 w = blk[k >> (kb + 1)];
-      if ((s & 1) == 0)
-        ct_bfly<true>(x[k], x[k + (1 << kb)], w, negp, p4);
-      else
-        ct_bfly<false>(x[k], x[k + (1 << kb)], w, negp, p4);
-    }
-  }
-}
-template <int LOGS, int LOGN>
-__device__ __forceinline__ void inv_radix16_staged(u64 (&x)[16], int gl, const ulonglong2* tws, int n, u64 negp,
-                                                   u64 p4) {
-#pragma unroll
-  for (int kb = 0; kb < 4; kb++) {
-    const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
-#pragma unroll
-    for (int k = 0; k < 16; k++) {
-      if (k & (1 << kb)) continue;
-      gs_bfly(x[k], x[k + (1 << kb)], blk[k >> (kb + 1)], negp, p4);
-    }
-  }
-}
-
 // EPI: the fused rescale of NttEpi (null for the plain transform).
 template <int LOGN, int LOGE, bool EPI>
 __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTables& T, const NttEpi* e) {
@@ -548,7 +557,7 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
     h = (int)cg::this_cluster().block_rank();
   }
   ulonglong2* const tws = reinterpret_cast<ulonglong2*>(sm + S::E);
-  stage_mid_twiddles<LOGN, LOGE>(tws, tw, h);
+  stage_mid_twiddles<LOGN, S::NA, S::NB>(tws, tw, h);
   const u64* src = L.src;
   SwitchIn sw;
   if constexpr (EPI) sw = switch_in(b, T, e, L, src);
@@ -658,7 +667,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
   ulonglong2* const tws = reinterpret_cast<ulonglong2*>(sm + S::E);
-  stage_mid_twiddles<LOGN, LOGE>(tws, tw, h);
+  stage_mid_twiddles<LOGN, S::NA, S::NB>(tws, tw, h);
 #pragma unroll 1
   for (int g = tid; g < S::GROUPS; g += kThreads16) {  // pass C^-1
     u64 x[16];
@@ -788,7 +797,7 @@ cudaError_t launch_t_epi(const NttBatch& b, const NttEpi& e, const DeviceTables&
   using S = Shape<LOGN>;
   auto kern = ntt_fwd_epi_kernel<LOGN>;
   static std::atomic<unsigned long long> attr_done;
-  const size_t smem = sizeof(u64) * S::E;
+  const size_t smem = S::SMEM;
   const cudaError_t ea = once_per_device(attr_done, [&] {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
@@ -816,7 +825,7 @@ cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cud
   using S = Shape<LOGN>;
   auto kern = inverse ? ntt_inv_kernel<LOGN> : ntt_fwd_kernel<LOGN>;
   static std::atomic<unsigned long long> attr_done[2];
-  const size_t smem = sizeof(u64) * S::E;
+  const size_t smem = S::SMEM;
   const cudaError_t ea = once_per_device(attr_done[inverse], [&] {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
