@@ -9,8 +9,9 @@
 // ring (one launch per pipeline stage for all of them, at their own levels; the rings' batches overlap on the
 // device), and keeps up to max_inflight batches in flight, each on a stream of its own (a lane), so requests that
 // arrive while a batch runs are admitted into the next one as soon as a lane and memory free up and run beside
-// it on the GPU instead of queueing behind it.  A released result is freed once every batch that was in flight at
-// its release has completed (a batch may still read it), and completed batches retire in any order.  Bootstrap requests (FIDES_OP_BOOTSTRAP, with the plan set
+// it on the GPU instead of queueing behind it.  A released result is freed once no pending request and no batch in
+// flight reads it (a client may release a result right after submitting requests that take it as an operand), and
+// completed batches retire in any order.  Bootstrap requests (FIDES_OP_BOOTSTRAP, with the plan set
 // by fides_server_set_bootstrap_plan) admitted together run as one fides_eval_bootstrap_batch.  Each request's
 // latency is stamped on the host from submit to the completion of its batch's CUDA event.
 #include <cuda_runtime.h>
@@ -51,8 +52,8 @@ struct Req {
 struct InFlight {
   std::vector<cudaEvent_t> evs;  // one per ring that took part
   std::vector<uint64_t> tickets;
+  std::vector<std::pair<uint32_t, uint32_t>> reads;  // (ring, handle) operands of its requests
   size_t footprint;
-  uint64_t id;  // launch order
   uint32_t lane;
 };
 
@@ -64,7 +65,6 @@ struct Ring {
 
 struct DeferredFree {
   uint32_t ring, handle;
-  uint64_t after;  // freed once every batch with an id up to this one has completed
 };
 
 }  // namespace
@@ -118,19 +118,28 @@ struct fides_server {
     }
     std::deque<InFlight> inflight;
     std::vector<DeferredFree> deferred;
-    uint64_t launched = 0;
     size_t inflight_bytes = 0;
-    // A result is freed (stream-ordered on its context's own stream, which carries no batches) once no batch that
-    // could read it is still in flight.
+    // A released result is freed (stream-ordered on its context's own stream, which carries no batches) once no
+    // pending request and no batch in flight reads it; until then it stays on the deferred list.
     auto flush_frees = [&] {
-      uint64_t oldest = UINT64_MAX;
-      for (const InFlight& f : inflight) oldest = std::min(oldest, f.id);
+      if (deferred.empty()) return;
+      std::vector<std::pair<uint32_t, uint32_t>> busy;
+      for (const InFlight& f : inflight) busy.insert(busy.end(), f.reads.begin(), f.reads.end());
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        for (uint64_t tk : pending) {
+          const Req& r = reqs[tk];
+          busy.push_back({r.ring, r.op.a});
+          busy.push_back({r.ring, r.op.b});
+        }
+      }
+      std::sort(busy.begin(), busy.end());
       size_t k = 0;
       for (const DeferredFree& d : deferred) {
-        if (d.after < oldest)
-          fides_ct_free(rings[d.ring].ctx, d.handle);
-        else
+        if (std::binary_search(busy.begin(), busy.end(), std::make_pair(d.ring, d.handle)))
           deferred[k++] = d;
+        else
+          fides_ct_free(rings[d.ring].ctx, d.handle);
       }
       deferred.resize(k);
     };
@@ -162,8 +171,7 @@ struct fides_server {
         if (idle_wait) cv_work.wait(lk, [&] { return stop || !pending.empty() || !to_free.empty(); });
       }
       if (idle_wait) continue;
-      for (auto& fr : frees) deferred.push_back(DeferredFree{fr.first, fr.second, launched});
-      flush_frees();
+      for (auto& fr : frees) deferred.push_back(DeferredFree{fr.first, fr.second});
       if (!take.empty()) {
         std::vector<fides_op> ops(take.size());
         std::vector<uint32_t> ring_of(take.size());
@@ -178,7 +186,10 @@ struct fides_server {
         }
         std::vector<int> rcs(ops.size(), FIDES_OK);
         InFlight f;
-        f.id = ++launched;
+        for (size_t i = 0; i < ops.size(); i++) {
+          f.reads.push_back({ring_of[i], ops[i].a});
+          f.reads.push_back({ring_of[i], ops[i].b});
+        }
         f.lane = 0;  // the first lane no batch in flight uses (one exists: fewer than max_inflight are in flight)
         for (bool used = true; used; f.lane += used ? 1 : 0) {
           used = false;
@@ -240,8 +251,10 @@ struct fides_server {
         }
         inflight_bytes += bytes;
         inflight.push_back(f);
+        flush_frees();
         continue;
       }
+      flush_frees();
       if (inflight.empty()) continue;
       // Retire a completed batch (the lanes run concurrently, so any of them may finish first).  While all run,
       // keep admitting new arrivals if a lane is free; with every lane busy, wait for the oldest batch.

@@ -456,8 +456,10 @@ int fides_key_load_file(fides_ctx* ctx, const char* path);
  * per call).  One worker thread owns the context: while a server runs, use the context only through it.
  * Clients on any thread submit independent requests (operands must be resident ciphertext handles); the worker
  * admits every pending request that fits `mem_budget_bytes` (output + key-switch workspace per request) up to
- * `max_batch`, runs them with fides_eval_batch, and keeps up to `max_inflight_batches` batches queued on the GPU,
- * so arrivals during a batch join the next one.  Latency = submit to completion of the request's batch. */
+ * `max_batch`, runs them with fides_eval_batch, and keeps up to `max_inflight_batches` batches in flight, each on a
+ * stream of its own, so arrivals during a batch join the next one, which runs beside it on the GPU.  Work queued
+ * on the context before the server starts completes first.  Latency = submit to completion of the request's
+ * batch. */
 typedef struct fides_server fides_server;
 typedef struct {
   uint32_t max_batch;
@@ -484,7 +486,9 @@ int fides_server_submit(fides_server* s, const fides_op* op, uint64_t* ticket);
 int fides_server_submit_to(fides_server* s, uint32_t ring, const fides_op* op, uint64_t* ticket);
 /* Blocks until the request finished; returns its status and result handle. */
 int fides_server_wait(fides_server* s, uint64_t ticket, uint32_t* out, double* latency_ms);
-/* Frees the request's result ciphertext (done by the worker) and forgets the ticket. */
+/* Frees the request's result ciphertext and forgets the ticket.  The worker frees it once no pending request and
+ * no batch in flight reads it, so a result may be released right after submitting requests that take it as an
+ * operand. */
 int fides_server_release(fides_server* s, uint64_t ticket);
 int fides_server_stats_get(fides_server* s, fides_server_stats* st);
 int fides_server_reset_stats(fides_server* s);
