@@ -344,8 +344,10 @@ __global__ void __launch_bounds__(kT) key_split_kernel(u64* __restrict__ k, size
 
 // ModDown basis conversion P -> Q_t: grid (N/512 (N/256 for more than 16 special primes), polys per job), two
 // adjacent coefficients per thread (one above 16 special primes); reads the (coefficient-form) P rows of inner.
+// Up to 11 special primes the instance is held to 80 registers, three CTAs per SM (ten primes: 90 -> 80 registers
+// with 4 bytes of spills; the 64-rotation step 7,670 -> 7,687 ops/s).
 template <int K>
-__global__ void __launch_bounds__(kT) moddown_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
+__global__ void __launch_bounds__(kT, K <= 11 ? 3 : 1) moddown_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                           const PrimeConst* __restrict__ pc) {
   extern __shared__ uint2 cs[];  // [K][t]
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
