@@ -402,6 +402,7 @@ def run_ours(args, rank, world, dist):
         "hmult_cfg1": cfg1,
         "ntt_cfg2": ntt["summary"],
         "ntt_autotune_n16": ctx.ntt_tuning(),
+        "ks_inner_autotune_n16": ctx.ks_tuning(),
         "pipes": dict(pipes, ntt_fwd_butterflies_per_clk_sm=round(
             NTT_BUTTERFLIES_CFG2 / (ntt["summary"]["ms_ntt"] * 1e-3) / pipes["sms"] / (pipes["clock_mhz"] * 1e6), 3)),
         "roofline": dict(ntt["roofline"], step={

@@ -136,6 +136,8 @@ _SIGS = {
     "fides_lt_free": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fides_ctx_ntt_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fides_ctx_ntt_tuning_set": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "fides_ctx_ks_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "fides_ctx_ks_tuning_set": (C.c_int, [C.c_void_p, C.c_int32]),
     "fides_ctx_set_mem_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fides_ctx_mem_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "fides_ctx_set_input_check": (C.c_int, [C.c_void_p, C.c_int]),
@@ -585,6 +587,16 @@ class CryptoContext:
 
     def set_ntt_variant(self, fwd_variant: int, inv_variant: int = 0):
         _check(lib().fides_ctx_ntt_tuning_set(self._h, fwd_variant, inv_variant))
+
+    def ks_tuning(self) -> dict:
+        """The key inner product's tile the autotuner chose (coefficient pairs per thread) and its timings."""
+        it = C.c_int32()
+        ms = (C.c_float * 4)()
+        _check(lib().fides_ctx_ks_tuning(self._h, C.byref(it), ms))
+        return {"pairs_per_thread": it.value, "ms_1_2_4_8": [round(ms[i], 4) for i in range(4)]}
+
+    def set_ks_tile(self, pairs_per_thread: int):
+        _check(lib().fides_ctx_ks_tuning_set(self._h, pairs_per_thread))
 
     def encode(self, z, scale: float, towers: int) -> int:
         """Plaintext handle: the slot vector z (complex, length a power of two <= N/2) encoded on the GPU."""

@@ -109,6 +109,24 @@ int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms) {
   return FIDES_OK;
 }
 
+int fides_ctx_ks_tuning(fides_ctx* ctx, int32_t* iters, float* ms) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  if (iters) *iters = ctx->c->crt.ks_iters > 0 ? ctx->c->crt.ks_iters : std::min(4, ctx->c->N / 512);
+  if (ms)
+    for (int v = 0; v < fgb::Context::kKsTileVariants; v++) ms[v] = ctx->c->ks_tune_ms[v];
+  return FIDES_OK;
+}
+
+int fides_ctx_ks_tuning_set(fides_ctx* ctx, int32_t iters) {
+  if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
+  if ((iters != 1 && iters != 2 && iters != 4 && iters != 8) || iters > ctx->c->N / 512)
+    return fail(FIDES_EINVAL, "coefficient pairs per thread must be 1, 2, 4 or 8 and at most N / 512");
+  cudaStreamSynchronize(ctx->c->stream);
+  ctx->c->crt.ks_iters = iters;
+  ctx->c->ks_tuned = true;  // no later tuning overrides the caller's choice
+  return FIDES_OK;
+}
+
 int fides_ctx_set_mem_limit(fides_ctx* ctx, uint64_t bytes) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
   ctx->c->mem_limit = (size_t)bytes;

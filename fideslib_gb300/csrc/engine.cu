@@ -388,6 +388,39 @@ bool Context::build(const u64* roots, std::string* err) {
   return true;
 }
 
+cudaError_t Context::tune_ks(const KsBatch& kb, cudaStream_t s) {
+  // Every tile writes the same inner products, so the batch's own launch is timed once per tile that the ring
+  // allows (a thread block covers 512 * iters coefficients) and the caller's launch follows with the fastest.
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaError_t e = cudaEventCreate(&ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+  if (e == cudaSuccess) e = launch_ks_inner(kb, ring_, crt, d_pc, s);  // warm-up with the current tile
+  float best = 0;
+  int pick = 0;
+  for (int v = 0; v < kKsTileVariants && e == cudaSuccess; v++) {
+    const int it = 1 << v;
+    if (it > N / 512) continue;
+    crt.ks_iters = it;
+    e = cudaEventRecord(ev[0], s);
+    if (e == cudaSuccess) e = launch_ks_inner(kb, ring_, crt, d_pc, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+    float el = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&el, ev[0], ev[1]);
+    if (e != cudaSuccess) break;
+    ks_tune_ms[v] = el;
+    if (pick == 0 || el < best) {
+      best = el;
+      pick = it;
+    }
+  }
+  crt.ks_iters = pick;  // 0 (the kernel's default) if nothing was timed
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
+  ks_tuned = true;
+  return e;
+}
+
 u64* Context::alloc_limbs(size_t nlimbs, cudaStream_t s) {
   const size_t bytes = nlimbs * (size_t)N * sizeof(u64);
   std::lock_guard<std::mutex> lk(mem_mu_);
@@ -658,7 +691,8 @@ cudaError_t Context::keyswitch_run(const KsReq* reqs, int n, cudaStream_t s) {
       KsBatch& dst = r.ext_mode ? ex : md;
       dst.jobs[dst.njobs++] = j;
     }
-    err = launch_ks_inner(kb, ring_, crt, d_pc, s);
+    if (!ks_tuned && kb.njobs >= kKsTuneJobs) err = tune_ks(kb, s);  // the first batch of this size tunes the tile
+    if (err == cudaSuccess) err = launch_ks_inner(kb, ring_, crt, d_pc, s);
     if (err == cudaSuccess) err = moddown_jobs(md, s);
     if (err == cudaSuccess) err = launch_ext_epilogue(ex, ring_, crt, d_pc, s);
   }

@@ -79,6 +79,12 @@ class Context {
 
   DeviceTables tabs{};
   float ntt_tune_ms[kNttSizeClasses * (kNttFwdVariants + kNttInvVariants)] = {};  // tune_ntt timings
+  // Key inner product tile (coefficient pairs per thread: 1, 2, 4 or 8), tuned on the context's first key-switch
+  // launch of at least kKsTuneJobs jobs; until then (and where a tile does not apply) ks_tune_ms holds -1.
+  static constexpr int kKsTileVariants = 4;
+  static constexpr int kKsTuneJobs = 16;
+  float ks_tune_ms[kKsTileVariants] = {-1.f, -1.f, -1.f, -1.f};
+  bool ks_tuned = false;  // also set by fides_ctx_ks_tuning_set
   CrtTables crt{};
   PrimeConst* d_pc = nullptr;
   const ulonglong2* psi_brev = nullptr;  // [ntow][N] {psi^brev(i), shoup} in natural order (monomial products)
@@ -213,6 +219,9 @@ class Context {
   std::unordered_map<const void*, size_t> mem_sizes_;
   Context() = default;
   bool build(const u64* roots, std::string* err);
+  // Key inner product tile: runs the inner products of kb once per tile (identical results), timed on s with CUDA
+  // events, and sets crt.ks_iters to the fastest (ks_tune_ms holds the timings).  Synchronises with s once.
+  cudaError_t tune_ks(const KsBatch& kb, cudaStream_t s);
   std::vector<void*> owned_;  // device allocations freed at destruction
   void* dmalloc(size_t bytes);
   // INTT of the special rows, ModDown conversion, NTT and epilogue for the jobs of kb (inner, md, out, t, polys,

@@ -767,7 +767,7 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
     for (int i = 0; i < k; i++) tmax = std::max(tmax, bb.jobs[i].t);
     rows = (tmax + c.np) * k;
   }
-  const int iters = std::min(4, r.N / (2 * kT));  // N / 512 is a power of two >= 2
+  const int iters = std::min(c.ks_iters > 0 ? c.ks_iters : 4, r.N / (2 * kT));  // N / 512 is a power of two >= 2
   dim3 grid(r.N / (2 * kT * iters), rows, 1);
   switch (c.dnum) {  // beta <= dnum: size the register arrays exactly (fewer registers, more resident warps)
 #define FGB_KSI_CASE(B_)                                          \

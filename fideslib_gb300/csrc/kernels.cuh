@@ -29,6 +29,7 @@ inline cudaError_t once_per_device(std::atomic<unsigned long long>& done, F set)
 // CRT tables resident on the device (built once per context, Context::build).
 struct CrtTables {
   int nq, np, alpha, dnum, ntow;
+  int ks_iters;  // coefficient pairs per thread of the key inner product (power of two; 0 = 4), picked by tune_ks
   // ModUp, digit d with s towers: base b = (d*alpha + s-1)*alpha
   const ulonglong2* mu_qhinv;  // [b + i] = {[Qhat_i^-1]_{q_i}, shoup}
   const uint32_t* mu_qhat;     // [((b + i)*ntow + tower)*2 + {0,1}] = 30-bit slices (lo, hi) of [Qhat_i]_{m_tower}

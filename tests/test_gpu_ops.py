@@ -274,3 +274,42 @@ def test_batched_rotations_full_ring_cfg3(engine_lib):
         g, k = keys[idx]
         assert np.array_equal(gpu.store_ciphertext(o), orc.rotate(cts[t][0], g, k)), (t, idx)
     gpu.close()
+
+
+def test_every_inner_product_tile_bit_exact(env):
+    """The key inner product's tile (coefficient pairs per thread), tuned on the first key-switch launch of at least
+    16 ciphertexts: every tile the ring allows gives the oracle's residues for a batch of rotations at ragged levels
+    (a dnum-4 ring takes the three-product accumulation, the others the four-product one)."""
+    import fideslib_gb300 as F
+    ts = [env.nq, max(1, env.nq // 2), 1, max(1, env.nq - 1)]
+    cases = []
+    for k in range(16):
+        t, index = ts[k % 4], (1, -5)[k % 2]
+        g, key = env.rot_key(index)
+        ct = np.ascontiguousarray(env.orc.encrypt(500 + k, env.s, env.pt)[:, :t])
+        cases.append((env.gpu.load_ciphertext(ct, env.scale), index, env.orc.rotate(ct, g, key)))
+    ops = [(F.OP_ROTATE, h, 0, index) for h, index, _ in cases]
+
+    def check(tag):
+        outs = env.gpu.eval_batch(ops)
+        for o, (_, index, exp) in zip(outs, cases):
+            assert np.array_equal(env.gpu.store_ciphertext(o), exp), (tag, index)
+            env.gpu.free(o)
+
+    check("first batch")  # 16 jobs: tunes the tile if no earlier batch did
+    tun = env.gpu.ks_tuning()
+    allowed = [i for i in (1, 2, 4, 8) if i <= env.N // 512]
+    assert tun["pairs_per_thread"] in allowed, tun
+    assert all(tun["ms_1_2_4_8"][k] > 0 for k, i in enumerate((1, 2, 4, 8)) if i in allowed), tun
+    try:
+        for iters in (1, 2, 4, 8):
+            if iters not in allowed:
+                with pytest.raises(F.FidesError):
+                    env.gpu.set_ks_tile(iters)
+                continue
+            env.gpu.set_ks_tile(iters)
+            check(iters)
+    finally:
+        env.gpu.set_ks_tile(tun["pairs_per_thread"])
+    for h, _, _ in cases:
+        env.gpu.free(h)
