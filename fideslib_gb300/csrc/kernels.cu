@@ -22,6 +22,18 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
+bool pdl_for(long long ctas) {
+  static std::atomic<int> sms[64];  // SM count per device, 0 until first asked
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  int n = sms[dev].load(std::memory_order_relaxed);
+  if (n == 0) {
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+    sms[dev].store(n, std::memory_order_relaxed);
+  }
+  return ctas < n;
+}
+
 namespace {
 
 constexpr int kT = 256;
@@ -186,6 +198,7 @@ __device__ __forceinline__ void modup_body(const KsJob& J, const Ring& r, const 
 template <int MAXS>
 __global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                         const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   extern __shared__ uint2 cs[];
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const KsJob& J = b.jobs[z];
@@ -233,6 +246,7 @@ template <int MAXB>
 __global__ void __launch_bounds__(kT, MAXB <= 3 ? 3 : 2)
     ks_inner_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c, const PrimeConst* __restrict__ pc,
                     int iters) {
+  pdl_prologue();
   int q, rr, tmax;
   if (b.row_outer) {  // block row y = rr * njobs + q
     q = (int)blockIdx.y % b.njobs;
@@ -349,6 +363,7 @@ __global__ void __launch_bounds__(kT) key_split_kernel(u64* __restrict__ k, size
 template <int K>
 __global__ void __launch_bounds__(kT, K <= 11 ? 3 : 1) moddown_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                           const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   extern __shared__ uint2 cs[];  // [K][t]
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const KsJob& J = b.jobs[z];
@@ -380,6 +395,7 @@ __global__ void __launch_bounds__(kT, K <= 11 ? 3 : 1) moddown_conv_kernel(const
 // out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/512, rows); inner_Q arrives in [0, 4p).
 __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_constant__ KsBatch b, Ring r,
                                                               CrtTables c, const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const KsJob& J = b.jobs[z];
   const int t = J.t, row = (int)blockIdx.y - b.row_begin[z];
@@ -414,6 +430,7 @@ __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_const
 // a Q-basis ciphertext into the extended basis.
 __global__ void __launch_bounds__(kT) ext_epilogue_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                           const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const KsJob& J = b.jobs[z];
   const int t = J.t, ext = t + c.np, row = (int)blockIdx.y - b.row_begin[z];
@@ -453,6 +470,7 @@ __device__ __forceinline__ void st2(u64* p, ulonglong2 v) { *reinterpret_cast<ul
 
 __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ TensorBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const TensorJob& J = b.jobs[z];
   const int j = (int)blockIdx.y - b.row_begin[z];
@@ -468,6 +486,7 @@ __global__ void __launch_bounds__(kT) tensor_kernel(const __grid_constant__ Tens
 
 __global__ void __launch_bounds__(kT) addsub_kernel(const __grid_constant__ AddBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const AddJob& J = b.jobs[z];
   const int j = (int)blockIdx.y - b.row_begin[z];
@@ -485,6 +504,7 @@ __global__ void __launch_bounds__(kT) addsub_kernel(const __grid_constant__ AddB
 // OpenFHE NativeVector::SwitchModulus: values above om/2 are lifted to v - om before reduction mod nm.
 __global__ void __launch_bounds__(kT) ptop_kernel(const __grid_constant__ PtBatch b, Ring r,
                                                   const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const PtJob& J = b.jobs[z];
   const int j = (int)blockIdx.y - b.row_begin[z];
@@ -505,6 +525,7 @@ __global__ void __launch_bounds__(kT) ptop_kernel(const __grid_constant__ PtBatc
 
 __global__ void __launch_bounds__(kT) scalar_kernel(const __grid_constant__ ScalarBatch b, Ring r,
                                                     const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const ScalarJob& J = b.jobs[z];
   const ScalarSet& S = b.sets[J.set];
@@ -521,6 +542,7 @@ __global__ void __launch_bounds__(kT) scalar_kernel(const __grid_constant__ Scal
 // products, each product reduced (Shoup) and summed mod q.
 __global__ void __launch_bounds__(kT) wsum_kernel(const __grid_constant__ WsumBatch b, Ring r,
                                                   const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const WsumJob& J = b.jobs[z];
   const int row = (int)blockIdx.y - b.row_begin[z];
@@ -548,6 +570,7 @@ __global__ void __launch_bounds__(kT) wsum_kernel(const __grid_constant__ WsumBa
 __global__ void __launch_bounds__(kT) monomial_kernel(const __grid_constant__ MonoBatch b, Ring r,
                                                       const PrimeConst* __restrict__ pc,
                                                       const ulonglong2* __restrict__ tw) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const MonoJob& J = b.jobs[z];
   const int row = (int)blockIdx.y - b.row_begin[z];
@@ -581,6 +604,7 @@ __device__ __forceinline__ void cp_async8(u64* dst, const u64* src, bool on) {
 
 __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBatch b, Ring r,
                                                    const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   extern __shared__ __align__(16) u64 stage[];  // [2 rounds][kDotWords][kT]
   const int y = (int)blockIdx.y, job = y % b.njobs, j = y / b.njobs;
   const DotJob& J = b.jobs[job];
@@ -652,6 +676,7 @@ __global__ void __launch_bounds__(kT) ptdot_kernel(const __grid_constant__ DotBa
 
 __global__ void __launch_bounds__(kT) sum_kernel(const __grid_constant__ SumBatch b, Ring r,
                                                  const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const SumJob& J = b.jobs[z];
   const int row = (int)blockIdx.y - b.row_begin[z];
@@ -667,6 +692,7 @@ __global__ void __launch_bounds__(kT) sum_kernel(const __grid_constant__ SumBatc
 // Centred lift of tower 0 into towers 0..T-1 (OpenFHE SwitchModulus semantics, as in Rescale).
 __global__ void __launch_bounds__(kT) raise_switch_kernel(const __grid_constant__ RaiseBatch b, Ring r,
                                                           const PrimeConst* __restrict__ pc) {
+  pdl_prologue();
   const int z = find_job(b.row_begin, b.njobs, (int)blockIdx.y);
   const RaiseJob& J = b.jobs[z];
   const int row = (int)blockIdx.y - b.row_begin[z];
@@ -714,15 +740,15 @@ cudaError_t launch_modup_conv(const KsBatch& b, const Ring& r, const CrtTables& 
   const int rows = with_rows(b, bb, [alpha](const KsJob& j) { return (j.t + alpha - 1) / alpha; });
   dim3 grid(r.N / (c.alpha <= 16 ? 2 * kT : kT), rows, 1);
   if (c.alpha <= 8)
-    modup_conv_kernel<8><<<grid, kT, smem, s>>>(bb, r, c, pc);
+    launch_pdl(modup_conv_kernel<8>, grid, dim3(kT), smem, s, bb, r, c, pc);
   else if (c.alpha <= 10)
-    modup_conv_kernel<10><<<grid, kT, smem, s>>>(bb, r, c, pc);
+    launch_pdl(modup_conv_kernel<10>, grid, dim3(kT), smem, s, bb, r, c, pc);
   else if (c.alpha <= 12)
-    modup_conv_kernel<12><<<grid, kT, smem, s>>>(bb, r, c, pc);
+    launch_pdl(modup_conv_kernel<12>, grid, dim3(kT), smem, s, bb, r, c, pc);
   else if (c.alpha <= 16)
-    modup_conv_kernel<16><<<grid, kT, smem, s>>>(bb, r, c, pc);
+    launch_pdl(modup_conv_kernel<16>, grid, dim3(kT), smem, s, bb, r, c, pc);
   else
-    modup_conv_kernel<32><<<grid, kT, smem, s>>>(bb, r, c, pc);
+    launch_pdl(modup_conv_kernel<32>, grid, dim3(kT), smem, s, bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -772,7 +798,7 @@ cudaError_t launch_ks_inner(const KsBatch& b, const Ring& r, const CrtTables& c,
   switch (c.dnum) {  // beta <= dnum: size the register arrays exactly (fewer registers, more resident warps)
 #define FGB_KSI_CASE(B_)                                          \
   case B_:                                                        \
-    ks_inner_kernel<B_><<<grid, kT, 0, s>>>(bb, r, c, pc, iters); \
+    launch_pdl(ks_inner_kernel<B_>, grid, dim3(kT), 0, s, bb, r, c, pc, iters); \
     break;
     FGB_KSI_CASE(1) FGB_KSI_CASE(2) FGB_KSI_CASE(3) FGB_KSI_CASE(4) FGB_KSI_CASE(5) FGB_KSI_CASE(6)
     FGB_KSI_CASE(7) FGB_KSI_CASE(8)
@@ -823,7 +849,7 @@ cudaError_t launch_moddown_conv(const KsBatch& b, const Ring& r, const CrtTables
   switch (c.np) {
 #define FGB_MD_CASE(K_)                                                    \
   case K_:                                                                 \
-    moddown_conv_kernel<K_><<<grid, kT, smem, s>>>(bb, r, c, pc);          \
+    launch_pdl(moddown_conv_kernel<K_>, grid, dim3(kT), smem, s, bb, r, c, pc);          \
     break;
     FGB_MD_CASE(1) FGB_MD_CASE(2) FGB_MD_CASE(3) FGB_MD_CASE(4) FGB_MD_CASE(5) FGB_MD_CASE(6) FGB_MD_CASE(7)
     FGB_MD_CASE(8) FGB_MD_CASE(9) FGB_MD_CASE(10) FGB_MD_CASE(11) FGB_MD_CASE(12) FGB_MD_CASE(13)
@@ -842,7 +868,7 @@ cudaError_t launch_moddown_epilogue(const KsBatch& b, const Ring& r, const CrtTa
   KsBatch bb;
   const int rows = with_rows(b, bb, [](const KsJob& j) { return (j.polys ? j.polys : 2) * j.t; });
   dim3 grid(r.N / (2 * kT), rows, 1);
-  moddown_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
+  launch_pdl(moddown_epilogue_kernel, grid, dim3(kT), 0, s, bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -854,7 +880,7 @@ cudaError_t launch_ext_epilogue(const KsBatch& b, const Ring& r, const CrtTables
   const int np = c.np;
   const int rows = with_rows(b, bb, [np](const KsJob& j) { return 2 * (j.t + np); });
   dim3 grid(r.N / (2 * kT), rows, 1);
-  ext_epilogue_kernel<<<grid, kT, 0, s>>>(bb, r, c, pc);
+  launch_pdl(ext_epilogue_kernel, grid, dim3(kT), 0, s, bb, r, c, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -864,7 +890,7 @@ cudaError_t launch_tensor(const TensorBatch& b, const Ring& r, int nq, const Pri
   TensorBatch bb;
   const int rows = with_rows(b, bb, [](const TensorJob& j) { return j.t; });
   dim3 grid(r.N / (2 * kT), rows, 1);
-  tensor_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
+  launch_pdl(tensor_kernel, grid, dim3(kT), 0, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -874,7 +900,7 @@ cudaError_t launch_addsub(const AddBatch& b, const Ring& r, int nq, const PrimeC
   AddBatch bb;
   const int rows = with_rows(b, bb, [](const AddJob& j) { return j.t; });
   dim3 grid(r.N / (2 * kT), rows, 1);
-  addsub_kernel<<<grid, kT, 0, s>>>(bb, r, pc);
+  launch_pdl(addsub_kernel, grid, dim3(kT), 0, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -883,7 +909,7 @@ cudaError_t launch_ptop(const PtBatch& b, const Ring& r, const PrimeConst* pc, c
   if (b.njobs <= 0) return cudaSuccess;
   PtBatch bb;
   const int rows = with_rows(b, bb, [](const PtJob& j) { return j.t; });
-  ptop_kernel<<<dim3(r.N / (2 * kT), rows, 1), kT, 0, s>>>(bb, r, pc);
+  launch_pdl(ptop_kernel, dim3(r.N / (2 * kT), rows, 1), dim3(kT), 0, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -892,7 +918,7 @@ cudaError_t launch_scalar(const ScalarBatch& b, const Ring& r, const PrimeConst*
   if (b.njobs <= 0) return cudaSuccess;
   ScalarBatch bb;
   const int rows = with_rows(b, bb, [](const ScalarJob& j) { return j.t; });
-  scalar_kernel<<<dim3(r.N / (2 * kT), rows, 1), kT, 0, s>>>(bb, r, pc);
+  launch_pdl(scalar_kernel, dim3(r.N / (2 * kT), rows, 1), dim3(kT), 0, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -902,7 +928,7 @@ cudaError_t launch_wsum(const WsumBatch& b, const Ring& r, const PrimeConst* pc,
   if (b.nterms < 1 || b.nterms > kMaxWsumTerms) return cudaErrorInvalidValue;
   WsumBatch bb;
   const int rows = with_rows(b, bb, [](const WsumJob& j) { return 2 * j.t; });
-  wsum_kernel<<<dim3(r.N / (2 * kT), rows, 1), kT, 0, s>>>(bb, r, pc);
+  launch_pdl(wsum_kernel, dim3(r.N / (2 * kT), rows, 1), dim3(kT), 0, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -912,7 +938,7 @@ cudaError_t launch_monomial(const MonoBatch& b, const Ring& r, const PrimeConst*
   if (b.njobs <= 0) return cudaSuccess;
   MonoBatch bb;
   const int rows = with_rows(b, bb, [](const MonoJob& j) { return 2 * j.t; });
-  monomial_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc, tw_fwd);
+  launch_pdl(monomial_kernel, dim3(r.N / kT, rows, 1), dim3(kT), 0, s, bb, r, pc, tw_fwd);
   count_launch();
   return cudaGetLastError();
 }
@@ -935,7 +961,7 @@ cudaError_t launch_ptdot(const DotBatch& b, const Ring& r, const PrimeConst* pc,
     return cudaFuncSetAttribute(ptdot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
   if (ea != cudaSuccess) return ea;
-  ptdot_kernel<<<dim3(r.N / kT, (b.t + b.np) * b.njobs, 1), kT, smem, s>>>(bb, r, pc);
+  launch_pdl(ptdot_kernel, dim3(r.N / kT, (b.t + b.np) * b.njobs, 1), dim3(kT), smem, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -944,7 +970,7 @@ cudaError_t launch_sum(const SumBatch& b, const Ring& r, const PrimeConst* pc, c
   if (b.njobs <= 0) return cudaSuccess;
   SumBatch bb;
   const int rows = with_rows(b, bb, [](const SumJob& j) { return 2 * (j.t + j.np); });
-  sum_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  launch_pdl(sum_kernel, dim3(r.N / kT, rows, 1), dim3(kT), 0, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }
@@ -953,7 +979,7 @@ cudaError_t launch_raise_switch(const RaiseBatch& b, const Ring& r, const PrimeC
   if (b.njobs <= 0) return cudaSuccess;
   RaiseBatch bb;
   const int rows = with_rows(b, bb, [](const RaiseJob& j) { return 2 * j.T; });
-  raise_switch_kernel<<<dim3(r.N / kT, rows, 1), kT, 0, s>>>(bb, r, pc);
+  launch_pdl(raise_switch_kernel, dim3(r.N / kT, rows, 1), dim3(kT), 0, s, bb, r, pc);
   count_launch();
   return cudaGetLastError();
 }

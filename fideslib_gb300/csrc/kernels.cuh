@@ -12,6 +12,37 @@ namespace fgb {
 
 constexpr int kMaxJobs = 64;
 
+// Programmatic dependent launch for latency-bound launches.  A pipeline kernel whose grid is smaller than the
+// GPU's SM count is launched with the programmatic-serialization attribute (launch_pdl), so its CTAs are scheduled
+// while the previous kernel of the same stream is still running instead of after it.  Every pipeline kernel
+// starts with pdl_prologue(): griddepcontrol.wait blocks until the previous kernel has completed and its writes
+// are visible (a no-op for a kernel launched without the attribute), then griddepcontrol.launch_dependents lets
+// the next kernel be scheduled the same way.  Nothing is read or written before the wait, so the stream order of
+// every memory access is unchanged.  Larger grids launch as before: with the attribute on every launch, one
+// HMult + relinearise + Rescale at N = 2^13 went 0.115 -> 0.092 ms, but 64 of them batched lost 6%, hoisted
+// rotations 4% and the bootstrap batch 3%.
+__device__ __forceinline__ void pdl_prologue() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+// Whether a launch of `ctas` CTAs takes the programmatic-serialization attribute (fewer CTAs than the current
+// device has SMs).
+bool pdl_for(long long ctas);
+template <typename... P, typename... A>
+inline cudaError_t launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_for((long long)grid.x * grid.y * grid.z) ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
+}
+
 // Runs `set` (a kernel attribute such as its dynamic shared-memory limit, which applies per device) once per device
 // of the process; safe to call from several host threads.
 template <class F>

@@ -408,6 +408,7 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
 template <int LOGN>
 __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_constant__ NttBatch b,
                                                            const __grid_constant__ DeviceTables T) {
+  pdl_prologue();
   ntt_fwd_body<LOGN, false>(b, T, nullptr);
 }
 
@@ -415,12 +416,14 @@ template <int LOGN>
 __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_epi_kernel(const __grid_constant__ NttBatch b,
                                                                const __grid_constant__ DeviceTables T,
                                                                const __grid_constant__ NttEpi e) {
+  pdl_prologue();
   ntt_fwd_body<LOGN, true>(b, T, &e);
 }
 
 template <int LOGN>
 __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_constant__ NttBatch b,
                                                            const __grid_constant__ DeviceTables T) {
+  pdl_prologue();
   using S = Shape<LOGN>;
   extern __shared__ __align__(16) u64 sm[];
   const int tid = threadIdx.x;
@@ -640,6 +643,7 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
 template <int LOGN, int LOGE>
 __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_constant__ NttBatch b,
                                                                  const __grid_constant__ DeviceTables T) {
+  pdl_prologue();
   ntt16_fwd_body<LOGN, LOGE, false>(b, T, nullptr);
 }
 
@@ -648,6 +652,7 @@ template <int LOGN, int LOGE>
 __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_epi_kernel(const __grid_constant__ NttBatch b,
                                                                      const __grid_constant__ DeviceTables T,
                                                                      const __grid_constant__ NttEpi e) {
+  pdl_prologue();
   ntt16_fwd_body<LOGN, LOGE, true>(b, T, &e);
 }
 
@@ -656,6 +661,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_epi_kernel(const __gr
 template <int LOGN, int LOGE>
 __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_constant__ NttBatch b,
                                                                  const __grid_constant__ DeviceTables T) {
+  pdl_prologue();
   using S = Shape16<LOGN, LOGE>;
   extern __shared__ __align__(16) u64 sm[];
   const int tid = threadIdx.x;
@@ -749,13 +755,16 @@ cudaError_t launch16(const NttBatch& b, const DeviceTables& t, bool inverse, cud
   cfg.blockDim = dim3(kThreads16, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = S::C;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[1].id = cudaLaunchAttributeClusterDimension;
+  attr[1].val.clusterDim.x = S::C;
+  attr[1].val.clusterDim.y = 1;
+  attr[1].val.clusterDim.z = 1;
+  // the programmatic-serialization attribute for a grid of fewer CTAs than SMs (see launch_pdl), the cluster shape
+  cfg.attrs = pdl_for((long long)cfg.gridDim.x * cfg.gridDim.y) ? attr : attr + 1;
+  cfg.numAttrs = (cfg.attrs == attr ? 1 : 0) + (S::C > 1 ? 1 : 0);
   cudaError_t e = cudaLaunchKernelEx(&cfg, kern, b, t);
   if (e != cudaSuccess) return e;
   count_launch();
@@ -779,13 +788,16 @@ cudaError_t launch16_epi(const NttBatch& b, const NttEpi& e, const DeviceTables&
   cfg.blockDim = dim3(kThreads16, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = S::C;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[1].id = cudaLaunchAttributeClusterDimension;
+  attr[1].val.clusterDim.x = S::C;
+  attr[1].val.clusterDim.y = 1;
+  attr[1].val.clusterDim.z = 1;
+  // the programmatic-serialization attribute for a grid of fewer CTAs than SMs (see launch_pdl), the cluster shape
+  cfg.attrs = pdl_for((long long)cfg.gridDim.x * cfg.gridDim.y) ? attr : attr + 1;
+  cfg.numAttrs = (cfg.attrs == attr ? 1 : 0) + (S::C > 1 ? 1 : 0);
   cudaError_t err = cudaLaunchKernelEx(&cfg, kern, b, t, e);
   if (err != cudaSuccess) return err;
   count_launch();
@@ -807,13 +819,16 @@ cudaError_t launch_t_epi(const NttBatch& b, const NttEpi& e, const DeviceTables&
   cfg.blockDim = dim3(kThreads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = S::C;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[1].id = cudaLaunchAttributeClusterDimension;
+  attr[1].val.clusterDim.x = S::C;
+  attr[1].val.clusterDim.y = 1;
+  attr[1].val.clusterDim.z = 1;
+  // the programmatic-serialization attribute for a grid of fewer CTAs than SMs (see launch_pdl), the cluster shape
+  cfg.attrs = pdl_for((long long)cfg.gridDim.x * cfg.gridDim.y) ? attr : attr + 1;
+  cfg.numAttrs = (cfg.attrs == attr ? 1 : 0) + (S::C > 1 ? 1 : 0);
   cudaError_t err = cudaLaunchKernelEx(&cfg, kern, b, t, e);
   if (err != cudaSuccess) return err;
   count_launch();
@@ -835,13 +850,16 @@ cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cud
   cfg.blockDim = dim3(kThreads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = S::C;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = S::C > 1 ? 1 : 0;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[1].id = cudaLaunchAttributeClusterDimension;
+  attr[1].val.clusterDim.x = S::C;
+  attr[1].val.clusterDim.y = 1;
+  attr[1].val.clusterDim.z = 1;
+  // the programmatic-serialization attribute for a grid of fewer CTAs than SMs (see launch_pdl), the cluster shape
+  cfg.attrs = pdl_for((long long)cfg.gridDim.x * cfg.gridDim.y) ? attr : attr + 1;
+  cfg.numAttrs = (cfg.attrs == attr ? 1 : 0) + (S::C > 1 ? 1 : 0);
   cudaError_t e = cudaLaunchKernelEx(&cfg, kern, b, t);
   if (e != cudaSuccess) return e;
   count_launch();
