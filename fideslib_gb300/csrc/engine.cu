@@ -511,7 +511,11 @@ struct NttQueue {
   cudaStream_t s;
   NttBatch b{};
   cudaError_t err = cudaSuccess;
-  NttQueue(const DeviceTables& t, bool inv, cudaStream_t st) : tabs(t), inverse(inv), s(st) {}
+  // lazy (inverse only): outputs left in [0, 4p), for transforms whose only reader is a basis conversion (its
+  // Shoup product by the Qhat^-1 / Phat^-1 factor takes any 64-bit input)
+  NttQueue(const DeviceTables& t, bool inv, cudaStream_t st, bool lazy = false) : tabs(t), inverse(inv), s(st) {
+    b.lazy_out = lazy ? 1 : 0;
+  }
   void add(const u64* src, u64* dst, long long ss, long long ds, int limbs, int npolys, const uint8_t* prime_of) {
     if (err != cudaSuccess || limbs <= 0 || npolys <= 0) return;
     if (b.njobs == kMaxNttJobs) flush();
@@ -541,9 +545,9 @@ cudaError_t Context::modup(const u64* const* a, const int* ts, u64* const* coeff
   const size_t NN = (size_t)N;
   cudaError_t err = cudaSuccess;
   uint8_t pm[64];
-  // 1) INTT of every input into its coefficient buffer
+  // 1) INTT of every input into its coefficient buffer (read only by the conversion: left in [0, 4p))
   {
-    NttQueue q(tabs, true, s);
+    NttQueue q(tabs, true, s, true);
     for (int g = 0; g < ng; g++) {
       for (int j = 0; j < ts[g]; j++) pm[j] = (uint8_t)j;
       q.add(a[g], coeff[g], 0, 0, ts[g], 1, pm);
@@ -705,8 +709,8 @@ cudaError_t Context::moddown_jobs(const KsBatch& kb, cudaStream_t s) {
   const size_t NN = (size_t)N;
   uint8_t pm[64];
   cudaError_t err;
-  {
-    NttQueue q(tabs, true, s);
+  {  // the P rows to coefficient form, read only by the ModDown conversion: left in [0, 4p)
+    NttQueue q(tabs, true, s, true);
     for (int k = 0; k < np; k++) pm[k] = (uint8_t)(nq + k);
     for (int b = 0; b < kb.njobs; b++) {
       const KsJob& j = kb.jobs[b];

@@ -420,7 +420,8 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_epi_kernel(const __grid_c
   ntt_fwd_body<LOGN, true>(b, T, &e);
 }
 
-template <int LOGN>
+// LAZY: outputs left in [0, 4p) (NttBatch::lazy_out), a compile-time choice so the exact path pays no branch.
+template <int LOGN, bool LAZY>
 __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_constant__ NttBatch b,
                                                            const __grid_constant__ DeviceTables T) {
   pdl_prologue();
@@ -480,7 +481,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
 #pragma unroll
       for (int k = 0; k < R; k++) {
         const int l = k * 256 + tid;
-        if (l < S::E) L.dst[l] = csub(csub(x[k], p2), p);
+        if (l < S::E) L.dst[l] = LAZY ? x[k] : csub(csub(x[k], p2), p);
       }
       return;
     } else {
@@ -505,7 +506,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
       const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
       inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, negp, p4, &last);
 #pragma unroll
-      for (int hh = 0; hh < S::C; hh++) L.dst[hh * S::E + l] = csub(csub(x[hh], p2), p);
+      for (int hh = 0; hh < S::C; hh++) L.dst[hh * S::E + l] = LAZY ? x[hh] : csub(csub(x[hh], p2), p);
     }
     cl.sync();  // peers may still be reading this CTA's shared memory
   }
@@ -657,8 +658,9 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_epi_kernel(const __gr
 }
 
 // Inverse of the same shape (Gentleman–Sande, passes C^-1, B^-1, A^-1, then the cross-CTA phase X^-1 reading
-// the peers' shared memory; N^-1 applied on the way out), with LOGE = 12 or 13 (autotuned).
-template <int LOGN, int LOGE>
+// the peers' shared memory; N^-1 applied on the way out), with LOGE = 12 or 13 (autotuned); LAZY as for
+// ntt_inv_kernel.
+template <int LOGN, int LOGE, bool LAZY>
 __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_constant__ NttBatch b,
                                                                  const __grid_constant__ DeviceTables T) {
   pdl_prologue();
@@ -732,7 +734,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
       const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
       inv_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4, &last);
 #pragma unroll
-      for (int k = 0; k < R; k++) L.dst[k * 4096 + col] = csub(csub(x[k], p2), p);
+      for (int k = 0; k < R; k++) L.dst[k * 4096 + col] = LAZY ? x[k] : csub(csub(x[k], p2), p);
     }
     if constexpr (S::C > 1) cg::this_cluster().sync();  // peers may still be reading this CTA's shared memory
   }
@@ -741,10 +743,13 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
 template <int LOGN, int LOGE>
 cudaError_t launch16(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape16<LOGN, LOGE>;
-  auto kern = inverse ? ntt16_inv_kernel<LOGN, LOGE> : ntt16_fwd_kernel<LOGN, LOGE>;
-  static std::atomic<unsigned long long> attr_done[2];
+  const int which = inverse ? (b.lazy_out ? 2 : 1) : 0;
+  auto kern = which == 2 ? ntt16_inv_kernel<LOGN, LOGE, true>
+              : which == 1 ? ntt16_inv_kernel<LOGN, LOGE, false>
+                           : ntt16_fwd_kernel<LOGN, LOGE>;
+  static std::atomic<unsigned long long> attr_done[3];
   const size_t smem = S::SMEM;
-  const cudaError_t ea = once_per_device(attr_done[inverse], [&] {
+  const cudaError_t ea = once_per_device(attr_done[which], [&] {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess && S::C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return e;
@@ -838,10 +843,11 @@ cudaError_t launch_t_epi(const NttBatch& b, const NttEpi& e, const DeviceTables&
 template <int LOGN>
 cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape<LOGN>;
-  auto kern = inverse ? ntt_inv_kernel<LOGN> : ntt_fwd_kernel<LOGN>;
-  static std::atomic<unsigned long long> attr_done[2];
+  const int which = inverse ? (b.lazy_out ? 2 : 1) : 0;
+  auto kern = which == 2 ? ntt_inv_kernel<LOGN, true> : which == 1 ? ntt_inv_kernel<LOGN, false> : ntt_fwd_kernel<LOGN>;
+  static std::atomic<unsigned long long> attr_done[3];
   const size_t smem = S::SMEM;
-  const cudaError_t ea = once_per_device(attr_done[inverse], [&] {
+  const cudaError_t ea = once_per_device(attr_done[which], [&] {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
   if (ea != cudaSuccess) return ea;
