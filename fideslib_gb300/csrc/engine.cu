@@ -511,8 +511,9 @@ struct NttQueue {
   cudaStream_t s;
   NttBatch b{};
   cudaError_t err = cudaSuccess;
-  // lazy (inverse only): outputs left in [0, 4p), for transforms whose only reader is a basis conversion (its
-  // Shoup product by the Qhat^-1 / Phat^-1 factor takes any 64-bit input)
+  // lazy: outputs left in [0, 4p), for transforms whose readers reduce them: the basis conversions (their Shoup
+  // product by the Qhat^-1 / Phat^-1 factor takes any 64-bit input), the ModDown epilogue, the key inner product
+  // of at most three digits
   NttQueue(const DeviceTables& t, bool inv, cudaStream_t st, bool lazy = false) : tabs(t), inverse(inv), s(st) {
     b.lazy_out = lazy ? 1 : 0;
   }
@@ -569,7 +570,10 @@ cudaError_t Context::modup(const u64* const* a, const int* ts, u64* const* coeff
     err = launch_modup_conv(kb, ring_, crt, d_pc, s);
   }
   if (err == cudaSuccess) {
-    NttQueue q(tabs, false, s);
+    // The converted digits are read only by the key inner product.  With at most three digits it accumulates four
+    // 30-bit-slice products per term, which stay exact for digit values below 2^62, so the transform may leave them
+    // in [0, 4p) (beta * (2^32 * 2^30) < 2^64 for beta <= 3); with more digits they are fully reduced.
+    NttQueue q(tabs, false, s, dnum <= 3);
     for (int g = 0; g < ng; g++) {
       const int t = ts[g], beta = (t + alpha - 1) / alpha;
       for (int d = 0; d < beta; d++) {
@@ -722,7 +726,7 @@ cudaError_t Context::moddown_jobs(const KsBatch& kb, cudaStream_t s) {
   }
   if (err == cudaSuccess) err = launch_moddown_conv(kb, ring_, crt, d_pc, s);
   if (err == cudaSuccess) {
-    NttQueue q(tabs, false, s);
+    NttQueue q(tabs, false, s, true);  // read only by the epilogue, which takes [0, 4p)
     for (int b = 0; b < kb.njobs; b++) {
       const KsJob& j = kb.jobs[b];
       for (int k = 0; k < j.t; k++) pm[k] = (uint8_t)k;

@@ -392,7 +392,8 @@ __global__ void __launch_bounds__(kT, K <= 11 ? 3 : 1) moddown_conv_kernel(const
   conv_rows<K, NC>(yl, yh, cs, t, J.md + (size_t)poly * t * r.N + n, (size_t)r.N, pc, [](int j) { return j; });
 }
 
-// out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/512, rows); inner_Q arrives in [0, 4p).
+// out = automorph((inner_Q - NTT(conv)) * P^-1 + add): grid (N/512, rows); inner_Q and NTT(conv) arrive in [0, 4p)
+// (both left lazy by their producers), so x + 4p - y is in (0, 8p) and the Shoup product by P^-1 reduces it.
 __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_constant__ KsBatch b, Ring r,
                                                               CrtTables c, const PrimeConst* __restrict__ pc) {
   pdl_prologue();
@@ -404,15 +405,15 @@ __global__ void __launch_bounds__(kT) moddown_epilogue_kernel(const __grid_const
   const size_t N = r.N;
   const u64 q = pc[j].p;
   const ulonglong2 w = c.md_pinv[j];
-  ulonglong2 x = *reinterpret_cast<const ulonglong2*>(J.inner + ((size_t)poly * (t + c.np) + j) * N + n);
-  x = make_ulonglong2(csub(csub(x.x, 2 * q), q), csub(csub(x.y, 2 * q), q));  // inner products are in [0, 4p)
+  const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(J.inner + ((size_t)poly * (t + c.np) + j) * N + n);
   const ulonglong2 y = *reinterpret_cast<const ulonglong2*>(J.md + ((size_t)poly * t + j) * N + n);
+  const u64 q4 = 4 * q;
   const u64* add = poly == 0 ? J.add0 : J.add1;
   const ulonglong2 a = add ? *reinterpret_cast<const ulonglong2*>(add + (size_t)j * N + n) : make_ulonglong2(0, 0);
   u64* out = J.out + ((size_t)poly * t + j) * N;
 #pragma unroll
   for (int e = 0; e < 2; e++) {
-    u64 v = shoup(sub_mod(e ? x.y : x.x, e ? y.y : y.x, q), w.x, w.y, q);
+    u64 v = shoup((e ? x.y : x.x) + q4 - (e ? y.y : y.x), w.x, w.y, q);
     if (add) v = add_mod(v, e ? a.y : a.x, q);
     uint32_t pos = n + e;
     if (J.galois_inv != 1) {

@@ -301,7 +301,8 @@ __device__ __forceinline__ void epi_store16(const NttEpi* e, const LimbRef& L, i
 }
 
 // EPI: the fused rescale of NttEpi (null for the plain transform).
-template <int LOGN, bool EPI>
+// LAZY (plain transform only): outputs left in [0, 4p) (NttBatch::lazy_out) instead of [0, p).
+template <int LOGN, bool EPI, bool LAZY = false>
 __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTables& T, const NttEpi* e) {
   using S = Shape<LOGN>;
   extern __shared__ __align__(16) u64 sm[];
@@ -397,19 +398,24 @@ __device__ __forceinline__ void ntt_fwd_body(const NttBatch& b, const DeviceTabl
 #pragma unroll
       for (int k = 0; k < 16; k += 2) {
         ulonglong2 v;
-        v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
-        v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
+        if constexpr (LAZY) {
+          v.x = csub(csub(x[k], 2 * p4), p4);
+          v.y = csub(csub(x[k + 1], 2 * p4), p4);
+        } else {
+          v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
+          v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
+        }
         out[k / 2] = v;
       }
     }
   }
 }
 
-template <int LOGN>
+template <int LOGN, bool LAZY>
 __global__ void __launch_bounds__(kThreads, 2) ntt_fwd_kernel(const __grid_constant__ NttBatch b,
                                                            const __grid_constant__ DeviceTables T) {
   pdl_prologue();
-  ntt_fwd_body<LOGN, false>(b, T, nullptr);
+  ntt_fwd_body<LOGN, false, LAZY>(b, T, nullptr);
 }
 
 template <int LOGN>
@@ -546,7 +552,7 @@ struct Shape16 {
 };
 
 // EPI: the fused rescale of NttEpi (null for the plain transform).
-template <int LOGN, int LOGE, bool EPI>
+template <int LOGN, int LOGE, bool EPI, bool LAZY = false>
 __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTables& T, const NttEpi* e) {
   using S = Shape16<LOGN, LOGE>;
   extern __shared__ __align__(16) u64 sm[];
@@ -633,19 +639,24 @@ __device__ __forceinline__ void ntt16_fwd_body(const NttBatch& b, const DeviceTa
 #pragma unroll
       for (int k = 0; k < 16; k += 2) {
         ulonglong2 v;
-        v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
-        v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
+        if constexpr (LAZY) {
+          v.x = csub(csub(x[k], 2 * p4), p4);
+          v.y = csub(csub(x[k + 1], 2 * p4), p4);
+        } else {
+          v.x = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
+          v.y = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
+        }
         out[k / 2] = v;
       }
     }
   }
 }
 
-template <int LOGN, int LOGE>
+template <int LOGN, int LOGE, bool LAZY>
 __global__ void __launch_bounds__(kThreads16, 3) ntt16_fwd_kernel(const __grid_constant__ NttBatch b,
                                                                  const __grid_constant__ DeviceTables T) {
   pdl_prologue();
-  ntt16_fwd_body<LOGN, LOGE, false>(b, T, nullptr);
+  ntt16_fwd_body<LOGN, LOGE, false, LAZY>(b, T, nullptr);
 }
 
 // The forward transform with the fused rescale (NttEpi).
@@ -743,11 +754,12 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
 template <int LOGN, int LOGE>
 cudaError_t launch16(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape16<LOGN, LOGE>;
-  const int which = inverse ? (b.lazy_out ? 2 : 1) : 0;
-  auto kern = which == 2 ? ntt16_inv_kernel<LOGN, LOGE, true>
-              : which == 1 ? ntt16_inv_kernel<LOGN, LOGE, false>
-                           : ntt16_fwd_kernel<LOGN, LOGE>;
-  static std::atomic<unsigned long long> attr_done[3];
+  const int which = (inverse ? 2 : 0) + (b.lazy_out ? 1 : 0);
+  auto kern = which == 3   ? ntt16_inv_kernel<LOGN, LOGE, true>
+              : which == 2 ? ntt16_inv_kernel<LOGN, LOGE, false>
+              : which == 1 ? ntt16_fwd_kernel<LOGN, LOGE, true>
+                           : ntt16_fwd_kernel<LOGN, LOGE, false>;
+  static std::atomic<unsigned long long> attr_done[4];
   const size_t smem = S::SMEM;
   const cudaError_t ea = once_per_device(attr_done[which], [&] {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -843,9 +855,12 @@ cudaError_t launch_t_epi(const NttBatch& b, const NttEpi& e, const DeviceTables&
 template <int LOGN>
 cudaError_t launch_t(const NttBatch& b, const DeviceTables& t, bool inverse, cudaStream_t s) {
   using S = Shape<LOGN>;
-  const int which = inverse ? (b.lazy_out ? 2 : 1) : 0;
-  auto kern = which == 2 ? ntt_inv_kernel<LOGN, true> : which == 1 ? ntt_inv_kernel<LOGN, false> : ntt_fwd_kernel<LOGN>;
-  static std::atomic<unsigned long long> attr_done[3];
+  const int which = (inverse ? 2 : 0) + (b.lazy_out ? 1 : 0);
+  auto kern = which == 3   ? ntt_inv_kernel<LOGN, true>
+              : which == 2 ? ntt_inv_kernel<LOGN, false>
+              : which == 1 ? ntt_fwd_kernel<LOGN, true>
+                           : ntt_fwd_kernel<LOGN, false>;
+  static std::atomic<unsigned long long> attr_done[4];
   const size_t smem = S::SMEM;
   const cudaError_t ea = once_per_device(attr_done[which], [&] {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -26,7 +26,7 @@ constexpr int kMaxNttJobs = 64;
 
 struct NttBatch {
   int njobs;
-  int lazy_out;  // inverse only: outputs left in [0, 4p) (for the basis conversions, whose first step reduces them)
+  int lazy_out;  // outputs left in [0, 4p) instead of [0, p), for readers that reduce them (see NttQueue)
   int limb_begin[kMaxNttJobs + 1];  // prefix sums of limbs * npolys: grid.y covers exactly the real limbs
   NttJob jobs[kMaxNttJobs];
 };
