@@ -117,12 +117,14 @@ __device__ __forceinline__ int conv_tower(int jj, int start, int s, int t, int n
 // halves and the constants c_{i,jj} staged in shared memory as 30-bit halves (one shared load serves the NC
 // coefficients).  S is a compile-time constant so no multiply-add is issued for absent towers.  Every output feeds
 // a forward NTT, which accepts residues in [0, 8p), so the outputs are left unreduced in that range (the NTT's own
-// output is fully reduced).
+// output is fully reduced).  Up to 10 inputs two outputs are interleaved (unroll 2: the reduction of one overlaps the
+// products of the next; the ModUp instance is held to three CTAs per SM for it): 64-rotation step 7,855 -> 7,905
+// ops/s, with larger digits the extra registers spill.
 template <int S, int NC, class TowerOf>
 __device__ __forceinline__ void conv_rows(const uint32_t (&yl)[NC][S], const uint32_t (&yh)[NC][S], const uint2* cs,
                                           int nout, u64* out, size_t stride, const PrimeConst* __restrict__ pc,
                                           TowerOf tower_of) {
-#pragma unroll 1
+#pragma unroll(S <= 10 ? 2 : 1)
   for (int jj = 0; jj < nout; jj++) {
     u64 hi[NC], lo[NC];
 #pragma unroll
@@ -196,7 +198,7 @@ __device__ __forceinline__ void modup_body(const KsJob& J, const Ring& r, const 
 // instance compiles (8, 10, 12, 16 or 32), so the common small digits do not pay for the registers of large ones.  The
 // digit's 30-bit-sliced [Qhat_i]_{m_j} constants are staged in shared memory.
 template <int MAXS>
-__global__ void __launch_bounds__(kT) modup_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
+__global__ void __launch_bounds__(kT, MAXS <= 10 ? 3 : 1) modup_conv_kernel(const __grid_constant__ KsBatch b, Ring r, CrtTables c,
                                                         const PrimeConst* __restrict__ pc) {
   pdl_prologue();
   extern __shared__ uint2 cs[];
