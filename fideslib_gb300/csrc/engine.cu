@@ -590,18 +590,33 @@ cudaError_t Context::modup(const u64* const* a, const int* ts, u64* const* coeff
   return err;
 }
 
-cudaError_t Context::keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s) {
+cudaError_t Context::keyswitch_batch(const KsReq* reqs_in, int n, cudaStream_t s) {
+  const KsReq* reqs = reqs_in;
+  std::vector<KsReq> by_key;
   if (n >= kKsSplit && reqs[0].ext_mode == 0) {  // (the double-hoisted transforms measured faster unsplit)
     // the first half ends at a request boundary that no ModUp group (same a, t, digits) straddles
-    auto same = [&](int i, int k) {
-      return reqs[i].a == reqs[k].a && reqs[i].t == reqs[k].t && reqs[i].digits == reqs[k].digits;
+    auto split_at = [&](const KsReq* r) {
+      auto same = [&](int i, int k) { return r[i].a == r[k].a && r[i].t == r[k].t && r[i].digits == r[k].digits; };
+      int h = n / 2;
+      for (; h < n; h++) {
+        bool straddles = false;
+        for (int i = 0; i < h && !straddles; i++)
+          for (int k = h; k < n && !straddles; k++) straddles = same(i, k);
+        if (!straddles) break;
+      }
+      return h;
     };
-    int h = n / 2;
-    for (; h < n; h++) {
-      bool straddles = false;
-      for (int i = 0; i < h && !straddles; i++)
-        for (int k = h; k < n && !straddles; k++) straddles = same(i, k);
-      if (!straddles) break;
+    // Requests ordered by key first, so that the requests of one key land in one half and its inner products read
+    // the key from HBM once (the launcher groups a half's jobs by key); if that order leaves no clean split (ModUp
+    // groups spread over several keys), the given order is tried.
+    by_key.assign(reqs, reqs + n);
+    std::stable_sort(by_key.begin(), by_key.end(),
+                     [](const KsReq& x, const KsReq& y) { return std::less<const u64*>()(x.key, y.key); });
+    int h = split_at(by_key.data());
+    if (h < n) {
+      reqs = by_key.data();
+    } else {
+      h = split_at(reqs);
     }
     if (h < n) {
       cudaError_t err = cudaSuccess;
