@@ -265,9 +265,16 @@ __device__ __forceinline__ void inv_radix16_staged(u64 (&x)[16], int gl, const u
 
 // Input side of the fused rescale: the job's one row per poly (coefficients of prime switch_top) switched into
 // this limb's prime on load.
+// The switched value x (+ diff) is below q_top + p; the transform takes inputs below 16p, so the reduction into
+// [0, p) is skipped unless q_top >= 15p (prime sets of very different sizes): the dropped tower's prime is then
+// within 15 times the others', which the moduli of a CKKS chain always are.
 struct SwitchIn {
   u64 diff = 0, half = 0, one_sh = 0, p = 0;
-  __device__ __forceinline__ u64 operator()(u64 x) const { return shoup(x > half ? x + diff : x, 1ull, one_sh, p); }
+  bool reduce = true;
+  __device__ __forceinline__ u64 operator()(u64 x) const {
+    const u64 v = x > half ? x + diff : x;
+    return reduce ? shoup(v, 1ull, one_sh, p) : v;
+  }
 };
 
 __device__ __forceinline__ SwitchIn switch_in(const NttBatch& b, const DeviceTables& T, const NttEpi* e,
@@ -279,6 +286,7 @@ __device__ __forceinline__ SwitchIn switch_in(const NttBatch& b, const DeviceTab
   sw.one_sh = T.pc[L.prime].one_sh;
   sw.diff = sw.p - shoup(om, 1ull, sw.one_sh, sw.p);
   sw.half = om >> 1;
+  sw.reduce = om >= 15 * sw.p;  // 15p < 2^64 for p < 2^60
   return sw;
 }
 
