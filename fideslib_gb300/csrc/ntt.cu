@@ -290,21 +290,23 @@ __device__ __forceinline__ SwitchIn switch_in(const NttBatch& b, const DeviceTab
   return sw;
 }
 
-// Output side of the fused rescale for a thread's 16 contiguous residues x (in [0, 16p)) at n0 .. n0 + 15.
+// Output side of the fused rescale for a thread's 16 contiguous residues x (in [0, 16p)) at n0 .. n0 + 15: out =
+// (x_tower - NTT) * q_l^-1 mod p, fully reduced.
 template <int LOGN>
 __device__ __forceinline__ void epi_store16(const NttEpi* e, const LimbRef& L, int n0, const u64 (&x)[16], u64 p) {
   constexpr int N = 1 << LOGN;
-  const u64 p2 = 2 * p, p4 = 4 * p;
+  const u64 p4 = 4 * p;
   const NttEpiJob& E = e->jobs[L.job];
   const ulonglong2 w = E.w[L.row];
   const u64* xr = E.x + ((size_t)L.poly * E.x_ps + L.row) * N + n0;
   ulonglong2* orow = reinterpret_cast<ulonglong2*>(E.out + ((size_t)L.poly * E.out_ps + L.row) * N + n0);
 #pragma unroll
   for (int k = 0; k < 16; k += 2) {
+    // y in [0, 4p) after two compare-and-subtracts, x in [0, p): x + 4p - y in (0, 5p), reduced by the Shoup product
     const ulonglong2 xv = *reinterpret_cast<const ulonglong2*>(xr + k);
-    const u64 y0 = csub(csub(csub(csub(x[k], 2 * p4), p4), p2), p);
-    const u64 y1 = csub(csub(csub(csub(x[k + 1], 2 * p4), p4), p2), p);
-    orow[k / 2] = make_ulonglong2(shoup(sub_mod(xv.x, y0, p), w.x, w.y, p), shoup(sub_mod(xv.y, y1, p), w.x, w.y, p));
+    const u64 y0 = csub(csub(x[k], 2 * p4), p4);
+    const u64 y1 = csub(csub(x[k + 1], 2 * p4), p4);
+    orow[k / 2] = make_ulonglong2(shoup(xv.x + p4 - y0, w.x, w.y, p), shoup(xv.y + p4 - y1, w.x, w.y, p));
   }
 }
 
