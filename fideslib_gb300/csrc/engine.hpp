@@ -111,9 +111,9 @@ class Context {
     int ext_mode = 0;
   };
   // All requests in one pipeline: requests with the same (a, t) share one ModUp (hoisting).  Batches of at least
-  // kKsSplit ordinary requests run as two halves on `s` and a side stream, so that the integer-bound transforms
-  // and conversions of one half overlap the memory-bound inner products and epilogues of the other (64 rotations
-  // at ragged levels: +0.9%; 64 products at N=2^13: +4.6%).
+  // kKsSplit ordinary requests run as two halves on `s` and a side stream (64 rotations at ragged levels: +0.9%; 64
+  // products at N=2^13: +4.6%), the requests ordered by key first so that each key's inner products fall in one
+  // half and read the key once.
   cudaError_t keyswitch_batch(const KsReq* reqs, int n, cudaStream_t s);
   static constexpr int kKsSplit = 32;
   // ModDown of `polys` polys of x ([polys][t+np][N], extended basis, evaluation form) into out ([polys][t][N]).

@@ -105,7 +105,7 @@ struct fides_server {
     return limbs * S;
   }
 
-  // Worker loop: admit -> launch (up to max_inflight batches queued) -> retire completed batches.
+  // Worker loop: admit -> launch (up to max_inflight batches in flight, one per lane) -> retire completed batches.
   void run() {
     cudaSetDevice(device);  // a new thread starts on device 0; the contexts live on the creator's device
     // Batches run on the server's own lanes.  Work the caller queued on a context before the server started
