@@ -56,3 +56,29 @@ def test_fused_rescale_every_variant(engine_lib, logN):
         h3 = ctx.load_ciphertext(np.ascontiguousarray(cts[1][:, :3]), 2.0 ** 45)
         assert np.array_equal(ctx.store_ciphertext(ctx.rescale(h3)), want_rs3), (logN, v, "rescale at 3 towers")
     ctx.close()
+
+
+@pytest.mark.parametrize("logN", [13, 16])
+def test_fused_rescale_mixed_prime_sizes(engine_lib, logN):
+    """A chain whose base prime is far smaller than the others (40 against 58 bits): rescaling drops a 58-bit tower,
+    which enters the 40-bit tower's transform through the full reduction (q_top >= 15 q_0) and the other towers'
+    unreduced; both, and a rescale down to the base prime, equal the oracle on every forward variant, with the
+    largest residues in the first coefficients."""
+    import fideslib_gb300 as F
+    N = 1 << logN
+    mods = O.make_moduli(logN, [40] + [58] * (NQ - 1), [60] * NP)
+    assert max(mods[1:NQ]) >= 15 * mods[0]
+    ctx = F.CryptoContext(logN, mods, NP, DNUM)
+    orc = O.Ctx(N, NQ, NP, DNUM, mods, threads=16)
+    ct = np.stack([orc.uniform(71, NQ), orc.uniform(72, NQ)])
+    for j in range(NQ):
+        ct[:, j, :5] = np.uint64(mods[j] - 1)
+    want = orc.rescale(ct)
+    want2 = orc.rescale(np.ascontiguousarray(ct[:, :2]))
+    for v in (0, 1, 2):
+        ctx.set_ntt_variant(v, 0)
+        h = ctx.load_ciphertext(ct, 2.0 ** 58)
+        assert np.array_equal(ctx.store_ciphertext(ctx.rescale(h)), want), (logN, v)
+        h2 = ctx.load_ciphertext(np.ascontiguousarray(ct[:, :2]), 2.0 ** 58)
+        assert np.array_equal(ctx.store_ciphertext(ctx.rescale(h2)), want2), (logN, v, "to the base prime")
+    ctx.close()
