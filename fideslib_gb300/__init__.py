@@ -591,9 +591,9 @@ class CryptoContext:
     def ks_tuning(self) -> dict:
         """The key inner product's tile the autotuner chose (coefficient pairs per thread) and its timings."""
         it = C.c_int32()
-        ms = (C.c_float * 4)()
+        ms = (C.c_float * 5)()
         _check(lib().fides_ctx_ks_tuning(self._h, C.byref(it), ms))
-        return {"pairs_per_thread": it.value, "ms_1_2_4_8": [round(ms[i], 4) for i in range(4)]}
+        return {"pairs_per_thread": it.value, "ms_1_2_4_8_16": [round(ms[i], 4) for i in range(5)]}
 
     def set_ks_tile(self, pairs_per_thread: int):
         _check(lib().fides_ctx_ks_tuning_set(self._h, pairs_per_thread))

@@ -119,8 +119,8 @@ int fides_ctx_ks_tuning(fides_ctx* ctx, int32_t* iters, float* ms) {
 
 int fides_ctx_ks_tuning_set(fides_ctx* ctx, int32_t iters) {
   if (!valid_ctx(ctx)) return fail(FIDES_EINVAL, "null context");
-  if ((iters != 1 && iters != 2 && iters != 4 && iters != 8) || iters > ctx->c->N / 512)
-    return fail(FIDES_EINVAL, "coefficient pairs per thread must be 1, 2, 4 or 8 and at most N / 512");
+  if ((iters != 1 && iters != 2 && iters != 4 && iters != 8 && iters != 16) || iters > ctx->c->N / 512)
+    return fail(FIDES_EINVAL, "coefficient pairs per thread must be 1, 2, 4, 8 or 16 and at most N / 512");
   cudaStreamSynchronize(ctx->c->stream);
   ctx->c->crt.ks_iters = iters;
   ctx->c->ks_tuned = true;  // no later tuning overrides the caller's choice

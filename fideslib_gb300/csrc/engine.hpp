@@ -79,11 +79,11 @@ class Context {
 
   DeviceTables tabs{};
   float ntt_tune_ms[kNttSizeClasses * (kNttFwdVariants + kNttInvVariants)] = {};  // tune_ntt timings
-  // Key inner product tile (coefficient pairs per thread: 1, 2, 4 or 8), tuned on the context's first key-switch
-  // launch of at least kKsTuneJobs jobs; until then (and where a tile does not apply) ks_tune_ms holds -1.
-  static constexpr int kKsTileVariants = 4;
+  // Key inner product tile (coefficient pairs per thread: 1, 2, 4, 8 or 16), tuned on the context's first
+  // key-switch launch of at least kKsTuneJobs jobs; until then (and where a tile does not apply) ks_tune_ms holds -1.
+  static constexpr int kKsTileVariants = 5;
   static constexpr int kKsTuneJobs = 16;
-  float ks_tune_ms[kKsTileVariants] = {-1.f, -1.f, -1.f, -1.f};
+  float ks_tune_ms[kKsTileVariants] = {-1.f, -1.f, -1.f, -1.f, -1.f};
   bool ks_tuned = false;  // also set by fides_ctx_ks_tuning_set
   CrtTables crt{};
   PrimeConst* d_pc = nullptr;

@@ -129,10 +129,10 @@ int fides_ctx_set_input_check(fides_ctx* ctx, int enable);
 /* Overrides the autotuner's choices for every batch size (all variants give identical residues). */
 int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant, int32_t inv_variant);
 /* The key inner product's tile (no counterpart in the reference, whose fusedDotKSK_2_ launch shape is fixed,
- * src/CKKS/LimbPartitionMGPU.cu:444): the coefficient pairs each thread takes (1, 2, 4 or 8, at most N / 512).
+ * src/CKKS/LimbPartitionMGPU.cu:444): the coefficient pairs each thread takes (1, 2, 4, 8 or 16, at most N / 512).
  * The context's first key-switch launch of at least 16 ciphertexts runs its inner products once per tile, timed
  * with CUDA events (one synchronisation), and keeps the fastest.  iters = the tile in use (4 before that launch),
- * ms[0..3] = the timings of 1, 2, 4 and 8 (-1 before the tuning or where a tile does not apply).
+ * ms[0..4] = the timings of 1, 2, 4, 8 and 16 (-1 before the tuning or where a tile does not apply).
  * fides_ctx_ks_tuning_set sets the tile and turns the tuning off (every tile gives identical residues). */
 int fides_ctx_ks_tuning(fides_ctx* ctx, int32_t* iters, float* ms);
 int fides_ctx_ks_tuning_set(fides_ctx* ctx, int32_t iters);

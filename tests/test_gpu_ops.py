@@ -298,11 +298,11 @@ def test_every_inner_product_tile_bit_exact(env):
 
     check("first batch")  # 16 jobs: tunes the tile if no earlier batch did
     tun = env.gpu.ks_tuning()
-    allowed = [i for i in (1, 2, 4, 8) if i <= env.N // 512]
+    allowed = [i for i in (1, 2, 4, 8, 16) if i <= env.N // 512]
     assert tun["pairs_per_thread"] in allowed, tun
-    assert all(tun["ms_1_2_4_8"][k] > 0 for k, i in enumerate((1, 2, 4, 8)) if i in allowed), tun
+    assert all(tun["ms_1_2_4_8_16"][k] > 0 for k, i in enumerate((1, 2, 4, 8, 16)) if i in allowed), tun
     try:
-        for iters in (1, 2, 4, 8):
+        for iters in (1, 2, 4, 8, 16):
             if iters not in allowed:
                 with pytest.raises(F.FidesError):
                     env.gpu.set_ks_tile(iters)
