@@ -155,7 +155,7 @@ int fides_ctx_ntt_tuning_set(fides_ctx* ctx, int32_t fwd_variant, int32_t inv_va
   cudaStreamSynchronize(ctx->c->stream);
   fgb::DeviceTables& t = ctx->c->tabs;
   t.fwd_variant = t.fwd_variant_small = t.fwd_variant_tiny = fwd_variant;
-  t.inv_variant = t.inv_variant_small = t.inv_variant_tiny = inv_variant;
+  t.inv_variant = t.inv_variant_small = t.inv_variant_tiny = t.inv_variant_ks = inv_variant;
   return FIDES_OK;
 }
 

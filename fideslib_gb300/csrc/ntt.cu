@@ -68,24 +68,97 @@ __device__ __forceinline__ void ct_bfly(u64& X, u64& Y, const ulonglong2& w, u64
   Y = x - t + p4;
 }
 
-// Inverse (GS): X, Y in [0, 4p) -> X + Y (reduced below 4p), (X - Y + 4p) w in [0, 4p).
-__device__ __forceinline__ void gs_bfly(u64& X, u64& Y, const ulonglong2& w, u64 negp, u64 p4) {
-  u64 s = X + Y;
-  s = s >= p4 ? s - p4 : s;
-  const u64 d = X - Y + p4;
-  X = s;
-  Y = shoup_lazy4(d, w.x, w.y, negp);
+// Inverse (GS): X, Y -> X + Y, (X - Y + b_Y p) w, where b_Y p bounds Y.  The product is in [0, 4p) whatever its
+// input, so only the sums grow.  Every residue of a pass carries a bound b p (b a power of two) that its position
+// fixes at compile time (GsPlan): a compare-and-subtract (b p -> b p / 2) is spent only where a sum could reach 16p
+// (< 2^64 for p < 2^60) and where the pass hands its residues on (bound 8p between passes; the transform's input is
+// below 4p).  That is about 0.53 compare-and-subtracts per butterfly instead of one.
+template <int R>
+struct GsPlan {
+  unsigned char bx[R][1 << R], by[R][1 << R];  // bounds of X (at k) and Y (at k + 2^kb) before stage kb's butterfly
+  unsigned char hx[R][1 << R], hy[R][1 << R];  // halvings applied to each before it
+  unsigned char bend[1 << R], hend[1 << R];    // bound at the end of the pass and the halvings that meet ENDB
+};
+
+// FINAL: the pass ends the transform; its last stage is the N^-1-scaled one (both outputs are products, < 4p).
+// lim: the largest sum allowed (16p; 8p keeps every offset and subtrahend at 4p, one 64-bit constant fewer for a
+// pass whose registers are at the limit).
+template <int R>
+__host__ __device__ constexpr GsPlan<R> gs_plan(int b0, int endb, bool final_pass, int lim = 16) {
+  GsPlan<R> P{};
+  int b[1 << R] = {};
+  for (int k = 0; k < (1 << R); k++) b[k] = b0;
+  for (int kb = 0; kb < R; kb++)
+    for (int k = 0; k < (1 << R); k++) {
+      if (k & (1 << kb)) continue;
+      const int j = k + (1 << kb);
+      P.bx[kb][k] = (unsigned char)b[k];
+      P.by[kb][k] = (unsigned char)b[j];
+      int hx = 0, hy = 0;
+      while (b[k] + b[j] > lim) {
+        if (b[k] >= b[j]) {
+          b[k] /= 2;
+          hx++;
+        } else {
+          b[j] /= 2;
+          hy++;
+        }
+      }
+      P.hx[kb][k] = (unsigned char)hx;
+      P.hy[kb][k] = (unsigned char)hy;
+      b[k] = (final_pass && kb == R - 1) ? 4 : b[k] + b[j];
+      b[j] = 4;
+    }
+  for (int k = 0; k < (1 << R); k++) {
+    P.bend[k] = (unsigned char)b[k];
+    int h = 0;
+    while (endb > 0 && b[k] > endb) {
+      b[k] /= 2;
+      h++;
+    }
+    P.hend[k] = (unsigned char)h;
+  }
+  return P;
 }
 
-// The inverse's last stage (s = 0, one twiddle w1 = psi^-brev(1)) with N^-1 folded in: X, Y in [0, 4p) ->
-// (X + Y) N^-1, (X - Y + 4p) w1 N^-1, both in [0, 4p).  Saves the separate scaling of every output by N^-1.
+// v < b p -> the same residue below (b >> h) p, by h compare-and-subtracts (b, h compile-time after unrolling).
+__device__ __forceinline__ u64 gs_reduce(u64 v, int b, int h, u64 p) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    if (i < h) {
+      b >>= 1;
+      v = csub(v, p * (u64)b);
+    }
+  return v;
+}
+
+// The inverse's last stage (s = 0, one twiddle w1 = psi^-brev(1)) with N^-1 folded in: (X + Y) N^-1,
+// (X - Y + b_Y p) w1 N^-1, both in [0, 4p).  Saves the separate scaling of every output by N^-1.
 struct LastStage {
   u64 ninv, ninv_sh, w1ninv, w1ninv_sh;
 };
-__device__ __forceinline__ void gs_bfly_last(u64& X, u64& Y, const LastStage& c, u64 negp, u64 p4) {
-  const u64 s = X + Y, d = X - Y + p4;
-  X = shoup_lazy4(s, c.ninv, c.ninv_sh, negp);
-  Y = shoup_lazy4(d, c.w1ninv, c.w1ninv_sh, negp);
+
+// Butterfly of pair (k, k + 2^kb) at stage kb of a pass planned by P; last != null: the N^-1-scaled final stage.
+template <int R>
+__device__ __forceinline__ void gs_bfly(u64 (&x)[1 << R], const GsPlan<R>& P, int kb, int k, const ulonglong2& w,
+                                        u64 p, u64 negp, const LastStage* last = nullptr) {
+  const int j = k + (1 << kb);
+  const u64 X = gs_reduce(x[k], P.bx[kb][k], P.hx[kb][k], p);
+  const u64 Y = gs_reduce(x[j], P.by[kb][k], P.hy[kb][k], p);
+  const u64 d = X - Y + p * (u64)(P.by[kb][k] >> P.hy[kb][k]);
+  if (last) {
+    x[k] = shoup_lazy4(X + Y, last->ninv, last->ninv_sh, negp);
+    x[j] = shoup_lazy4(d, last->w1ninv, last->w1ninv_sh, negp);
+  } else {
+    x[k] = X + Y;
+    x[j] = shoup_lazy4(d, w.x, w.y, negp);
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void gs_end(u64 (&x)[1 << R], const GsPlan<R>& P, u64 p) {
+#pragma unroll
+  for (int k = 0; k < (1 << R); k++) x[k] = gs_reduce(x[k], P.bend[k], P.hend[k], p);
 }
 
 // Radix-2^LOGR stages over x[k] = a[G*2^(LOGS+LOGR) + k*2^LOGS + low] (low < 2^LOGS).  At the sub-stage on
@@ -121,17 +194,21 @@ __device__ __forceinline__ void fwd_radix(u64 (&x)[1 << LOGR], int G, const ulon
   }
 }
 
-// last != null: these stages end the transform (their final stage is s = 0), which then applies N^-1 (LastStage).
-template <int LOGR, int LOGS, int LOGN>
+// Inverse stages of a pass (LOGS = 0: the transform's first pass, input below 4p; otherwise below 8p).  A pass whose
+// stages reach s = 0 ends the transform and takes last (N^-1, LastStage); its outputs are below 4p, every other
+// pass's below 8p.  LIM: gs_plan's lim.
+template <int LOGR, int LOGS, int LOGN, int LIM = 16>
 __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulonglong2* __restrict__ tw, u64 negp,
-                                          u64 p4, const LastStage* last = nullptr) {
+                                          u64 p, const LastStage* last = nullptr) {
+  constexpr bool kFinal = LOGS + LOGR == LOGN;
+  constexpr GsPlan<LOGR> P = gs_plan<LOGR>(LOGS == 0 ? 4 : 8, kFinal ? 0 : 8, kFinal, LIM);
   if constexpr (LOGS == 0) {
     // The inverse's first pass (16 contiguous residues per thread, each thread's 15 twiddles its own and read from
     // L2): all 15 twiddle loads are issued before the first butterfly, so their latencies overlap instead of
     // adding up stage by stage (640-limb inverse 0.5325 -> 0.5192 ms; the same in the forward's last pass, whose
     // inputs come from shared memory, measured 0.4465 -> 0.4526 ms and is not done).  s >= LOGN - 4 > 0 here, so
     // the last-stage scaling never applies.
-    static_assert(LOGR == 4, "the first pass of the inverse works on 16-residue groups");
+    static_assert(LOGR == 4 && !kFinal, "the first pass of the inverse works on 16-residue groups");
     ulonglong2 wv[15];  // stage kb's twiddles start at 16 - (16 >> kb): 8, 4, 2 and 1 of them
 #pragma unroll
     for (int kb = 0, q = 0; kb < LOGR; kb++)
@@ -142,9 +219,10 @@ __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulon
 #pragma unroll
       for (int k = 0; k < (1 << LOGR); k++) {
         if (k & (1 << kb)) continue;
-        gs_bfly(x[k], x[k + (1 << kb)], wv[16 - (16 >> kb) + (k >> (kb + 1))], negp, p4);
+        gs_bfly<LOGR>(x, P, kb, k, wv[16 - (16 >> kb) + (k >> (kb + 1))], p, negp);
       }
     }
+    gs_end<LOGR>(x, P, p);
     return;
   }
 #pragma unroll
@@ -153,14 +231,15 @@ __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulon
 #pragma unroll
     for (int k = 0; k < (1 << LOGR); k++) {
       if (k & (1 << kb)) continue;
-      if (s == 0 && last) {
-        gs_bfly_last(x[k], x[k + (1 << kb)], *last, negp, p4);
+      if (s == 0) {
+        gs_bfly<LOGR>(x, P, kb, k, ulonglong2{}, p, negp, last);
       } else {
         const ulonglong2 w = __ldg(tw_entry<LOGR, LOGS, LOGN>(tw, s, kb, G, k >> (kb + 1)));
-        gs_bfly(x[k], x[k + (1 << kb)], w, negp, p4);
+        gs_bfly<LOGR>(x, P, kb, k, w, p, negp);
       }
     }
   }
+  if constexpr (!kFinal) gs_end<LOGR>(x, P, p);
 }
 
 struct LimbRef {
@@ -250,16 +329,19 @@ __device__ __forceinline__ void fwd_radix16_staged(u64 (&x)[16], int gl, const u
 }
 template <int LOGS, int LOGN>
 __device__ __forceinline__ void inv_radix16_staged(u64 (&x)[16], int gl, const ulonglong2* tws, int n, u64 negp,
-                                                   u64 p4) {
+                                                   u64 p) {
+  static_assert(LOGS > 0 && LOGS + 4 < LOGN, "a staged pass neither starts nor ends the inverse");
+  constexpr GsPlan<4> P = gs_plan<4>(8, 8, false);
 #pragma unroll
   for (int kb = 0; kb < 4; kb++) {
     const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
 #pragma unroll
     for (int k = 0; k < 16; k++) {
       if (k & (1 << kb)) continue;
-      gs_bfly(x[k], x[k + (1 << kb)], blk[k >> (kb + 1)], negp, p4);
+      gs_bfly<4>(x, P, kb, k, blk[k >> (kb + 1)], p, negp);
     }
   }
+  gs_end<4>(x, P, p);
 }
 
 
@@ -464,7 +546,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
       x[k] = v.x;
       x[k + 1] = v.y;
     }
-    inv_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p4);
+    inv_radix<4, 0, LOGN>(x, h * (S::E / 16) + g, tw, negp, p);
 #pragma unroll
     for (int k = 0; k < 16; k += 2) *reinterpret_cast<ulonglong2*>(sm + swz(g * 16 + k)) = make_ulonglong2(x[k], x[k + 1]);
   }
@@ -477,7 +559,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    inv_radix16_staged<4, LOGN>(x, high, tws, S::NB, negp, p4);
+    inv_radix16_staged<4, LOGN>(x, high, tws, S::NB, negp, p);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -485,6 +567,9 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
 
   {  // pass A^-1
     constexpr int R = 1 << S::LOGRA;
+    // gs_plan's lim for this radix-32 pass: 8 keeps one 64-bit constant out of the registers (128 a thread, 20 bytes
+    // of spills with 16); 640 limbs at N = 2^16 take 0.494 ms against 0.507-0.522 ms with 16.
+    constexpr int kLim = 8;
     u64 x[R];
 #pragma unroll
     for (int k = 0; k < R; k++) {
@@ -493,7 +578,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
     }
     if constexpr (S::C == 1) {  // this pass ends the transform
       const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
-      inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4, &last);
+      inv_radix<S::LOGRA, 8, LOGN, kLim>(x, h, tw, negp, p, &last);
 #pragma unroll
       for (int k = 0; k < R; k++) {
         const int l = k * 256 + tid;
@@ -501,7 +586,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
       }
       return;
     } else {
-      inv_radix<S::LOGRA, 8, LOGN>(x, h, tw, negp, p4);
+      inv_radix<S::LOGRA, 8, LOGN, kLim>(x, h, tw, negp, p);
 #pragma unroll
       for (int k = 0; k < R; k++) sm[swz(k * 256 + tid)] = x[k];
     }
@@ -520,7 +605,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
 #pragma unroll
       for (int hh = 0; hh < S::C; hh++) x[hh] = ld_peer(peer_smem(sm + swz(l), hh));
       const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
-      inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, negp, p4, &last);
+      inv_radix<S::LOGC, S::LOGE, LOGN>(x, 0, tw, negp, p, &last);
 #pragma unroll
       for (int hh = 0; hh < S::C; hh++) L.dst[hh * S::E + l] = LAZY ? x[hh] : csub(csub(x[hh], p2), p);
     }
@@ -707,7 +792,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
       x[k] = v.x;
       x[k + 1] = v.y;
     }
-    inv_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p4);
+    inv_radix<4, 0, LOGN>(x, h * S::GROUPS + g, tw, negp, p);
 #pragma unroll
     for (int k = 0; k < 16; k += 2) *reinterpret_cast<ulonglong2*>(sm + swz(g * 16 + k)) = make_ulonglong2(x[k], x[k + 1]);
   }
@@ -719,7 +804,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(high * 256 + k * 16 + low)];
-    inv_radix16_staged<4, LOGN>(x, high, tws + 15 * S::NA, S::NB, negp, p4);
+    inv_radix16_staged<4, LOGN>(x, high, tws + 15 * S::NA, S::NB, negp, p);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(high * 256 + k * 16 + low)] = x[k];
   }
@@ -730,7 +815,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
     u64 x[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) x[k] = sm[swz(hi * 4096 + k * 256 + low)];
-    inv_radix16_staged<8, LOGN>(x, hi, tws, S::NA, negp, p4);
+    inv_radix16_staged<8, LOGN>(x, hi, tws, S::NA, negp, p);
 #pragma unroll
     for (int k = 0; k < 16; k++) sm[swz(hi * 4096 + k * 256 + low)] = x[k];
   }
@@ -753,7 +838,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
         for (int k = 0; k < R; k++) x[k] = sm[swz(k * 4096 + col)];
       }
       const LastStage last{pc.ninv, pc.ninv_sh, pc.w1ninv, pc.w1ninv_sh};
-      inv_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p4, &last);
+      inv_radix<S::LOGX, 12, LOGN>(x, 0, tw, negp, p, &last);
 #pragma unroll
       for (int k = 0; k < R; k++) L.dst[k * 4096 + col] = LAZY ? x[k] : csub(csub(x[k], p2), p);
     }
@@ -904,7 +989,10 @@ cudaError_t launch_ntt(const NttBatch& b, const DeviceTables& t, bool inverse, c
   if (b.njobs > kMaxNttJobs || b.limb_begin[b.njobs] > 65535) return cudaErrorInvalidValue;
   const long long work = (long long)b.limb_begin[b.njobs] << t.logN;
   const int cls = work <= kTinyNttWork ? 0 : work <= kSmallNttWork ? 1 : 2;
-  const int v = inverse ? (cls == 0 ? t.inv_variant_tiny : cls == 1 ? t.inv_variant_small : t.inv_variant)
+  const int v = inverse ? (cls == 0   ? t.inv_variant_tiny
+                           : cls == 1 ? t.inv_variant_small
+                           : b.lazy_out ? t.inv_variant_ks
+                                        : t.inv_variant)
                         : (cls == 0 ? t.fwd_variant_tiny : cls == 1 ? t.fwd_variant_small : t.fwd_variant);
   switch (t.logN) {
     case 10: return launch_t<10>(b, t, inverse, s);
@@ -983,7 +1071,7 @@ cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
       NttBatch b{};
       uint8_t pm[1] = {0};
       ntt_add_job(b, buf, buf, (long long)n, (long long)n, 1, sizes[size], pm);
-      float best = 0;
+      float best = 0, el_v[kNttInvVariants > kNttFwdVariants ? kNttInvVariants : kNttFwdVariants] = {};
       int pick = 0;
       for (int v = 0; v < nv && e == cudaSuccess; v++, slot++) {
         DeviceTables tv = t;
@@ -997,6 +1085,7 @@ cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
         float el = 0;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&el, ev[0], ev[1]);
         el /= 3;
+        el_v[v] = el;
         if (ms) ms[slot] = el;
         if (v == 0 || el < best) {
           best = el;
@@ -1007,6 +1096,8 @@ cudaError_t tune_ntt(DeviceTables& t, cudaStream_t s, float* ms) {
         int* dst[2][kNttSizeClasses] = {{&t.fwd_variant_tiny, &t.fwd_variant_small, &t.fwd_variant},
                                         {&t.inv_variant_tiny, &t.inv_variant_small, &t.inv_variant}};
         *dst[inverse][size] = pick;
+        if (inverse && size == kNttSizeClasses - 1)  // the faster radix-16 variant (3 CTAs per SM)
+          t.inv_variant_ks = el_v[1] <= el_v[2] ? 1 : 2;
       }
     }
   }

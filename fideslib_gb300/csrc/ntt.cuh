@@ -68,6 +68,11 @@ struct DeviceTables {
   int inv_variant = 0;  // inverse: 0 = radix-32/16, 1 = radix-16 with 4096, 2 = with 8192 residues per CTA
   int inv_variant_small = 0;
   int inv_variant_tiny = 0;
+  // The key switch's large inverse launches (lazy outputs), whose two halves run on two streams beside the other
+  // half's conversions and inner products: the faster of the radix-16 variants (1, 2; 80 registers a thread, three
+  // CTAs per SM), which share the SMs better than the radix-32/16 kernel (128 registers, two CTAs per SM).  At
+  // N = 2^16, 64 batched rotations run 1.1% faster with it although the radix-32/16 kernel is 1.6% faster alone.
+  int inv_variant_ks = 0;
 };
 constexpr int kNttFwdVariants = 3;
 constexpr int kNttInvVariants = 3;

@@ -112,7 +112,9 @@ int fides_ctx_set_stream(fides_ctx* ctx, void* stream);
  * with 8192 residues per CTA, 1 = radix-32/16 passes, 2 = radix-16 passes with 4096 residues per CTA (twice the
  * CTAs per limb); inverse: 0 = radix-32/16, 1 = radix-16 with 4096 per CTA, 2 = radix-16 with 8192 per CTA.
  * ms[0..17] = forward tiny v0..v2, small v0..v2, large v0..v2, then the inverse the same way (-1 where a single
- * kernel applies, N < 2^13). */
+ * kernel applies, N < 2^13).  The key switch's inverse launches of the large class run beside the other half of
+ * their batch on a second stream and use the faster of inverse variants 1 and 2 (ms[16], ms[17]), whose CTAs share
+ * an SM three at a time; fides_ctx_ntt_tuning_set fixes them too. */
 int fides_ctx_ntt_tuning(fides_ctx* ctx, int32_t* variant, float* ms);
 /* Device-memory budget of the context (the reference's pool has a release threshold only, Context.cu:74-80):
  * ciphertexts and per-op workspaces come from the stream-ordered pool and are counted; an op whose allocation

@@ -116,3 +116,28 @@ def test_forward_ntt_accepts_lazy_inputs(engine_lib, logN):
     for v in ((0, 1, 2) if logN >= 13 else (1,)):
         ctx.set_ntt_variant(v, 0)
         assert np.array_equal(ctx.ntt_host(lazy.copy(), 0, inverse=False), ctx.ntt_host(x.copy(), 0, inverse=False))
+
+
+@pytest.mark.parametrize("logN", [10, 12, 13, 14, 16])
+def test_inverse_ntt_accepts_lazy_inputs(engine_lib, logN):
+    """The inverse takes residues in [0, 4p) (the key inner product's and other kernels' lazy outputs): the
+    transform of x + k p, k < 4, equals the transform of x for every kernel variant, also with every residue at
+    the top of the range (4p - 1), where the per-position bounds of the lazy butterflies are tightest."""
+    N = 1 << logN
+    ctx, mods = make_ctx(logN, 2, bits=60)
+    rng = np.random.default_rng(logN + 11)
+    x = np.stack([rng.integers(0, mods[j], N, dtype=np.uint64) for j in range(2)])[None]
+    lazy = x.copy()
+    for j in range(2):
+        lazy[0, j] = x[0, j] + rng.integers(0, 4, N, dtype=np.uint64) * np.uint64(mods[j])
+    top = np.stack([np.full(N, 4 * mods[j] - 1, dtype=np.uint64) for j in range(2)])[None]
+    top_red = np.stack([np.full(N, mods[j] - 1, dtype=np.uint64) for j in range(2)])[None]
+    for v in ((0, 1, 2) if logN >= 13 else (0,)):
+        ctx.set_ntt_variant(1 if logN < 13 else 0, v)
+        ref = ctx.ntt_host(x.copy(), 0, inverse=True)
+        for j in range(2):
+            _, itab = O.ntt_tables(N, mods[j], ctx.roots[j])
+            assert np.array_equal(ref[0, j], O.ntt_inv(x[0, j], mods[j], itab)), (logN, v, j)
+        assert np.array_equal(ctx.ntt_host(lazy.copy(), 0, inverse=True), ref), (logN, v)
+        assert np.array_equal(ctx.ntt_host(top.copy(), 0, inverse=True),
+                              ctx.ntt_host(top_red.copy(), 0, inverse=True)), (logN, v)
