@@ -16,8 +16,8 @@
 // For N = 2^13 .. 2^16 the forward transform uses a radix-16 variant of the same cluster layout (ntt16_fwd_kernel
 // below: four radix-16 passes, 16 residues per thread, three CTAs per SM).
 // Butterflies are Harvey-lazy with a cheaper quotient estimate (shoup_lazy4, products in [0, 4p)): forward
-// values live in [0, 16p) (the compare-and-subtract on every other stage), inverse in [0, 4p); outputs are reduced
-// to [0, p).  Needs p < 2^60.  Shared memory is
+// values live in [0, 16p) (the compare-and-subtract on every other stage), inverse values below 16p with a
+// compile-time bound per position (GsPlan); outputs are reduced to [0, p).  Needs p < 2^60.  Shared memory is
 // XOR-swizzled on bits 1..3 (word l stored at l ^ (((l >> 4) & 7) << 1)): the passes that hold 16 residues at a
 // stride (X, A, B) access 64-bit words of distinct banks in every half-warp, and the last pass, whose thread holds
 // 16 contiguous residues, moves them as eight 16-byte pairs (the swizzle keeps pairs adjacent and aligned) with
