@@ -78,6 +78,7 @@ struct GsPlan {
   unsigned char bx[R][1 << R], by[R][1 << R];  // bounds of X (at k) and Y (at k + 2^kb) before stage kb's butterfly
   unsigned char hx[R][1 << R], hy[R][1 << R];  // halvings applied to each before it
   unsigned char bend[1 << R], hend[1 << R];    // bound at the end of the pass and the halvings that meet ENDB
+  bool ok;                                     // every halving count within gs_reduce's three
 };
 
 // FINAL: the pass ends the transform; its last stage is the N^-1-scaled one (both outputs are products, < 4p).
@@ -86,6 +87,7 @@ struct GsPlan {
 template <int R>
 __host__ __device__ constexpr GsPlan<R> gs_plan(int b0, int endb, bool final_pass, int lim = 16) {
   GsPlan<R> P{};
+  P.ok = true;
   int b[1 << R] = {};
   for (int k = 0; k < (1 << R); k++) b[k] = b0;
   for (int kb = 0; kb < R; kb++)
@@ -106,6 +108,7 @@ __host__ __device__ constexpr GsPlan<R> gs_plan(int b0, int endb, bool final_pas
       }
       P.hx[kb][k] = (unsigned char)hx;
       P.hy[kb][k] = (unsigned char)hy;
+      P.ok = P.ok && hx <= 3 && hy <= 3;
       b[k] = (final_pass && kb == R - 1) ? 4 : b[k] + b[j];
       b[j] = 4;
     }
@@ -117,6 +120,7 @@ __host__ __device__ constexpr GsPlan<R> gs_plan(int b0, int endb, bool final_pas
       h++;
     }
     P.hend[k] = (unsigned char)h;
+    P.ok = P.ok && h <= 3;
   }
   return P;
 }
@@ -202,6 +206,7 @@ __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulon
                                           u64 p, const LastStage* last = nullptr) {
   constexpr bool kFinal = LOGS + LOGR == LOGN;
   constexpr GsPlan<LOGR> P = gs_plan<LOGR>(LOGS == 0 ? 4 : 8, kFinal ? 0 : 8, kFinal, LIM);
+  static_assert(P.ok, "a residue needs more halvings than gs_reduce applies");
   if constexpr (LOGS == 0) {
     // The inverse's first pass (16 contiguous residues per thread, each thread's 15 twiddles its own and read from
     // L2): all 15 twiddle loads are issued before the first butterfly, so their latencies overlap instead of
@@ -223,23 +228,23 @@ __device__ __forceinline__ void inv_radix(u64 (&x)[1 << LOGR], int G, const ulon
       }
     }
     gs_end<LOGR>(x, P, p);
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int kb = 0; kb < LOGR; kb++) {
-    const int s = LOGN - 1 - (LOGS + kb);
+    for (int kb = 0; kb < LOGR; kb++) {
+      const int s = LOGN - 1 - (LOGS + kb);
 #pragma unroll
-    for (int k = 0; k < (1 << LOGR); k++) {
-      if (k & (1 << kb)) continue;
-      if (s == 0) {
-        gs_bfly<LOGR>(x, P, kb, k, ulonglong2{}, p, negp, last);
-      } else {
-        const ulonglong2 w = __ldg(tw_entry<LOGR, LOGS, LOGN>(tw, s, kb, G, k >> (kb + 1)));
-        gs_bfly<LOGR>(x, P, kb, k, w, p, negp);
+      for (int k = 0; k < (1 << LOGR); k++) {
+        if (k & (1 << kb)) continue;
+        if (s == 0) {
+          gs_bfly<LOGR>(x, P, kb, k, ulonglong2{}, p, negp, last);
+        } else {
+          const ulonglong2 w = __ldg(tw_entry<LOGR, LOGS, LOGN>(tw, s, kb, G, k >> (kb + 1)));
+          gs_bfly<LOGR>(x, P, kb, k, w, p, negp);
+        }
       }
     }
+    if constexpr (!kFinal) gs_end<LOGR>(x, P, p);
   }
-  if constexpr (!kFinal) gs_end<LOGR>(x, P, p);
 }
 
 struct LimbRef {
@@ -332,6 +337,7 @@ __device__ __forceinline__ void inv_radix16_staged(u64 (&x)[16], int gl, const u
                                                    u64 p) {
   static_assert(LOGS > 0 && LOGS + 4 < LOGN, "a staged pass neither starts nor ends the inverse");
   constexpr GsPlan<4> P = gs_plan<4>(8, 8, false);
+  static_assert(P.ok, "a residue needs more halvings than gs_reduce applies");
 #pragma unroll
   for (int kb = 0; kb < 4; kb++) {
     const ulonglong2* blk = tws + n * ((8 >> kb) - 1) + gl * (8 >> kb);
@@ -529,7 +535,7 @@ __global__ void __launch_bounds__(kThreads, 2) ntt_inv_kernel(const __grid_const
   const LimbRef L = locate(b, S::N);
   if (!L.valid) return;
   const PrimeConst& pc = T.pc[L.prime];
-  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp;
+  const u64 p = pc.p, p2 = 2 * p, negp = pc.negp;
   const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
@@ -776,7 +782,7 @@ __global__ void __launch_bounds__(kThreads16, 3) ntt16_inv_kernel(const __grid_c
   const LimbRef L = locate(b, S::N);
   if (!L.valid) return;
   const PrimeConst& pc = T.pc[L.prime];
-  const u64 p = pc.p, p2 = 2 * p, p4 = 4 * p, negp = pc.negp;
+  const u64 p = pc.p, p2 = 2 * p, negp = pc.negp;
   const ulonglong2* __restrict__ tw = T.tw_inv + (size_t)L.prime * S::N;
   int h = 0;
   if constexpr (S::C > 1) h = (int)cg::this_cluster().block_rank();
